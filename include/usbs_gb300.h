@@ -1,0 +1,107 @@
+/*
+ * usbs_gb300 — C ABI of the GB300 (sm_103a) USBS hot path.
+ *
+ * Conventions
+ *  - Every pointer argument is a DEVICE pointer unless its comment says
+ *    otherwise; the library never frees or reallocates caller memory.
+ *  - `stream` is a cudaStream_t passed as void* (NULL = legacy default stream).
+ *    Calls are stream-ordered and asynchronous unless stated otherwise.
+ *  - Return value: 0 on success, negative on a host-side error (bad sizes,
+ *    launch failure); usbs_last_error() then holds a thread-local message.
+ *    Numerical/device conditions are reported through the `info`/`status`
+ *    words the caller passes (device memory, read after synchronising).
+ *  - `precision` selects the storage/arithmetic type of the n-sized vectors:
+ *    64 = FP64 throughout (the parity path), 32 = FP32 vectors and dot products
+ *    with FP64 team reductions and FP64 projected eigensolve.
+ *  - Triples: the reference's constraint tensor A is a list of (c, i, j, a)
+ *    (A_indices rows and A_data, utils/maxcut_helpers.py:26-33,
+ *    utils/qap_helpers.py:175-318).  The device keeps them sorted by
+ *    constraint (con_ptr / t_row / t_col / t_a) and by row (row_ptr / r_con /
+ *    r_col / r_a).  The Lanczos operator lives on the union pattern of C and
+ *    the triples' (i, j) positions (rowptr / col); slot_ptr / slot_tid list,
+ *    for every position of that pattern, the triples that land on it.
+ */
+#ifndef USBS_GB300_H
+#define USBS_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define USBS_GB300_ABI_VERSION 1
+
+/* ABI version of the loaded library (USBS_GB300_ABI_VERSION). */
+int usbs_abi_version(void);
+
+/* Last host-side error message of the calling thread ("" if none). */
+const char* usbs_last_error(void);
+
+/* Multiprocessor count and the number of co-resident Lanczos CTAs per SM for
+ * FP64 and FP32 on `device` (host pointers). */
+int usbs_device_info(int device, int* sm_count, int* lanczos_ctas_per_sm64,
+                     int* lanczos_ctas_per_sm32);
+
+/* Lanczos operator values on the union pattern:
+ *   op_val[p] = c_scale * c_val[p] + sum_{q in [slot_ptr[p], slot_ptr[p+1])}
+ *               t_a[slot_tid[q]] * w[t_con[slot_tid[q]]]
+ * i.e. the CSR of c_scale*C + A*(w).  Replaces the per-step
+ * `C @ q + apply_A_adjoint_slim(n, A_data, A_indices, w, q)` of
+ * solver/lanczos.py:86-87 by one assembled matrix per eigsh call.
+ * c_val or w may be NULL (term omitted).  op_val is double (precision 64) or
+ * float (precision 32). */
+int usbs_assemble_operator(long long nnz, const double* c_val, double c_scale,
+                           const int* slot_ptr, const int* slot_tid, const int* t_con,
+                           const double* t_a, const double* w, void* op_val, int precision,
+                           void* stream);
+
+/* y = Op x for the assembled CSR operator (the "C matvec" callback,
+ * solver/lanczos.py:86).  x, y, op_val in the type chosen by `precision`. */
+int usbs_operator_apply(int n, long long nnz, const int* rowptr, const int* col,
+                        const void* op_val, const void* x, void* y, int precision,
+                        void* stream);
+
+/* out[c] = sum_j sum_{t in c} t_a[t] U[t_row[t], j] U[t_col[t], j], c < m:
+ * apply_A_operator_slim (k = 1) / apply_A_operator_batched (k columns),
+ * solver/utils.py:11-16 and 27-31.  U column-major n x k with leading
+ * dimension ldu; out has m doubles. */
+int usbs_apply_A_operator(int m, int k, const int* con_ptr, const int* t_row, const int* t_col,
+                          const double* t_a, const double* U, int ldu, double* out,
+                          void* stream);
+
+/* out[i, q] = sum_{t with row i} r_a[t] z[r_con[t]] U[r_col[t], q], i < n:
+ * apply_A_adjoint_slim (k = 1) / apply_A_adjoint_batched, solver/utils.py:19-24
+ * and 34-37.  U and out column-major (ldu, ldo). */
+int usbs_apply_A_adjoint(int n, int k, const int* row_ptr, const int* r_con, const int* r_col,
+                         const double* r_a, const double* z, const double* U, int ldu,
+                         double* out, int ldo, void* stream);
+
+/* Workspace bytes needed by usbs_eigsh_smallest (host call, no GPU work). */
+size_t usbs_eigsh_workspace_bytes(int n, long long nnz, int inner_iterations, int precision);
+
+/* eigsh_smallest (solver/lanczos.py:239-284): the num_desired smallest
+ * eigenpairs of c_scale*C + A*(adjoint_left_vec) (the solvers pass c_scale = -1
+ * for their -C, solver/usbs.py:590) by thick-restart Lanczos with
+ * inner_iterations (<= 32) vectors, at most max_restarts cycles and absolute
+ * residual tolerance `tolerance`.
+ *   q0:   unit start vector, n entries of the `precision` type;
+ *   Q:    ldq x (inner_iterations + 1) column-major (`precision` type, ldq >= n);
+ *         on return Q[:, :num_desired] are the eigenvectors;
+ *   eigenvalues: num_desired doubles (ascending);
+ *   info: 8 ints: [0] saved vectors of the last restart, [1] converged count,
+ *         [2] restarts run, [3] breakdown restarts, [4] operator applications,
+ *         [5] status bits (1 barrier timeout, 8 projected eigensolver failure).
+ * Runs as one cooperative kernel; the call is asynchronous. */
+int usbs_eigsh_smallest(int n, long long nnz, const int* rowptr, const int* col,
+                        const double* c_val, double c_scale, const int* slot_ptr, const int* slot_tid,
+                        const int* t_con, const double* t_a, const double* adjoint_left_vec,
+                        const void* q0, int num_desired, int inner_iterations, int max_restarts,
+                        double tolerance, int precision, void* Q, int ldq, double* eigenvalues,
+                        int* info, void* workspace, size_t workspace_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* USBS_GB300_H */

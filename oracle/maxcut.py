@@ -1,0 +1,108 @@
+"""MaxCut SDP builder (oracle).  Restates ``utils/maxcut_helpers.py:26-92`` and the
+implicit / dual-only warm starts (``utils/maxcut_helpers.py:95-161, 232-289``).
+
+Input ``W`` is the (symmetric or not) weighted adjacency matrix, as the reference
+reads it from a .mat file.  C = 1/4 (diag(W 1) - W), symmetrised; constraints
+diag(X) = 1 as (i, i, i) triples.  ``Omega`` defaults to
+``hash_normal_matrix(1, n, sketch_dim)`` in place of ``PRNGKey(0)``.
+"""
+import numpy as np
+import scipy.sparse as sp
+
+from .common import SDPState, scale_sdp_state, unscale_sdp_state
+from .rng import hash_normal_matrix
+
+
+def laplacian_objective(W):
+    n = W.shape[0]
+    W = sp.csc_matrix(W, dtype=np.float64)
+    C = sp.spdiags((W @ np.ones((n, 1))).T, 0, n, n) - W
+    C = 0.5 * (C + C.T)
+    C = 0.25 * C
+    C = sp.csr_matrix(C)
+    C.sum_duplicates()
+    C.sort_indices()
+    return C
+
+
+def get_all_problem_data(n):
+    A_indices = np.repeat(np.arange(n)[:, None], 3, axis=1).astype(np.int64)
+    A_data = np.ones(n)
+    b = np.ones(n)
+    b_ineq_mask = np.zeros(n)
+    return A_data, A_indices, b, b_ineq_mask
+
+
+def initialize_state(W, sketch_dim, Omega=None):
+    C = laplacian_objective(W)
+    n = C.shape[0]
+    A_data, A_indices, b, mask = get_all_problem_data(n)
+    m = n
+    if sketch_dim == -1:
+        X, Om, P = np.zeros((n, n)), None, None
+    elif sketch_dim > 0:
+        X = None
+        Om = hash_normal_matrix(1, n, sketch_dim) if Omega is None else np.asarray(Omega)
+        P = np.zeros_like(Om)
+    else:
+        raise ValueError("Invalid value for sketch_dim")
+    st = SDPState(C=C, A_indices=A_indices, A_data=A_data, b=b, b_ineq_mask=mask, X=X, P=P,
+                  Omega=Om, y=np.zeros(m), z=np.zeros(m), tr_X=0.0, primal_obj=0.0,
+                  SCALE_C=1.0, SCALE_X=1.0, SCALE_A=np.ones(m))
+    return scale_sdp_state(st)
+
+
+def get_implicit_warm_start_state(old, W, sketch_dim, Omega_pad=None):
+    """utils/maxcut_helpers.py:95-161 (sketch or dense-X state, rows padded with zeros)."""
+    old = unscale_sdp_state(old)
+    C = laplacian_objective(W)
+    n = C.shape[0]
+    n_old = old.C.shape[0]
+    A_data, A_indices, b, mask = get_all_problem_data(n)
+    m = n
+    X, Om, P = old.X, old.Omega, old.P
+    if old.X is not None:
+        X = np.zeros((n, n))
+        X[:n_old, :n_old] = old.X
+    if old.P is not None:
+        P = np.zeros((n, sketch_dim))
+        P[:n_old] = old.P
+        if Omega_pad is None:
+            Omega_pad = hash_normal_matrix(n, n - n_old, sketch_dim)
+        Om = np.concatenate([old.Omega, Omega_pad], axis=0)
+    y = np.zeros(m)
+    y[:old.b.shape[0]] = old.y
+    z = np.zeros(m)
+    z[:old.b.shape[0]] = old.z
+    old_diag = old.C.diagonal()
+    new_diag = C.diagonal()
+    primal_obj = old.primal_obj - old_diag @ old.z + new_diag @ z
+    st = SDPState(C=C, A_indices=A_indices, A_data=A_data, b=b, b_ineq_mask=mask, X=X, P=P,
+                  Omega=Om, y=y, z=z, tr_X=old.tr_X, primal_obj=primal_obj,
+                  SCALE_C=1.0 / np.linalg.norm(C.data), SCALE_X=1.0 / float(n),
+                  SCALE_A=np.ones(m))
+    return scale_sdp_state(st)
+
+
+def get_dual_only_warm_start_state(old, W, sketch_dim, Omega=None):
+    """utils/maxcut_helpers.py:232-289."""
+    old = unscale_sdp_state(old)
+    C = laplacian_objective(W)
+    n = C.shape[0]
+    A_data, A_indices, b, mask = get_all_problem_data(n)
+    m = n
+    if sketch_dim == -1:
+        X, Om, P = np.zeros((n, n)), None, None
+    elif sketch_dim > 0:
+        X = None
+        Om = hash_normal_matrix(1, n, sketch_dim) if Omega is None else np.asarray(Omega)
+        P = np.zeros_like(Om)
+    else:
+        raise ValueError("Invalid value for sketch_dim")
+    y = np.zeros(m)
+    y[:old.b.shape[0]] = old.y
+    st = SDPState(C=C, A_indices=A_indices, A_data=A_data, b=b, b_ineq_mask=mask, X=X, P=P,
+                  Omega=Om, y=y, z=np.zeros(m), tr_X=0.0, primal_obj=0.0,
+                  SCALE_C=1.0 / np.linalg.norm(C.data), SCALE_X=1.0 / float(n),
+                  SCALE_A=np.ones(m))
+    return scale_sdp_state(st)

@@ -1,0 +1,134 @@
+"""QAP SDP relaxation builder (oracle).  Restates ``utils/qap_helpers.py:157-381``.
+
+``build_objective_matrix`` (157-172): lifted (l^2+1) x (l^2+1) objective from the
+Kronecker product of W (flow) and D (distance), shifted by one row/column.
+``get_all_problem_data`` (175-318): X00 = 1, arrow constraints diag(Y) = Y_0.,
+row and column sums, both partial traces, and Y >= 0 on the objective's upper
+triangle (as -Y <= 0 inequality rows).  ``initialize_state`` (321-381): C = -C,
+SCALE_X = 1/(l+1), SCALE_C = 1/||C||_F, SCALE_A from row norms and the ARPACK
+spectral norm of the scaled constraint matrix (qap_helpers.py:335).
+"""
+import numpy as np
+import scipy.sparse as sp
+from scipy.sparse.linalg import eigsh
+
+from .common import SDPState, scale_sdp_state
+from .rng import hash_normal_matrix
+
+
+def build_objective_matrix(D, W):
+    n = D.shape[0]
+    dr, dc = np.nonzero(D)
+    wr, wc = np.nonzero(W)
+    d_data = D[dr, dc]
+    w_data = W[wr, wc]
+    rows = (dr[None, :] + n * wr[:, None]).reshape(-1) + 1
+    cols = (dc[None, :] + n * wc[:, None]).reshape(-1) + 1
+    data = (d_data[None, :] * w_data[:, None]).reshape(-1)
+    return rows.astype(np.int64), cols.astype(np.int64), data, n * n + 1
+
+
+def get_all_problem_data(C_rows, C_cols, N):
+    n = N
+    l = int(np.sqrt(n - 1))
+    idx = [np.array([[0, 0, 0]])]
+    dat = [np.array([1.0])]
+    b = [np.array([1.0])]
+    msk = [np.array([0.0])]
+    mcount = 1
+    # diag(Y) = Y_0. (arrow)
+    ci = mcount + np.repeat(np.arange(n - 1), 3)
+    j = np.arange(1, n)
+    ca = (np.array([[1, 0, 1]]) * j[:, None]).reshape(-1)
+    cb = (np.array([[0, 1, 1]]) * j[:, None]).reshape(-1)
+    idx.append(np.stack([ci, ca, cb], 1))
+    dat.append(np.tile(np.array([-1.0, -1.0, 2.0]), n - 1))
+    b.append(np.zeros(n - 1))
+    msk.append(np.zeros(n - 1))
+    mcount += n - 1
+    # row sums
+    ci = mcount + np.repeat(np.arange(l), 2 * l)
+    jj = np.arange(1, n).reshape(l, l).flatten()
+    ca = (np.array([[1, 0]]) * jj[:, None]).reshape(-1)
+    cb = (np.array([[0, 1]]) * jj[:, None]).reshape(-1)
+    idx.append(np.stack([ci, ca, cb], 1))
+    dat.append(np.ones(2 * (n - 1)))
+    b.append(2.0 * np.ones(l))
+    msk.append(np.zeros(l))
+    mcount += l
+    # column sums
+    ci = mcount + np.repeat(np.arange(l), 2 * l)
+    jj = np.arange(1, n).reshape(l, l).T.flatten()
+    ca = (np.array([[1, 0]]) * jj[:, None]).reshape(-1)
+    cb = (np.array([[0, 1]]) * jj[:, None]).reshape(-1)
+    idx.append(np.stack([ci, ca, cb], 1))
+    dat.append(np.ones(2 * (n - 1)))
+    b.append(2.0 * np.ones(l))
+    msk.append(np.zeros(l))
+    mcount += l
+    # partial trace 1
+    ci = mcount + np.repeat(np.arange(n - 1), l)
+    ca = 1 + np.tile(np.arange(l)[:, None, None] + l * np.arange(l)[None, None, :],
+                     (1, l, 1)).reshape(-1)
+    cb = 1 + np.tile(np.arange(l)[None, :, None] + l * np.arange(l)[None, None, :],
+                     (l, 1, 1)).reshape(-1)
+    idx.append(np.stack([ci, ca, cb], 1))
+    idx.append(np.stack([ci, cb, ca], 1))
+    dat.append(np.ones(2 * ca.size))
+    b.append(2.0 * (ca == cb).reshape(l ** 2, l).T[0].astype(float))
+    msk.append(np.zeros(n - 1))
+    mcount += n - 1
+    # partial trace 2
+    ci = mcount + np.repeat(np.arange(n - 1), l)
+    ca = 1 + np.tile(l * np.arange(l)[:, None, None] + np.arange(l)[None, None, :],
+                     (1, l, 1)).reshape(-1)
+    cb = 1 + np.tile(l * np.arange(l)[None, :, None] + np.arange(l)[None, None, :],
+                     (l, 1, 1)).reshape(-1)
+    idx.append(np.stack([ci, ca, cb], 1))
+    idx.append(np.stack([ci, cb, ca], 1))
+    dat.append(np.ones(2 * ca.size))
+    b.append(2.0 * (ca == cb).reshape(l ** 2, l).T[0].astype(float))
+    msk.append(np.zeros(n - 1))
+    mcount += n - 1
+    # Y >= 0 on the objective's upper triangle
+    tri = C_rows <= C_cols
+    nt = int(tri.sum())
+    ci = mcount + np.arange(nt)
+    trip = np.stack([ci, C_rows[tri], C_cols[tri]], 1)
+    trip = np.concatenate([trip, trip[:, [0, 2, 1]]], 0)
+    idx.append(trip)
+    dat.append(np.full(trip.shape[0], -0.5))
+    b.append(np.zeros(nt))
+    msk.append(np.ones(nt))
+    return (np.concatenate(dat), np.concatenate(idx).astype(np.int64), np.concatenate(b),
+            np.concatenate(msk))
+
+
+def initialize_state(D, W, sketch_dim, Omega=None):
+    r, c, v, N = build_objective_matrix(D, W)
+    v = -v
+    C = sp.csr_matrix((v, (r, c)), shape=(N, N))
+    A_data, A_indices, b, mask = get_all_problem_data(r, c, N)
+    n, m = N, b.shape[0]
+    l = int(np.sqrt(n - 1))
+    SCALE_X = 1.0 / float(l + 1)
+    SCALE_C = 1.0 / np.linalg.norm(v)
+    SCALE_A = 1.0 / np.sqrt(np.bincount(A_indices[:, 0], weights=A_data ** 2, minlength=m))
+    A_mat = sp.coo_matrix((SCALE_A[A_indices[:, 0]] * A_data,
+                           (A_indices[:, 0], A_indices[:, 1] * n + A_indices[:, 2])),
+                          shape=(m, n * n)).tocsr()
+    norm_A = np.sqrt(eigsh(A_mat @ A_mat.T, k=1, which="LM", return_eigenvectors=False,
+                           maxiter=np.iinfo(np.int32).max)[0])
+    SCALE_A = SCALE_A / norm_A
+    if sketch_dim == -1:
+        X, Om, P = np.zeros((n, n)), None, None
+    elif sketch_dim > 0:
+        X = None
+        Om = hash_normal_matrix(1, n, sketch_dim) if Omega is None else np.asarray(Omega)
+        P = np.zeros_like(Om)
+    else:
+        raise ValueError("Invalid value for sketch_dim")
+    st = SDPState(C=C, A_indices=A_indices, A_data=A_data, b=b, b_ineq_mask=mask, X=X, P=P,
+                  Omega=Om, y=np.zeros(m), z=np.zeros(m), tr_X=0.0, primal_obj=0.0,
+                  SCALE_C=SCALE_C, SCALE_X=SCALE_X, SCALE_A=SCALE_A)
+    return scale_sdp_state(st)

@@ -1,0 +1,137 @@
+"""GPU parity of the operator callbacks and of eigsh_smallest against the oracle."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from oracle import lanczos as olz
+from oracle import maxcut as omaxcut
+from oracle import operators as oops
+from oracle import qap as oqap
+from oracle import rng as orng
+from usbs_gb300 import workloads as wl
+
+pytestmark = pytest.mark.gpu
+
+
+def _np(t):
+    return t.detach().cpu().numpy()
+
+
+def test_apply_A_operator_and_adjoint_qap(cuda):
+    from usbs_gb300 import api
+    from usbs_gb300.problem import DeviceProblem, layout
+    D, W = wl.qap_instance(6, 0, grid=5)
+    st = oqap.initialize_state(D, W, 6)
+    n, m = st.C.shape[0], st.b.shape[0]
+    prob = DeviceProblem(layout(st.C, st.A_data, st.A_indices, m=m), cuda)
+    rs = np.random.default_rng(0)
+    U = rs.standard_normal((n, 3))
+    z = rs.standard_normal(m)
+    got = _np(api.apply_A_operator_batched(m, None, None, U, problem=prob))
+    ref = oops.apply_A_operator_batched(m, st.A_data, st.A_indices, U)
+    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-12)
+    got = _np(api.apply_A_adjoint_batched(n, None, None, z, U, problem=prob))
+    ref = oops.apply_A_adjoint_batched(n, st.A_data, st.A_indices, z, U)
+    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-12)
+    got = _np(api.apply_A_operator_slim(m, st.A_data, st.A_indices, U[:, 0], n=n))
+    np.testing.assert_allclose(got, oops.apply_A_operator_slim(m, st.A_data, st.A_indices,
+                                                               U[:, 0]), rtol=1e-12, atol=1e-12)
+
+
+@pytest.mark.parametrize("precision,tol", [(64, 1e-13), (32, 2e-6)])
+def test_operator_apply_maxcut(cuda, precision, tol):
+    from usbs_gb300 import api
+    from usbs_gb300.problem import DeviceProblem, layout
+    Wg = wl.torus_graph(40, 1)
+    st = omaxcut.initialize_state(Wg, 4)
+    n = st.C.shape[0]
+    prob = DeviceProblem(layout(st.C, st.A_data, st.A_indices, m=n), cuda)
+    rs = np.random.default_rng(1)
+    w = rs.standard_normal(n)
+    x = rs.standard_normal(n)
+    ref = olz.make_operator((-st.C).tocsr(), st.A_data, st.A_indices, w)(x)
+    got = _np(api.operator_apply(prob, -1.0, w, x, precision=precision)).astype(np.float64)
+    assert np.abs(got - ref).max() <= tol * np.abs(ref).max()
+
+
+def _subspace_gap(A, B):
+    """Largest principal-angle sine between the column spans of A and B."""
+    qa, _ = np.linalg.qr(A)
+    qb, _ = np.linalg.qr(B)
+    s = np.linalg.svd(qa.T @ qb, compute_uv=False)
+    return float(np.sqrt(max(0.0, 1.0 - s.min() ** 2)))
+
+
+@pytest.mark.parametrize("name,nd", [("er", 11), ("torus", 10)])
+def test_eigsh_fp64_matches_oracle(cuda, name, nd):
+    from usbs_gb300 import api
+    from usbs_gb300.problem import DeviceProblem, layout
+    Wg = wl.er_graph(800, 19176, 0) if name == "er" else wl.torus_graph(30, 1)
+    st = omaxcut.initialize_state(Wg, 4)
+    n = st.C.shape[0]
+    prob = DeviceProblem(layout(st.C, st.A_data, st.A_indices, m=n), cuda)
+    y = np.random.default_rng(2).standard_normal(n) * 0.5
+    q0 = orng.default_q0(n)
+    trace = []
+    ov, oV, ost = olz.eigsh_smallest(n, (-st.C).tocsr(), st.A_data, st.A_indices, y, q0, nd, 32,
+                                     10, 1e-7, trace=trace)
+    gv, gV, info = api.eigsh_smallest(n, prob, None, None, y, q0, nd, 32, 10, 1e-7, c_scale=-1.0,
+                                      precision=64, return_info=True)
+    gv, gV = _np(gv), _np(gV)
+    assert info.status == 0
+    assert info.restarts == ost["restart"]
+    np.testing.assert_allclose(gv, ov, rtol=1e-9, atol=1e-9 * np.abs(ov).max())
+    # eigenvectors: compare the invariant quantities (column signs are free)
+    for j in range(nd):
+        c = abs(gV[:, j] @ oV[:, j])
+        assert c > 1 - 1e-7, (j, c)
+    np.testing.assert_allclose(gV.T @ gV, np.eye(nd), atol=1e-10)
+
+
+def test_eigsh_fp32_close_to_oracle(cuda):
+    from usbs_gb300 import api
+    from usbs_gb300.problem import DeviceProblem, layout
+    Wg = wl.torus_graph(60, 1)
+    st = omaxcut.initialize_state(Wg, 4)
+    n = st.C.shape[0]
+    prob = DeviceProblem(layout(st.C, st.A_data, st.A_indices, m=n), cuda)
+    y = np.zeros(n)
+    q0 = orng.default_q0(n)
+    ov, oV, _ = olz.eigsh_smallest(n, (-st.C).tocsr(), st.A_data, st.A_indices, y, q0, 10, 32, 10,
+                                   1e-7)
+    gv, gV, info = api.eigsh_smallest(n, prob, None, None, y, q0, 10, 32, 10, 1e-7, c_scale=-1.0,
+                                      precision=32, return_info=True)
+    gv = _np(gv)
+    scale = np.abs(ov).max()
+    assert np.abs(gv - ov).max() < 1e-4 * scale
+    assert info.status == 0
+
+
+def test_eigsh_path_laplacian_known_spectrum(cuda):
+    from usbs_gb300 import api
+    n = 500
+    W = sp.diags([np.ones(n - 1), np.ones(n - 1)], [-1, 1]).tocsr()
+    L = (sp.diags(np.asarray(W.sum(1)).ravel()) - W).tocsr()
+    A_data, A_idx, _, _ = omaxcut.get_all_problem_data(n)
+    exact = 2.0 - 2.0 * np.cos(np.pi * np.arange(n) / n)
+    gv, gV = api.eigsh_smallest(n, L, A_data, A_idx, np.zeros(n), orng.default_q0(n), 3, 32,
+                                300, 1e-10)
+    np.testing.assert_allclose(_np(gv), exact[:3], atol=1e-8)
+
+
+def test_eigsh_breakdown_small_operator(cuda):
+    """n < inner iterations forces a Krylov breakdown (solver/lanczos.py:107-117)."""
+    from usbs_gb300 import api
+    n = 8
+    rs = np.random.default_rng(5)
+    Wd = rs.random((n, n)); Wd = np.triu(Wd, 1); Wd = Wd + Wd.T
+    st = omaxcut.initialize_state(sp.csr_matrix(Wd), 2)
+    A_data, A_idx = st.A_data, st.A_indices
+    q0 = orng.default_q0(n)
+    ov, oV, _ = olz.eigsh_smallest(n, (-st.C).tocsr(), A_data, A_idx, np.zeros(n), q0, 3, 8, 3,
+                                   1e-12)
+    gv, gV, info = api.eigsh_smallest(n, st.C, A_data, A_idx, np.zeros(n), q0, 3, 8, 3, 1e-12,
+                                      c_scale=-1.0, return_info=True)
+    np.testing.assert_allclose(_np(gv), ov, atol=1e-9)
+    ex = np.linalg.eigvalsh((-st.C).toarray())[:3]
+    np.testing.assert_allclose(_np(gv), ex, atol=1e-9)

@@ -1,0 +1,91 @@
+"""Host-side layout of the problem data, and the C ABI library (CPU only)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import scipy.sparse as sp
+
+from usbs_gb300 import problem as P
+from usbs_gb300 import workloads as wl
+from oracle import maxcut as omaxcut
+from oracle import qap as oqap
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _check_layout(C, A_data, A_idx, m):
+    L = P.layout(C, A_data, A_idx, m=m)
+    n = C.shape[0]
+    # union pattern holds C exactly and every triple position
+    M = sp.csr_matrix((L.c_val, L.col, L.rowptr), shape=(n, n))
+    assert abs(M - C).max() == 0
+    pos = set(zip(np.repeat(np.arange(n), np.diff(L.rowptr)), L.col))
+    assert all((i, j) in pos for i, j in zip(A_idx[:, 1], A_idx[:, 2]))
+    # slot map: every triple exactly once, on its (i, j)
+    prow = np.repeat(np.arange(n), np.diff(L.rowptr))
+    seen = np.zeros(A_data.size, dtype=int)
+    for p in range(L.nnz):
+        for q in range(L.slot_ptr[p], L.slot_ptr[p + 1]):
+            t = L.slot_tid[q]
+            seen[t] += 1
+            assert A_idx[t, 1] == prow[p] and A_idx[t, 2] == L.col[p]
+    assert np.all(seen == 1)
+    # constraint-sorted copy reproduces A(u u^T)
+    u = np.random.default_rng(0).standard_normal(n)
+    ref = np.bincount(A_idx[:, 0], weights=A_data * u[A_idx[:, 1]] * u[A_idx[:, 2]], minlength=m)
+    got = np.zeros(m)
+    for c in range(m):
+        s = slice(L.con_ptr[c], L.con_ptr[c + 1])
+        got[c] = np.sum(L.t_a[s] * u[L.t_row[s]] * u[L.t_col[s]])
+    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-12)
+    # row-sorted copy reproduces A*(z) u
+    z = np.random.default_rng(1).standard_normal(m)
+    ref = np.bincount(A_idx[:, 1], weights=A_data * z[A_idx[:, 0]] * u[A_idx[:, 2]], minlength=n)
+    got = np.array([np.sum(L.r_a[L.row_ptr[i]:L.row_ptr[i + 1]]
+                           * z[L.r_con[L.row_ptr[i]:L.row_ptr[i + 1]]]
+                           * u[L.r_col[L.row_ptr[i]:L.row_ptr[i + 1]]]) for i in range(n)])
+    np.testing.assert_allclose(got, ref, rtol=1e-12, atol=1e-12)
+    return L
+
+
+def test_layout_maxcut():
+    W = wl.er_graph(60, 300, 0)
+    st = omaxcut.initialize_state(W, 4)
+    L = _check_layout(st.C, st.A_data, st.A_indices, 60)
+    assert L.diag_constraints
+
+
+def test_layout_qap_small():
+    D, W = wl.qap_instance(4, 0, grid=4)
+    st = oqap.initialize_state(D, W, 4)
+    L = _check_layout(st.C, st.A_data, st.A_indices, st.b.shape[0])
+    assert not L.diag_constraints
+
+
+def test_layout_rejects_bad_triples():
+    C = sp.eye(4, format="csr")
+    try:
+        P.layout(C, np.ones(1), np.array([[0, 7, 0]]), m=1)
+    except ValueError:
+        return
+    raise AssertionError("out-of-range triple accepted")
+
+
+def _declared_functions():
+    hdr = open(os.path.join(ROOT, "include", "usbs_gb300.h")).read()
+    hdr = re.sub(r"/\*.*?\*/", "", hdr, flags=re.S)
+    return sorted(set(re.findall(r"\b(usbs_[A-Za-z0-9_]+)\s*\(", hdr)))
+
+
+def test_library_builds_and_exports_every_declared_symbol():
+    from usbs_gb300 import build, _lib
+    path = build.build()
+    lib = ctypes.CDLL(path)
+    names = _declared_functions()
+    assert len(names) >= 8
+    for name in names:
+        assert hasattr(lib, name), f"{name} declared in include/usbs_gb300.h but not exported"
+    assert set(names) <= set(_lib.SIGNATURES), "ctypes signatures missing for some entry points"
+    lib.usbs_abi_version.restype = ctypes.c_int
+    assert lib.usbs_abi_version() == 1

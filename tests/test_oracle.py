@@ -1,0 +1,156 @@
+"""Pins the CPU oracle with mathematics (the reference ships no golden vectors,
+and its JAX implementation cannot run here).  CPU only."""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+
+from oracle import lanczos, loop, operators, rng
+from oracle import maxcut as omaxcut
+from oracle import usbs as ousbs
+from oracle import ipm as oipm
+
+
+def test_splitmix64_known_answer():
+    # Vigna's splitmix64 with state 0: first output 0xE220A8397B1DCDAF
+    z = rng._splitmix64(np.array([0], dtype=np.uint64))
+    assert int(z[0]) == 0xE220A8397B1DCDAF
+    z = rng._splitmix64(np.array([0x9E3779B97F4A7C15], dtype=np.uint64))
+    assert int(z[0]) == 0x6E789E6AA1B965F4
+
+
+def test_hash_normal_moments():
+    x = rng.hash_normal(7, 200000)
+    assert abs(x.mean()) < 0.01
+    assert abs(x.std() - 1.0) < 0.01
+    assert np.array_equal(x, rng.hash_normal(7, 200000))
+    assert not np.array_equal(x[:10], rng.hash_normal(8, 10))
+
+
+def test_cond_schedule_matches_reference_formula():
+    # utils/loop.py:86-92 worked by hand for base 2, maxiter 100:
+    # num = ceil(log(99)/log 2) + 1 = 8 -> 1,2,4,...,64; cumsum >= 100 from 64 on
+    assert loop.cond_schedule(100, 2.0) == [1, 2, 4, 8, 16, 32, 37]
+    assert sum(loop.cond_schedule(1000, 1.5)) == 1000
+    assert loop.cond_schedule(5, 1.0) == [1] * 5
+
+
+def test_while_loop_semantics():
+    # body runs while cond holds, at most maxiter times, cond checked after each body
+    calls = []
+    out = loop.while_loop(lambda v: v < 5, lambda v: calls.append(v) or v + 1, 0, 100)
+    assert out == 5 and calls == [0, 1, 2, 3, 4]
+    assert loop.while_loop(lambda v: True, lambda v: v + 1, 0, 7) == 7
+    assert loop.while_loop(lambda v: True, lambda v: v + 1, 0, 10, cond_exp_base=2.0) == 10
+
+
+def _path_laplacian(n):
+    W = sp.diags([np.ones(n - 1), np.ones(n - 1)], [-1, 1])
+    return (sp.diags(np.asarray(W.sum(1)).ravel()) - W).tocsr()
+
+
+def test_lanczos_path_laplacian_spectrum():
+    n = 200
+    L = _path_laplacian(n)
+    exact = 2.0 - 2.0 * np.cos(np.pi * np.arange(n) / n)
+    A_idx = np.zeros((0, 3), dtype=np.int64)
+    q0 = rng.default_q0(n)
+    vals, vecs, st = lanczos.eigsh_smallest(n, L, np.zeros(0), A_idx, np.zeros(1), q0, 3, 32,
+                                            200, 1e-10)
+    np.testing.assert_allclose(vals, exact[:3], atol=1e-8)
+    r = L @ vecs - vecs * vals[None, :]
+    assert np.linalg.norm(r, axis=0).max() < 1e-6
+    np.testing.assert_allclose(vecs.T @ vecs, np.eye(3), atol=1e-10)
+
+
+def test_lanczos_adjoint_term_diagonal_shift():
+    # C + A*(w) with diag triples and w = s 1 shifts the spectrum by s
+    n = 120
+    L = _path_laplacian(n)
+    A_data, A_idx, _, _ = omaxcut.get_all_problem_data(n)
+    q0 = rng.default_q0(n)
+    v0, _, _ = lanczos.eigsh_smallest(n, L, A_data, A_idx, np.zeros(n), q0, 2, 32, 100, 1e-10)
+    v1, _, _ = lanczos.eigsh_smallest(n, L, A_data, A_idx, np.full(n, 3.5), q0, 2, 32, 100, 1e-10)
+    np.testing.assert_allclose(v1, v0 + 3.5, atol=1e-8)
+
+
+def test_A_adjoint_identity():
+    rs = np.random.default_rng(0)
+    n, m, T = 50, 30, 400
+    A_idx = np.stack([rs.integers(0, m, T), rs.integers(0, n, T), rs.integers(0, n, T)], 1)
+    A_data = rs.standard_normal(T)
+    u = rs.standard_normal(n)
+    z = rs.standard_normal(m)
+    lhs = u @ operators.apply_A_adjoint_slim(n, A_data, A_idx, z, u)
+    rhs = z @ operators.apply_A_operator_slim(m, A_data, A_idx, u)
+    assert abs(lhs - rhs) < 1e-10 * (1 + abs(lhs))
+    V = rs.standard_normal((n, 4))
+    bat = operators.apply_A_operator_batched(m, A_data, A_idx, V)
+    ref = sum(operators.apply_A_operator_slim(m, A_data, A_idx, V[:, j]) for j in range(4))
+    np.testing.assert_allclose(bat, ref, rtol=1e-12, atol=1e-12)
+
+
+def test_create_Q_base_matches_tensor_definition():
+    rs = np.random.default_rng(1)
+    n, m, T, k = 20, 9, 60, 3
+    A_idx = np.stack([rs.integers(0, m, T), rs.integers(0, n, T), rs.integers(0, n, T)], 1)
+    A_data = rs.standard_normal(T)
+    V = rs.standard_normal((n, k))
+    U = operators.create_svec_matrix(k)
+    # solver/utils.py:53-65 written out with the explicit m x k x k tensor
+    base = np.zeros((m, k, k))
+    for t in range(T):
+        base[A_idx[t, 0]] += A_data[t] * np.outer(V[A_idx[t, 1]], V[A_idx[t, 2]])
+    proj = U @ base.reshape(m, k * k).T
+    ref = (proj[:, None, :] * proj[None, :, :]).sum(-1)
+    np.testing.assert_allclose(operators.create_Q_base(m, k, U, A_data, A_idx, V), ref,
+                               rtol=1e-12, atol=1e-12)
+
+
+def test_svec_isometry():
+    k = 5
+    U = operators.create_svec_matrix(k)
+    rs = np.random.default_rng(2)
+    A = rs.standard_normal((k, k)); A = A + A.T
+    B = rs.standard_normal((k, k)); B = B + B.T
+    assert abs(operators.svec(U, A) @ operators.svec(U, B) - np.sum(A * B)) < 1e-12
+    np.testing.assert_allclose(operators.svec_inv(U, operators.svec(U, A), k), A, atol=1e-12)
+
+
+def _complete_graph(n):
+    W = np.ones((n, n)) - np.eye(n)
+    return sp.csr_matrix(W)
+
+
+@pytest.mark.parametrize("n", [12])
+def test_usbs_complete_graph_value(n):
+    """MaxCut SDP of K_n with unit weights: max <L/4, X> s.t. diag X = 1 is n^2/4."""
+    st = omaxcut.initialize_state(_complete_graph(n), 4)
+    out, fin = ousbs.usbs(st, n, n, 2.0 * n, 2.0, 0.01, 0.25, 3, 1, 300, np.inf, 1e-6, 1e-6,
+                          1e-6, min(n, 32), 10, 1e-7, 100)
+    assert abs(out.primal_obj - n * n / 4.0) / (n * n / 4.0) < 2e-3
+    assert fin["max_infeas"] < 1e-2
+    # the dual bound never falls below the primal value it certifies
+    assert fin["obj_ub"] >= out.primal_obj - 1e-6 * n * n
+
+
+def test_lb_ipm_is_a_lower_model_value():
+    """The spectral lower-bound IPM (solver/usbs.py:195-356) at y with tr_X_bar = 0
+    returns b.y - max over the bundle face, which never exceeds the penalised dual."""
+    n, k = 40, 3
+    rs = np.random.default_rng(3)
+    W = sp.random(n, n, density=0.2, random_state=4)
+    W = ((W + W.T) > 0).astype(float)
+    W.setdiag(0)
+    st = omaxcut.initialize_state(sp.csr_matrix(W), 4)
+    C = st.C.toarray()
+    V, _ = np.linalg.qr(rs.standard_normal((n, k)))
+    U = operators.create_svec_matrix(k)
+    y = rs.standard_normal(n) * 0.1
+    GC = V.T @ C @ V
+    Gy = V.T @ np.diag(y) @ V
+    trace_ub = 2.0 * n
+    lb = oipm.compute_lb_spec_est_ipm(U, k, trace_ub, y.sum(), GC, Gy, 0.0, 0.0, 0.0, 1e-9, 100)
+    lam = np.linalg.eigvalsh(GC - Gy)
+    # bundle model: b.y + trace_ub * max(lambda_max(V^T (C - A*y) V), 0)
+    model = y.sum() + trace_ub * max(lam[-1], 0.0)
+    assert abs(lb - model) < 1e-5 * (1 + abs(model))

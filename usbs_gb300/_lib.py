@@ -1,0 +1,62 @@
+"""ctypes binding of libusbs_gb300.so (the C ABI in include/usbs_gb300.h).
+
+The library is built in-tree by :mod:`usbs_gb300.build`.  Nothing here falls
+back to another implementation: if the library cannot be loaded every entry
+point raises.
+"""
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libusbs_gb300.so")
+
+_lib = None
+
+c_int, c_ll, c_double, c_size_t, c_void_p = (ctypes.c_int, ctypes.c_longlong, ctypes.c_double,
+                                              ctypes.c_size_t, ctypes.c_void_p)
+P = c_void_p
+
+# name -> (restype, argtypes); must match include/usbs_gb300.h
+SIGNATURES = {
+    "usbs_abi_version": (c_int, []),
+    "usbs_last_error": (ctypes.c_char_p, []),
+    "usbs_device_info": (c_int, [c_int, P, P, P]),
+    "usbs_assemble_operator": (c_int, [c_ll, P, c_double, P, P, P, P, P, P, c_int, P]),
+    "usbs_operator_apply": (c_int, [c_int, c_ll, P, P, P, P, P, c_int, P]),
+    "usbs_apply_A_operator": (c_int, [c_int, c_int, P, P, P, P, P, c_int, P, P]),
+    "usbs_apply_A_adjoint": (c_int, [c_int, c_int, P, P, P, P, P, P, c_int, P, c_int, P]),
+    "usbs_eigsh_workspace_bytes": (c_size_t, [c_int, c_ll, c_int, c_int]),
+    "usbs_eigsh_smallest": (c_int, [c_int, c_ll, P, P, P, c_double, P, P, P, P, P, P, c_int, c_int, c_int,
+                                    c_double, c_int, P, c_int, P, P, P, c_size_t, P]),
+}
+
+
+class LibraryError(RuntimeError):
+    pass
+
+
+def load(build_if_missing=True):
+    """Load (building first if needed) and return the ctypes library handle."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if build_if_missing:
+        from . import build as _build
+        _build.build()
+    if not os.path.exists(LIB_PATH):
+        raise LibraryError(f"{LIB_PATH} is missing; run python -m usbs_gb300.build")
+    lib = ctypes.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if lib.usbs_abi_version() != 1:
+        raise LibraryError("libusbs_gb300 ABI version mismatch")
+    _lib = lib
+    return lib
+
+
+def check(rc, what):
+    if rc != 0:
+        msg = _lib.usbs_last_error().decode() if _lib is not None else ""
+        raise LibraryError(f"{what} failed (rc={rc}): {msg}")

@@ -1,0 +1,178 @@
+"""Reference-shaped entry points of the USBS hot path on the GB300.
+
+Each function keeps the name, argument order and meaning of the reference
+(rangell/usbs) and runs on the device through the C ABI of libusbs_gb300:
+
+* ``apply_A_operator_slim/_batched``  solver/utils.py:11-16, 27-31
+* ``apply_A_adjoint_slim/_batched``   solver/utils.py:19-24, 34-37
+* ``eigsh_smallest``                  solver/lanczos.py:239-284
+* ``usbs`` / ``cgal``                 solver/usbs.py:436, solver/cgal.py:21 (see solver.py)
+
+Inputs may be NumPy / SciPy (copied to the device) or CUDA torch tensors; the
+outputs are CUDA torch tensors.  There is no CPU path: without a CUDA device or
+without the built library every call raises.
+"""
+import ctypes
+
+import numpy as np
+import scipy.sparse as sp
+
+from . import _lib
+from .problem import DeviceProblem, layout
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("usbs_gb300 needs a CUDA device (GB300, sm_103a); none is visible")
+    return torch
+
+
+def _p(t):
+    return ctypes.c_void_p(int(t.data_ptr())) if t is not None else ctypes.c_void_p(0)
+
+
+def _stream():
+    torch = _torch()
+    return ctypes.c_void_p(int(torch.cuda.current_stream().cuda_stream))
+
+
+def _dev(x, dtype, device):
+    torch = _torch()
+    if isinstance(x, torch.Tensor):
+        return x.to(device=device, dtype=dtype).contiguous()
+    return torch.as_tensor(np.ascontiguousarray(x), dtype=dtype, device=device)
+
+
+def _vt(precision):
+    torch = _torch()
+    if precision == 64:
+        return torch.float64
+    if precision == 32:
+        return torch.float32
+    raise ValueError("precision must be 64 or 32")
+
+
+def _problem_for(C, A_data, A_indices, m, device):
+    if isinstance(C, DeviceProblem):
+        return C
+    return DeviceProblem(layout(C, A_data, A_indices, m=m), device=device)
+
+
+def _cols(U, n, device):
+    """Column-major device copy of an (n,) or (n, k) array: returns (tensor[k, ld], ld, k)."""
+    torch = _torch()
+    Ut = _dev(U, torch.float64, device)
+    if Ut.dim() == 1:
+        Ut = Ut.reshape(n, 1)
+    k = Ut.shape[1]
+    return Ut.t().contiguous(), n, k
+
+
+def apply_A_operator_batched(m, A_data, A_indices, vecs, *, problem=None, n=None, device="cuda"):
+    """sum_j A(v_j v_j^T) over the columns of ``vecs`` -> (m,) float64."""
+    torch = _torch()
+    lib = _lib.load()
+    if problem is None:
+        nn = n if n is not None else int(np.asarray(vecs).shape[0])
+        problem = DeviceProblem(layout(sp.csr_matrix((nn, nn)), A_data, A_indices, m=m), device)
+    Ucm, ld, k = _cols(vecs, problem.n, problem.device)
+    out = torch.empty(m, dtype=torch.float64, device=problem.device)
+    _lib.check(lib.usbs_apply_A_operator(m, k, _p(problem.con_ptr), _p(problem.t_row),
+                                         _p(problem.t_col), _p(problem.t_a), _p(Ucm), ld,
+                                         _p(out), _stream()), "usbs_apply_A_operator")
+    return out
+
+
+def apply_A_operator_slim(m, A_data, A_indices, u, **kw):
+    """A(u u^T) -> (m,) float64 (solver/utils.py:11-16)."""
+    return apply_A_operator_batched(m, A_data, A_indices, u, **kw)
+
+
+def apply_A_adjoint_batched(n, A_data, A_indices, z, vecs, *, problem=None, device="cuda"):
+    """[A*(z) v_j]_j for the columns of ``vecs`` -> (n, k) float64."""
+    torch = _torch()
+    lib = _lib.load()
+    zz = _dev(z, torch.float64, device if problem is None else problem.device)
+    if problem is None:
+        problem = DeviceProblem(layout(sp.csr_matrix((n, n)), A_data, A_indices, m=zz.numel()),
+                                device)
+    Ucm, ld, k = _cols(vecs, n, problem.device)
+    out = torch.empty((k, n), dtype=torch.float64, device=problem.device)
+    _lib.check(lib.usbs_apply_A_adjoint(n, k, _p(problem.row_ptr), _p(problem.r_con),
+                                        _p(problem.r_col), _p(problem.r_a), _p(zz), _p(Ucm), ld,
+                                        _p(out), n, _stream()), "usbs_apply_A_adjoint")
+    return out.t()
+
+
+def apply_A_adjoint_slim(n, A_data, A_indices, z, u, **kw):
+    """A*(z) u -> (n,) float64 (solver/utils.py:19-24)."""
+    return apply_A_adjoint_batched(n, A_data, A_indices, z, u, **kw)[:, 0]
+
+
+def operator_apply(problem, c_scale, w, x, precision=64):
+    """(c_scale * C + A*(w)) x on the device (the Lanczos operator, solver/lanczos.py:86-87)."""
+    torch = _torch()
+    lib = _lib.load()
+    vt = _vt(precision)
+    dev = problem.device
+    op = torch.empty(max(problem.nnz, 1), dtype=vt, device=dev)
+    wt = _dev(w, torch.float64, dev) if w is not None else None
+    _lib.check(lib.usbs_assemble_operator(problem.nnz, _p(problem.c_val), float(c_scale),
+                                          _p(problem.slot_ptr), _p(problem.slot_tid),
+                                          _p(problem.t_con), _p(problem.t_a0), _p(wt), _p(op),
+                                          precision, _stream()), "usbs_assemble_operator")
+    xt = _dev(x, vt, dev)
+    y = torch.empty(problem.n, dtype=vt, device=dev)
+    _lib.check(lib.usbs_operator_apply(problem.n, problem.nnz, _p(problem.rowptr),
+                                       _p(problem.col), _p(op), _p(xt), _p(y), precision,
+                                       _stream()), "usbs_operator_apply")
+    return y
+
+
+class EigshInfo:
+    def __init__(self, raw):
+        self.k_saved, self.num_converged, self.restarts, self.breakdowns, self.matvecs, \
+            self.status = (int(v) for v in raw[:6])
+
+    def __repr__(self):
+        return (f"EigshInfo(restarts={self.restarts}, converged={self.num_converged}, "
+                f"matvecs={self.matvecs}, breakdowns={self.breakdowns}, status={self.status})")
+
+
+def eigsh_smallest(n, C, A_data, A_indices, adjoint_left_vec, q0, num_desired, inner_iterations,
+                   max_restarts, tolerance, *, c_scale=1.0, precision=64, device="cuda",
+                   return_info=False, workspace=None):
+    """Smallest ``num_desired`` eigenpairs of c_scale*C + A*(adjoint_left_vec)
+    (solver/lanczos.py:239-284).  ``C`` is a SciPy sparse matrix or a prepared
+    :class:`DeviceProblem` (whose A data are then used).  Returns
+    ``(eigenvalues[num_desired] float64, eigenvectors[n, num_desired])``."""
+    torch = _torch()
+    lib = _lib.load()
+    w = np.asarray(adjoint_left_vec) if not isinstance(adjoint_left_vec, torch.Tensor) \
+        else adjoint_left_vec
+    prob = _problem_for(C, A_data, A_indices, int(w.shape[0]), device)
+    dev = prob.device
+    vt = _vt(precision)
+    wt = _dev(w, torch.float64, dev)
+    q0t = _dev(q0, vt, dev)
+    ld = (n + 31) // 32 * 32
+    Q = torch.empty((inner_iterations + 1, ld), dtype=vt, device=dev)
+    evals = torch.empty(num_desired, dtype=torch.float64, device=dev)
+    info = torch.zeros(8, dtype=torch.int32, device=dev)
+    need = int(lib.usbs_eigsh_workspace_bytes(n, prob.nnz, inner_iterations, precision))
+    if workspace is None or workspace.numel() < need:
+        workspace = torch.empty(need, dtype=torch.uint8, device=dev)
+    rc = lib.usbs_eigsh_smallest(n, prob.nnz, _p(prob.rowptr), _p(prob.col), _p(prob.c_val),
+                                 float(c_scale), _p(prob.slot_ptr), _p(prob.slot_tid),
+                                 _p(prob.t_con), _p(prob.t_a0), _p(wt), _p(q0t), num_desired,
+                                 inner_iterations, max_restarts, float(tolerance), precision,
+                                 _p(Q), ld, _p(evals), _p(info), _p(workspace), need, _stream())
+    _lib.check(rc, "usbs_eigsh_smallest")
+    vecs = Q[:num_desired, :n].t()
+    if return_info:
+        inf = EigshInfo(info.cpu().tolist())
+        if inf.status & 1:
+            raise RuntimeError("eigsh_smallest: a team barrier timed out on the device")
+        return evals, vecs, inf
+    return evals, vecs

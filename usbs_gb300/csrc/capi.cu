@@ -1,0 +1,185 @@
+// extern "C" entry points of libusbs_gb300 (declared in include/usbs_gb300.h).
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+#include <mutex>
+#include "../../include/usbs_gb300.h"
+#include "common.cuh"
+#include "internal.h"
+
+namespace usbs {
+
+static thread_local char g_err[512] = "";
+
+void set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+static DeviceInfo g_info[64];
+static std::mutex g_info_mu;
+
+int get_device_info(DeviceInfo* out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) { set_error("cudaGetDevice: %s", cudaGetErrorString(e)); return -5; }
+  if (dev < 0 || dev >= 64) { set_error("device index %d out of range", dev); return -2; }
+  std::lock_guard<std::mutex> lk(g_info_mu);
+  DeviceInfo& di = g_info[dev];
+  if (di.device != dev) {
+    int sms = 0;
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) { set_error("device attribute: %s", cudaGetErrorString(e)); return -5; }
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev);
+    if (!coop) { set_error("device %d does not support cooperative launches", dev); return -5; }
+    di.sm_count = sms;
+    di.lanczos_occ64 = lanczos_occupancy(64);
+    di.lanczos_occ32 = lanczos_occupancy(32);
+    di.device = dev;
+  }
+  *out = di;
+  return 0;
+}
+
+static size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+}  // namespace usbs
+
+using namespace usbs;
+
+extern "C" {
+
+int usbs_abi_version(void) { return USBS_GB300_ABI_VERSION; }
+
+const char* usbs_last_error(void) { return g_err; }
+
+int usbs_device_info(int device, int* sm_count, int* occ64, int* occ32) {
+  int prev = 0;
+  cudaGetDevice(&prev);
+  if (cudaSetDevice(device) != cudaSuccess) { set_error("cudaSetDevice(%d) failed", device); return -5; }
+  DeviceInfo di;
+  int rc = get_device_info(&di);
+  cudaSetDevice(prev);
+  if (rc) return rc;
+  if (sm_count) *sm_count = di.sm_count;
+  if (occ64) *occ64 = di.lanczos_occ64;
+  if (occ32) *occ32 = di.lanczos_occ32;
+  return 0;
+}
+
+int usbs_assemble_operator(long long nnz, const double* c_val, double c_scale,
+                           const int* slot_ptr, const int* slot_tid, const int* t_con,
+                           const double* t_a, const double* w, void* op_val, int precision,
+                           void* stream) {
+  if (precision != 32 && precision != 64) { set_error("precision must be 32 or 64"); return -2; }
+  if (nnz < 0 || nnz > 0x7fffffffLL) { set_error("nnz %lld out of range", nnz); return -2; }
+  if (w && (!slot_ptr || !slot_tid || !t_con || !t_a)) {
+    set_error("assemble: w given without the slot map / triples");
+    return -2;
+  }
+  return assemble_operator((int)nnz, c_val, c_scale, slot_ptr, slot_tid, t_con, t_a, w, op_val,
+                           precision, (cudaStream_t)stream);
+}
+
+int usbs_operator_apply(int n, long long nnz, const int* rowptr, const int* col,
+                        const void* op_val, const void* x, void* y, int precision,
+                        void* stream) {
+  if (precision != 32 && precision != 64) { set_error("precision must be 32 or 64"); return -2; }
+  if (n < 0) { set_error("n < 0"); return -2; }
+  DeviceInfo di;
+  int rc = get_device_info(&di);
+  if (rc) return rc;
+  return csr_spmv(n, nnz, rowptr, col, op_val, x, y, precision, di.sm_count,
+                  (cudaStream_t)stream);
+}
+
+int usbs_apply_A_operator(int m, int k, const int* con_ptr, const int* t_row, const int* t_col,
+                          const double* t_a, const double* U, int ldu, double* out,
+                          void* stream) {
+  if (m < 0 || k < 1 || ldu < 1) { set_error("apply_A_operator: bad sizes m=%d k=%d ldu=%d", m, k, ldu); return -2; }
+  return apply_A_operator(m, con_ptr, t_row, t_col, t_a, U, ldu, k, out, (cudaStream_t)stream);
+}
+
+int usbs_apply_A_adjoint(int n, int k, const int* row_ptr, const int* r_con, const int* r_col,
+                         const double* r_a, const double* z, const double* U, int ldu,
+                         double* out, int ldo, void* stream) {
+  if (n < 0 || k < 1 || ldu < n || ldo < n) {
+    set_error("apply_A_adjoint: bad sizes n=%d k=%d ldu=%d ldo=%d", n, k, ldu, ldo);
+    return -2;
+  }
+  return apply_A_adjoint(n, row_ptr, r_con, r_col, r_a, z, U, ldu, k, out, ldo,
+                         (cudaStream_t)stream);
+}
+
+size_t usbs_eigsh_workspace_bytes(int n, long long nnz, int inner_iterations, int precision) {
+  DeviceInfo di;
+  if (get_device_info(&di)) {
+    // no device: size for the largest GB300 team (152 SMs x 4 CTAs)
+    di.sm_count = 152;
+    di.lanczos_occ64 = di.lanczos_occ32 = 4;
+  }
+  const int vt = (precision == 64) ? 8 : 4;
+  const int ld = (n + 31) & ~31;
+  const int nctas = lanczos_team_size(di, n, precision);
+  size_t b = a256((size_t)(nnz > 0 ? nnz : 1) * vt);
+  b += a256(2 * MAXM * sizeof(double));
+  b += lanczos_workspace_bytes(n, ld, inner_iterations, precision, nctas);
+  return b;
+}
+
+int usbs_eigsh_smallest(int n, long long nnz, const int* rowptr, const int* col,
+                        const double* c_val, double c_scale, const int* slot_ptr, const int* slot_tid,
+                        const int* t_con, const double* t_a, const double* adjoint_left_vec,
+                        const void* q0, int num_desired, int inner_iterations, int max_restarts,
+                        double tolerance, int precision, void* Q, int ldq, double* eigenvalues,
+                        int* info, void* workspace, size_t workspace_bytes, void* stream) {
+  if (precision != 32 && precision != 64) { set_error("precision must be 32 or 64"); return -2; }
+  if (n < 1 || ldq < n || inner_iterations < 1 || inner_iterations > MAXM ||
+      num_desired < 1 || num_desired > inner_iterations || max_restarts < 0) {
+    set_error("eigsh: bad sizes n=%d ldq=%d inner_iterations=%d (<= %d) num_desired=%d "
+              "max_restarts=%d", n, ldq, inner_iterations, MAXM, num_desired, max_restarts);
+    return -2;
+  }
+  if (nnz < 0 || nnz > 0x7fffffffLL) { set_error("nnz %lld out of range", nnz); return -2; }
+  const size_t need = usbs_eigsh_workspace_bytes(n, nnz, inner_iterations, precision);
+  if (!workspace || workspace_bytes < need) {
+    set_error("eigsh: workspace of %zu bytes given, %zu needed", workspace_bytes, need);
+    return -2;
+  }
+  DeviceInfo di;
+  int rc = get_device_info(&di);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int vt = (precision == 64) ? 8 : 4;
+  char* w = (char*)workspace;
+  void* op_val = w; w += a256((size_t)(nnz > 0 ? nnz : 1) * vt);
+  double* alpha = (double*)w;
+  double* beta = alpha + MAXM;
+  w += a256(2 * MAXM * sizeof(double));
+  rc = assemble_operator((int)nnz, c_val, c_scale, slot_ptr, slot_tid, t_con, t_a, adjoint_left_vec,
+                         op_val, precision, st);
+  if (rc) return rc;
+  if (cudaMemcpyAsync(Q, q0, (size_t)n * vt, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+      cudaMemsetAsync(alpha, 0, 2 * MAXM * sizeof(double), st) != cudaSuccess) {
+    set_error("eigsh: staging copy failed");
+    return -5;
+  }
+  LanczosProblem p;
+  p.n = n; p.ld = ldq; p.m = inner_iterations; p.num_desired = num_desired;
+  p.max_restarts = max_restarts; p.nnz = nnz; p.tol = tolerance;
+  p.rowptr = rowptr; p.col = col; p.val = op_val; p.Q = Q;
+  p.alpha = alpha; p.beta = beta; p.ctl = info; p.status = info + 5; p.work = w;
+  rc = lanczos_run(di, &p, 1, precision, st);
+  if (rc) return rc;
+  if (cudaMemcpyAsync(eigenvalues, alpha, (size_t)num_desired * sizeof(double),
+                      cudaMemcpyDeviceToDevice, st) != cudaSuccess) {
+    set_error("eigsh: result copy failed");
+    return -5;
+  }
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,262 @@
+// Small dense FP64 linear algebra executed by one warp or one CTA in shared
+// memory: the projected Lanczos eigenproblem (m <= 32), the k x k bundle
+// matrices (k <= 16) and the s x s IPM Newton systems (s <= 136).
+//
+// Methods (textbook, own code):
+//  * symmetric eigensolver: Householder tridiagonalisation followed by the
+//    implicit symmetric QR iteration with Wilkinson shift (Golub & Van Loan,
+//    Matrix Computations, 4th ed., Alg. 8.3.1 and 8.3.3), eigenvectors
+//    accumulated, eigenvalues sorted ascending;
+//  * LU with partial pivoting and forward/back substitution (G&VL Alg. 3.4.1);
+//  * Cholesky (G&VL Alg. 4.2.1) as the positive-definiteness test.
+#pragma once
+#include "common.cuh"
+
+namespace usbs {
+
+// Eigen-decomposition of the symmetric n x n matrix A (row-major, lda) by one
+// warp.  On return w[0..n-1] holds the eigenvalues in ascending order and
+// Z (row-major, ldz) the eigenvectors as columns.  A is destroyed.  Returns
+// false if the QR iteration did not converge in 30 n sweeps.  n <= 32.
+__device__ bool warp_syev(double* A, int lda, int n, double* w, double* Z, int ldz) {
+  const int lane = threadIdx.x & 31;
+  // Z = I
+  for (int j = 0; j < n; ++j)
+    if (lane < n) Z[lane * ldz + j] = (lane == j) ? 1.0 : 0.0;
+  __syncwarp();
+  // ---- Householder tridiagonalisation: A <- H A H, Z <- Z H ----
+  for (int j = 0; j + 2 < n; ++j) {
+    const int r0 = j + 1;  // reflector acts on rows/cols r0..n-1
+    double xi = (lane > r0 && lane < n) ? A[lane * lda + j] : 0.0;
+    double sigma = warp_sum(xi * xi);
+    double alpha = A[r0 * lda + j];
+    if (sigma == 0.0) continue;  // already tridiagonal in this column
+    double nrm = sqrt(alpha * alpha + sigma);
+    double v0 = (alpha <= 0.0) ? (alpha - nrm) : (-sigma / (alpha + nrm));
+    double beta = 2.0 * v0 * v0 / (sigma + v0 * v0);
+    // v (length n, zero outside r0..n-1), v[r0] = 1
+    double vi = (lane == r0) ? 1.0 : ((lane > r0 && lane < n) ? xi / v0 : 0.0);
+    // p = beta * A_sub v  (lane i computes component i); every lane shuffles
+    double p = 0.0;
+    for (int l = r0; l < n; ++l) {
+      double vl = __shfl_sync(0xffffffffu, vi, l);
+      if (lane >= r0 && lane < n) p += A[lane * lda + l] * vl;
+    }
+    p *= beta;
+    double K = 0.5 * beta * warp_sum(p * vi);
+    double wv = p - K * vi;
+    __syncwarp();
+    // A_sub -= v w^T + w v^T
+    for (int l = r0; l < n; ++l) {
+      double vl = __shfl_sync(0xffffffffu, vi, l);
+      double wl = __shfl_sync(0xffffffffu, wv, l);
+      if (lane >= r0 && lane < n) A[lane * lda + l] -= vi * wl + wv * vl;
+    }
+    __syncwarp();
+    if (lane == r0) { A[r0 * lda + j] = nrm; A[j * lda + r0] = nrm; }
+    if (lane > r0 && lane < n) { A[lane * lda + j] = 0.0; A[j * lda + lane] = 0.0; }
+    // Z <- Z (I - beta v v^T): row i of Z: z_i -= beta (z_i . v) v^T
+    for (int i = 0; i < n; ++i) {
+      double zv = warp_sum((lane < n) ? Z[i * ldz + lane] * vi : 0.0);
+      if (lane < n) Z[i * ldz + lane] -= beta * zv * vi;
+    }
+    __syncwarp();
+  }
+  // ---- implicit symmetric QR with Wilkinson shift on (d, e) ----
+  // d/e held redundantly by all lanes in registers would need dynamic indexing;
+  // keep them in A's diagonal / subdiagonal (shared memory), lane 0 writes.
+  double* d = w;                 // eigenvalues end up here
+  for (int i = lane; i < n; i += 32) d[i] = A[i * lda + i];
+  __syncwarp();
+  // subdiagonal e[i] = A[i+1][i] stored in A[(i+1)*lda + i]
+  const double eps = 1.1102230246251565e-16;
+  int iters = 0, maxit = 30 * n;
+  int hi = n - 1;
+  while (hi > 0) {
+    // deflate the trailing off-diagonal if negligible
+    {
+      double e = A[hi * lda + hi - 1];
+      if (fabs(e) <= eps * (fabs(d[hi - 1]) + fabs(d[hi])) || fabs(e) < 1e-300) {
+        __syncwarp();
+        if (lane == 0) A[hi * lda + hi - 1] = 0.0;
+        __syncwarp();
+        --hi;
+        continue;
+      }
+    }
+    // start p of the unreduced block ending at hi
+    int p = hi - 1;
+    while (p > 0) {
+      double e = A[p * lda + p - 1];
+      if (fabs(e) <= eps * (fabs(d[p - 1]) + fabs(d[p])) || fabs(e) < 1e-300) {
+        __syncwarp();
+        if (lane == 0) A[p * lda + p - 1] = 0.0;
+        __syncwarp();
+        break;
+      }
+      --p;
+    }
+    if (++iters > maxit) return false;
+    // Wilkinson shift from the trailing 2x2
+    double a1 = d[hi - 1], a2 = d[hi], b = A[hi * lda + hi - 1];
+    double dd = 0.5 * (a1 - a2);
+    double den = dd + copysign(hypot(dd, b), dd == 0.0 ? 1.0 : dd);
+    double mu = a2 - b * b / den;
+    double x = d[p] - mu, z = A[(p + 1) * lda + p];
+    for (int k = p; k < hi; ++k) {
+      double r = hypot(x, z);
+      double c = (r == 0.0) ? 1.0 : x / r;
+      double s = (r == 0.0) ? 0.0 : z / r;
+      double ak = d[k], ak1 = d[k + 1], bk = A[(k + 1) * lda + k];
+      double f = (k + 1 < hi) ? A[(k + 2) * lda + k + 1] : 0.0;
+      // new 2x2 block
+      double nak = c * c * ak + 2.0 * c * s * bk + s * s * ak1;
+      double nak1 = s * s * ak - 2.0 * c * s * bk + c * c * ak1;
+      double nbk = c * s * (ak1 - ak) + (c * c - s * s) * bk;
+      __syncwarp();
+      if (lane == 0) {
+        if (k > p) A[k * lda + k - 1] = r;   // e[k-1] after removing the bulge
+        d[k] = nak;
+        d[k + 1] = nak1;
+        A[(k + 1) * lda + k] = nbk;
+        if (k + 1 < hi) A[(k + 2) * lda + k + 1] = c * f;
+      }
+      // rotate eigenvector columns k, k+1: (Z P^T)
+      if (lane < n) {
+        double zk = Z[lane * ldz + k], zk1 = Z[lane * ldz + k + 1];
+        Z[lane * ldz + k] = c * zk + s * zk1;
+        Z[lane * ldz + k + 1] = -s * zk + c * zk1;
+      }
+      __syncwarp();
+      if (k + 1 < hi) { x = nbk; z = s * f; }
+    }
+  }
+  __syncwarp();
+  // sort ascending (selection sort, swap columns of Z)
+  for (int i = 0; i < n - 1; ++i) {
+    int kmin = i;
+    double vmin = d[i];
+    for (int j = i + 1; j < n; ++j)
+      if (d[j] < vmin) { vmin = d[j]; kmin = j; }
+    if (kmin != i) {
+      __syncwarp();
+      double di = d[i];
+      if (lane < n) {
+        double t = Z[lane * ldz + i];
+        Z[lane * ldz + i] = Z[lane * ldz + kmin];
+        Z[lane * ldz + kmin] = t;
+      }
+      if (lane == 0) { d[kmin] = di; d[i] = vmin; }
+      __syncwarp();
+    }
+  }
+  return true;
+}
+
+// Solve A x = b (n x n, row-major lda, in shared memory) by LU with partial
+// pivoting, executed by the whole CTA.  A and b are destroyed; x overwrites b.
+// `red` needs >= 2*blockDim/32 doubles and ints for the pivot search.
+// Returns false (uniformly) if a pivot is exactly zero.
+__device__ bool block_lu_solve(double* A, int lda, double* b, int n, double* redv, int* redi) {
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5;
+  const int nw = nt >> 5;
+  __shared__ int s_piv;
+  __shared__ int s_ok;
+  if (tid == 0) s_ok = 1;
+  for (int j = 0; j < n; ++j) {
+    // pivot search over rows j..n-1 of column j
+    double best = -1.0;
+    int bi = j;
+    for (int i = j + tid; i < n; i += nt) {
+      double a = fabs(A[i * lda + j]);
+      if (a > best) { best = a; bi = i; }
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      double ob = __shfl_xor_sync(0xffffffffu, best, o);
+      int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+    }
+    if (lane == 0) { redv[wid] = best; redi[wid] = bi; }
+    __syncthreads();
+    if (tid == 0) {
+      double bb = redv[0];
+      int ii = redi[0];
+      for (int w2 = 1; w2 < nw; ++w2)
+        if (redv[w2] > bb || (redv[w2] == bb && redi[w2] < ii)) { bb = redv[w2]; ii = redi[w2]; }
+      s_piv = ii;
+      if (bb == 0.0) s_ok = 0;
+    }
+    __syncthreads();
+    const int piv = s_piv;
+    if (piv != j) {
+      for (int c = tid; c < n; c += nt) {
+        double t = A[j * lda + c];
+        A[j * lda + c] = A[piv * lda + c];
+        A[piv * lda + c] = t;
+      }
+      if (tid == 0) { double t = b[j]; b[j] = b[piv]; b[piv] = t; }
+      __syncthreads();
+    }
+    const double inv = 1.0 / A[j * lda + j];
+    // multipliers (column j below the diagonal)
+    for (int i = j + 1 + tid; i < n; i += nt) A[i * lda + j] *= inv;
+    __syncthreads();
+    const int rows = n - j - 1, cols = n - j - 1;
+    for (int e = tid; e < rows * cols; e += nt) {
+      int i = j + 1 + e / cols, c = j + 1 + e % cols;
+      A[i * lda + c] -= A[i * lda + j] * A[j * lda + c];
+    }
+    for (int i = j + 1 + tid; i < n; i += nt) b[i] -= A[i * lda + j] * b[j];
+    __syncthreads();
+  }
+  // back substitution (column oriented)
+  for (int j = n - 1; j >= 0; --j) {
+    if (tid == 0) b[j] = b[j] / A[j * lda + j];
+    __syncthreads();
+    for (int i = tid; i < j; i += nt) b[i] -= A[i * lda + j] * b[j];
+    __syncthreads();
+  }
+  return s_ok != 0;
+}
+
+// Inverse of the n x n matrix A (row-major lda) by one warp: Gauss-Jordan with
+// partial pivoting.  Ainv (row-major ldi) receives the result; A is destroyed.
+__device__ bool warp_inverse(double* A, int lda, int n, double* Ainv, int ldi) {
+  const int lane = threadIdx.x & 31;
+  for (int i = 0; i < n; ++i)
+    if (lane < n) Ainv[i * ldi + lane] = (i == lane) ? 1.0 : 0.0;
+  __syncwarp();
+  bool ok = true;
+  for (int j = 0; j < n; ++j) {
+    double best = -1.0;
+    int bi = j;
+    for (int i = j; i < n; ++i) {
+      double a = fabs(A[i * lda + j]);
+      if (a > best) { best = a; bi = i; }
+    }
+    if (best == 0.0) ok = false;
+    if (bi != j && lane < n) {
+      double t = A[j * lda + lane]; A[j * lda + lane] = A[bi * lda + lane]; A[bi * lda + lane] = t;
+      t = Ainv[j * ldi + lane]; Ainv[j * ldi + lane] = Ainv[bi * ldi + lane];
+      Ainv[bi * ldi + lane] = t;
+    }
+    __syncwarp();
+    double inv = 1.0 / A[j * lda + j];
+    __syncwarp();
+    if (lane < n) { A[j * lda + lane] *= inv; Ainv[j * ldi + lane] *= inv; }
+    __syncwarp();
+    for (int i = 0; i < n; ++i) {
+      if (i == j) continue;
+      double f = A[i * lda + j];
+      __syncwarp();
+      if (lane < n) {
+        A[i * lda + lane] -= f * A[j * lda + lane];
+        Ainv[i * ldi + lane] -= f * Ainv[j * ldi + lane];
+      }
+      __syncwarp();
+    }
+  }
+  return ok;
+}
+
+}  // namespace usbs

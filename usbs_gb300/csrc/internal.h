@@ -1,0 +1,63 @@
+// Host-side declarations shared by the translation units of libusbs_gb300.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace usbs {
+
+// Device properties cached per device.
+struct DeviceInfo {
+  int device = -1;
+  int sm_count = 0;
+  int lanczos_occ64 = 0;   // co-resident Lanczos CTAs per SM (FP64)
+  int lanczos_occ32 = 0;   // co-resident Lanczos CTAs per SM (FP32)
+};
+int get_device_info(DeviceInfo* out);
+
+void set_error(const char* fmt, ...);
+
+// ---------------------------------------------------------------- Lanczos
+// One eigsh_smallest problem on the device.  Q[:, 0] must hold the unit start
+// vector.  `prec` 64 (double storage/arithmetic) or 32 (float storage, FP32
+// dot products, FP64 team reductions and FP64 projected eigensolve).
+struct LanczosProblem {
+  int n, ld, m, num_desired, max_restarts;
+  long long nnz;
+  double tol;
+  const int* rowptr;
+  const int* col;
+  const void* val;      // assembled operator values (double or float)
+  void* Q;              // ld x (m+1), column-major
+  double* alpha;        // m: Ritz values (alpha_hat) after the last restart
+  double* beta;         // m
+  int* ctl;             // 8 ints: k_next, nconv, restarts, breakdowns, steps
+  int* status;
+  void* work;           // workspace of lanczos_workspace_bytes()
+};
+size_t lanczos_workspace_bytes(int n, int ld, int m, int prec, int nctas);
+int lanczos_team_size(const DeviceInfo& di, int n, int prec);
+int lanczos_lanes(int n, long long nnz);
+int lanczos_occupancy(int prec);
+// Runs `count` independent problems in one cooperative launch (one team each).
+int lanczos_run(const DeviceInfo& di, const LanczosProblem* probs, int count, int prec,
+                cudaStream_t stream);
+
+// ---------------------------------------------------------------- operators
+// op_val[p] = alpha_c * c_val[p] + sum_{t in slot p} a[t] * w[con[t]]
+int assemble_operator(int nnz, const double* c_val, double alpha_c, const int* slot_ptr,
+                      const int* slot_tid, const int* con, const double* a, const double* w,
+                      void* op_val, int prec, cudaStream_t stream);
+// y = M x  for CSR M (values double or float), optional per-row partial dots
+int csr_spmv(int n, long long nnz, const int* rowptr, const int* col, const void* val,
+             const void* x, void* y, int prec, int sm_count, cudaStream_t stream);
+// out[c] += sum over triples of constraint c: a * u[i] . u[j]   (k columns, ld)
+int apply_A_operator(int m, const int* con_ptr, const int* t_row, const int* t_col,
+                     const double* a, const double* U, int ldu, int k, double* out,
+                     cudaStream_t stream);
+// out[i, :] = sum over triples with row i: a * z[con] * U[j, :]
+int apply_A_adjoint(int n, const int* row_ptr, const int* r_con, const int* r_col,
+                    const double* r_a, const double* z, const double* U, int ldu, int k,
+                    double* out, int ldo, cudaStream_t stream);
+
+}  // namespace usbs

@@ -1,0 +1,567 @@
+// Thick-restart Lanczos (smallest eigenpairs) as one cooperative launch.
+//
+// Reference: solver/lanczos.py:80-236 (restart loop, CGS2 full
+// reorthogonalisation, arrowhead projected matrix, gap-ratio restart choice).
+//
+// Layout and schedule.  The CTAs of the launch are split into teams, one team
+// per problem.  A team owns a contiguous range of 256-row tiles of its problem;
+// every phase below walks the same tiles, so a CTA only ever reads and writes
+// its own rows of Q and of the work vectors, except for the SpMV gathers of x
+// (read through L2 with ld.global.cg after a team barrier).  One Lanczos step i
+// is three phases separated by team barriers:
+//   A  y = Op x  (CSR, `lanes` threads per row) fused with h1 = Q[:, :i+1]^T y
+//   B  q1 = y - Q h1, fused with h2 = Q^T q1
+//   C  q2 = q1 - Q h2, fused with ||q2||^2
+// The normalisation q2 / beta is folded into the next phase A (x = v * 1/beta),
+// which also stores Q[:, i+1] for its rows.  Partial sums go to a per-team
+// [pass][cta][column] buffer and every CTA reduces them in the same fixed order,
+// so all CTAs hold bit-identical alpha/beta and take identical branches.
+// At a restart CTA 0 builds the arrowhead matrix and runs the FP64 warp
+// eigensolver; after a barrier every CTA rotates its rows of Q by the saved
+// Ritz vectors.
+#include <vector>
+#include "common.cuh"
+#include "dense.cuh"
+#include "internal.h"
+
+namespace usbs {
+
+constexpr int LZ_BLOCK = 256;
+constexpr int LZ_NW = LZ_BLOCK / 32;
+constexpr int MAX_TEAMS = 48;
+constexpr int MP1 = MAXM + 1;
+
+template <typename VT>
+struct TeamDesc {
+  int n, ld, m, num_desired, max_restarts, lanes, first_cta, nctas;
+  double tol;
+  const int* rowptr;
+  const int* col;
+  const VT* val;
+  VT* Q;
+  VT* vbuf;
+  double* part;
+  double* Ybuf;
+  double* alpha;
+  double* beta;
+  int* ctl;
+  unsigned int* bar;
+  int* status;
+};
+
+template <typename VT>
+struct TeamBatch {
+  int count;
+  TeamDesc<VT> t[MAX_TEAMS];
+};
+
+template <typename VT>
+struct LzShared {
+  double ys[LZ_BLOCK];
+  double wred[LZ_NW][MP1];
+  double h[MP1];
+  double alpha[MAXM];
+  double beta[MAXM];
+  double T[MAXM * MP1];
+  double Z[MAXM * MP1];
+  double ritz[MAXM];
+  VT Ys[MAXM * MAXM];
+  int order[MAXM];
+  int k_next, nconv;
+};
+
+// acc[c] (c < nv) summed over the CTA, written to out[c]
+template <typename VT, typename AT>
+__device__ __forceinline__ void block_reduce_cols(const AT* acc, int nv, LzShared<VT>& sh,
+                                                  double* out) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int c = 0; c < MP1; ++c) {
+    if (c < nv) {
+      double v = warp_sum((double)acc[c]);
+      if (lane == 0) sh.wred[wid][c] = v;
+    }
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) {
+    double s = 0.0;
+#pragma unroll
+    for (int w = 0; w < LZ_NW; ++w) s += sh.wred[w][c];
+    out[c] = s;
+  }
+}
+
+// h[c] = sum over the team's CTAs of part_pass[r][c], identical order in every CTA
+template <typename VT>
+__device__ __forceinline__ void reduce_part(const double* part_pass, int R, int nv,
+                                            LzShared<VT>& sh) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int c = wid; c < nv; c += LZ_NW) {
+    double s = 0.0;
+    for (int r = lane; r < R; r += 32) s += __ldcg(part_pass + (size_t)r * MP1 + c);
+    s = warp_sum(s);
+    if (lane == 0) sh.h[c] = s;
+  }
+  __syncthreads();
+}
+
+// Phase A: y = Op (xsrc * xscale) for own rows -> vout, acc[c] = Q[:, c] . y (c <= i).
+// If wq, also stores Q[:, i] = xsrc * xscale for own rows.
+template <typename VT>
+__device__ void phase_spmv(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0, int t1, int i,
+                           const VT* xsrc, VT xscale, bool wq, VT* vout, double* part_out) {
+  typedef typename Acc<VT>::type AT;
+  AT acc[MP1];
+#pragma unroll
+  for (int c = 0; c < MP1; ++c) acc[c] = (AT)0;
+  const int tid = threadIdx.x, L = P.lanes, gpp = LZ_BLOCK / L;
+  const int g = tid / L, lig = tid - g * L;
+  const size_t ld = (size_t)P.ld;
+  for (int tile = t0; tile < t1; ++tile) {
+    const int base = tile * LZ_BLOCK;
+    for (int pass = 0; pass < L; ++pass) {
+      const int rl = pass * gpp + g;
+      const int row = base + rl;
+      AT s = (AT)0;
+      if (row < P.n) {
+        const int pe = P.rowptr[row + 1];
+        for (int p = P.rowptr[row] + lig; p < pe; p += L)
+          s += (AT)P.val[p] * (AT)__ldcg(xsrc + P.col[p]);
+      }
+      for (int o = L >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lig == 0) sh.ys[rl] = (double)s;
+    }
+    __syncthreads();
+    const int row = base + tid;
+    if (row < P.n) {
+      const VT y = (VT)sh.ys[tid] * xscale;
+      vout[row] = y;
+      VT xn = (VT)0;
+      if (wq) {
+        xn = __ldcg(xsrc + row) * xscale;
+        P.Q[(size_t)i * ld + row] = xn;
+      }
+#pragma unroll
+      for (int c = 0; c < MP1; ++c) {
+        if (c <= i) {
+          const VT qc = (wq && c == i) ? xn : P.Q[(size_t)c * ld + row];
+          acc[c] += (AT)qc * (AT)y;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  block_reduce_cols(acc, i + 1, sh, part_out);
+}
+
+// Breakdown pass a: buf = hash_normal(key) for own rows, acc[c] = Q[:, c] . buf (c < nv)
+template <typename VT>
+__device__ void phase_random(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0, int t1, int nv,
+                             uint64_t key, VT* buf, double* part_out) {
+  typedef typename Acc<VT>::type AT;
+  AT acc[MP1];
+#pragma unroll
+  for (int c = 0; c < MP1; ++c) acc[c] = (AT)0;
+  const size_t ld = (size_t)P.ld;
+  for (int tile = t0; tile < t1; ++tile) {
+    const int row = tile * LZ_BLOCK + threadIdx.x;
+    if (row < P.n) {
+      const VT r = (VT)hash_normal(key, (uint64_t)row);
+      buf[row] = r;
+#pragma unroll
+      for (int c = 0; c < MP1; ++c)
+        if (c < nv) acc[c] += (AT)P.Q[(size_t)c * ld + row] * (AT)r;
+    }
+  }
+  block_reduce_cols(acc, nv, sh, part_out);
+}
+
+// Phase B: buf -= Q h (c < nv); acc[c] = Q[:, c] . buf
+template <typename VT>
+__device__ void phase_update_dot(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0, int t1, int nv,
+                                 VT* buf, double* part_out) {
+  typedef typename Acc<VT>::type AT;
+  AT acc[MP1];
+#pragma unroll
+  for (int c = 0; c < MP1; ++c) acc[c] = (AT)0;
+  const size_t ld = (size_t)P.ld;
+  for (int tile = t0; tile < t1; ++tile) {
+    const int row = tile * LZ_BLOCK + threadIdx.x;
+    if (row < P.n) {
+      VT qr[MP1];
+      VT s = (VT)0;
+#pragma unroll
+      for (int c = 0; c < MP1; ++c) {
+        if (c < nv) {
+          qr[c] = P.Q[(size_t)c * ld + row];
+          s += qr[c] * (VT)sh.h[c];
+        }
+      }
+      const VT q1 = buf[row] - s;
+      buf[row] = q1;
+#pragma unroll
+      for (int c = 0; c < MP1; ++c)
+        if (c < nv) acc[c] += (AT)qr[c] * (AT)q1;
+    }
+  }
+  block_reduce_cols(acc, nv, sh, part_out);
+}
+
+// Phase C: buf -= Q h (c < nv); part_out[0] = sum buf^2 over own rows
+template <typename VT>
+__device__ void phase_update_norm(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0, int t1, int nv,
+                                  VT* buf, double* part_out) {
+  typedef typename Acc<VT>::type AT;
+  AT nrm = (AT)0;
+  const size_t ld = (size_t)P.ld;
+  for (int tile = t0; tile < t1; ++tile) {
+    const int row = tile * LZ_BLOCK + threadIdx.x;
+    if (row < P.n) {
+      VT s = (VT)0;
+#pragma unroll
+      for (int c = 0; c < MP1; ++c)
+        if (c < nv) s += P.Q[(size_t)c * ld + row] * (VT)sh.h[c];
+      const VT q2 = buf[row] - s;
+      buf[row] = q2;
+      nrm += (AT)q2 * (AT)q2;
+    }
+  }
+  AT one[MP1];
+  one[0] = nrm;
+  block_reduce_cols(one, 1, sh, part_out);
+}
+
+// CTA 0 of a team: projected eigenproblem and thick-restart selection
+// (solver/lanczos.py:128-168, 202-221).  k = number of saved vectors of the
+// finished cycle, beta_last = beta[m-1].
+template <typename VT>
+__device__ void restart_select(const TeamDesc<VT>& P, LzShared<VT>& sh, int k) {
+  const int m = P.m, tid = threadIdx.x;
+  for (int e = tid; e < m * m; e += LZ_BLOCK) {
+    const int r = e / m, c = e - r * m;
+    double v = 0.0;
+    if (r == c) v = sh.alpha[r];
+    else if (c == k && r < k) v = sh.beta[r];
+    else if (r == k && c < k) v = sh.beta[c];
+    else if (c == r + 1 && r >= k) v = sh.beta[r];
+    else if (r == c + 1 && c >= k) v = sh.beta[c];
+    sh.T[r * MP1 + c] = v;
+  }
+  __syncthreads();
+  if (tid < 32) {
+    bool ok = warp_syev(sh.T, MP1, m, sh.ritz, sh.Z, MP1);
+    if (!ok && tid == 0) atomicOr(P.status, ST_SMALL_DENSE_FAIL);
+  }
+  __syncthreads();
+  if (tid == 0) {
+    const double bl = sh.beta[m - 1];
+    int nconv = m;
+    for (int c = 0; c < m; ++c) {
+      if (!(bl * fabs(sh.Z[(m - 1) * MP1 + c]) < P.tol)) { nconv = c; break; }
+    }
+    const int delta = min(m - P.num_desired, 2 * (m - nconv) / 5);
+    const double lt = sh.ritz[min(nconv, m - 1)];
+    int kl = 0;
+    double bv = 0.0;
+    for (int c = 0; c < m; ++c) {
+      const int kr = c + delta;
+      double g = 0.0;
+      if (kr <= m) g = (sh.ritz[c] - lt) / (sh.ritz[min(kr, m - 1)] - lt);
+      if (c == 0) { bv = g; kl = 0; if (isnan(g)) break; continue; }
+      if (isnan(g)) { kl = c; break; }
+      if (g > bv) { bv = g; kl = c; }
+    }
+    const int kright = kl + delta;
+    int kn = 0;
+    for (int c = 0; c < m; ++c)
+      if (kl >= c || kright < c) sh.order[kn++] = c;
+    int pos = kn;
+    for (int c = 0; c < m; ++c)
+      if (!(kl >= c || kright < c)) sh.order[pos++] = c;
+    sh.k_next = kn;
+    sh.nconv = nconv;
+  }
+  __syncthreads();
+  const int kn = sh.k_next;
+  const double bl = sh.beta[m - 1];
+  for (int e = tid; e < m * m; e += LZ_BLOCK) {
+    const int j = e / m, c = e - j * m;
+    P.Ybuf[j * m + c] = sh.Z[j * MP1 + sh.order[c]];
+  }
+  __syncthreads();
+  if (tid < m) {
+    const int c = tid;
+    const double a = (c < kn) ? sh.ritz[sh.order[c]] : 0.0;
+    const double b = (c < kn) ? bl * sh.Z[(m - 1) * MP1 + sh.order[c]] : 0.0;
+    sh.alpha[c] = a;
+    sh.beta[c] = b;
+    P.alpha[c] = a;
+    P.beta[c] = b;
+  }
+  if (tid == 0) {
+    P.ctl[0] = kn;
+    P.ctl[1] = sh.nconv;
+  }
+}
+
+template <typename VT>
+__global__ void __launch_bounds__(LZ_BLOCK)
+lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
+  __shared__ LzShared<VT> sh;
+  int team = 0;
+  for (int t = 1; t < batch.count; ++t)
+    if ((int)blockIdx.x >= batch.t[t].first_cta) team = t;
+  const TeamDesc<VT>& P = batch.t[team];
+  const int rank = (int)blockIdx.x - P.first_cta, R = P.nctas;
+  const int tid = threadIdx.x;
+  TeamBarrier bar{P.bar, R, P.status};
+  const int n = P.n, m = P.m;
+  const size_t ld = (size_t)P.ld;
+  const int ntiles = (n + LZ_BLOCK - 1) / LZ_BLOCK;
+  const int t0 = (int)((long long)ntiles * rank / R);
+  const int t1 = (int)((long long)ntiles * (rank + 1) / R);
+  double* part0 = P.part;
+  double* part1 = P.part + (size_t)R * MP1;
+  double* part2 = P.part + (size_t)2 * R * MP1;
+
+  int k = 0, nconv = 0, restart = 0, breakdowns = 0, steps = 0;
+  if (rank == 0 && tid < MAXM) { sh.alpha[tid] = 0.0; sh.beta[tid] = 0.0; }
+  __syncthreads();
+  int prev = 0;          // vbuf slot holding the latest unnormalised vector
+  VT invb = (VT)1;       // its normalisation
+  while (nconv < P.num_desired && restart < P.max_restarts) {
+    int cur = 0;
+    for (int i = k; i < m; ++i) {
+      const VT* xsrc;
+      bool wq;
+      if (i == k) {
+        xsrc = P.Q + (size_t)k * ld;
+        invb = (VT)1;
+        wq = false;
+      } else {
+        reduce_part(part2, R, 1, sh);
+        const double b = sqrt(sh.h[0]);
+        if (rank == 0 && tid == 0) sh.beta[i - 1] = b;
+        if (b < 1e-15) {
+          // Krylov space exhausted: random vector orthogonalised twice
+          // against Q[:, :i] (solver/lanczos.py:107-117)
+          ++breakdowns;
+          VT* buf = P.vbuf + (size_t)prev * ld;
+          phase_random(P, sh, t0, t1, i, (uint64_t)i, buf, part0 + (size_t)rank * MP1);
+          if (!bar.sync()) return;
+          reduce_part(part0, R, i, sh);
+          phase_update_dot(P, sh, t0, t1, i, buf, part1 + (size_t)rank * MP1);
+          if (!bar.sync()) return;
+          reduce_part(part1, R, i, sh);
+          phase_update_norm(P, sh, t0, t1, i, buf, part2 + (size_t)rank * MP1);
+          if (!bar.sync()) return;
+          reduce_part(part2, R, 1, sh);
+          invb = (VT)(1.0 / sqrt(sh.h[0]));
+        } else {
+          invb = (VT)(1.0 / b);
+        }
+        xsrc = P.vbuf + (size_t)prev * ld;
+        wq = true;
+      }
+      VT* vout = P.vbuf + (size_t)cur * ld;
+      phase_spmv(P, sh, t0, t1, i, xsrc, invb, wq, vout, part0 + (size_t)rank * MP1);
+      if (!bar.sync()) return;
+      reduce_part(part0, R, i + 1, sh);
+      const double h1i = sh.h[i];
+      phase_update_dot(P, sh, t0, t1, i + 1, vout, part1 + (size_t)rank * MP1);
+      if (!bar.sync()) return;
+      reduce_part(part1, R, i + 1, sh);
+      if (rank == 0 && tid == 0) sh.alpha[i] = h1i + sh.h[i];
+      phase_update_norm(P, sh, t0, t1, i + 1, vout, part2 + (size_t)rank * MP1);
+      if (!bar.sync()) return;
+      prev = cur;
+      cur ^= 1;
+      ++steps;
+    }
+    // ---- restart ----
+    const bool stepped = (k < m);
+    if (stepped) {
+      reduce_part(part2, R, 1, sh);
+      const double b = sqrt(sh.h[0]);
+      if (rank == 0 && tid == 0) sh.beta[m - 1] = b;
+      if (b < 1e-15) {
+        ++breakdowns;
+        VT* buf = P.vbuf + (size_t)prev * ld;
+        phase_random(P, sh, t0, t1, m, (uint64_t)m, buf, part0 + (size_t)rank * MP1);
+        if (!bar.sync()) return;
+        reduce_part(part0, R, m, sh);
+        phase_update_dot(P, sh, t0, t1, m, buf, part1 + (size_t)rank * MP1);
+        if (!bar.sync()) return;
+        reduce_part(part1, R, m, sh);
+        phase_update_norm(P, sh, t0, t1, m, buf, part2 + (size_t)rank * MP1);
+        if (!bar.sync()) return;
+        reduce_part(part2, R, 1, sh);
+        invb = (VT)(1.0 / sqrt(sh.h[0]));
+      } else {
+        invb = (VT)(1.0 / b);
+      }
+    }
+    __syncthreads();
+    if (rank == 0) restart_select(P, sh, k);
+    if (!bar.sync()) return;
+    const int kn = __ldcg(P.ctl + 0);
+    nconv = __ldcg(P.ctl + 1);
+    for (int e = tid; e < m * MAXM; e += LZ_BLOCK) {
+      const int j = e / MAXM, c = e - j * MAXM;
+      sh.Ys[e] = (c < kn) ? (VT)__ldcg(P.Ybuf + j * m + c) : (VT)0;
+    }
+    __syncthreads();
+    const VT* last = stepped ? (P.vbuf + (size_t)prev * ld) : (P.Q + (size_t)m * ld);
+    const VT lscale = stepped ? invb : (VT)1;
+    for (int tile = t0; tile < t1; ++tile) {
+      const int row = tile * LZ_BLOCK + tid;
+      if (row < n) {
+        VT qr[MAXM];
+#pragma unroll
+        for (int j = 0; j < MAXM; ++j) qr[j] = (j < m) ? P.Q[(size_t)j * ld + row] : (VT)0;
+        const VT xl = last[row] * lscale;
+        for (int c = 0; c < kn; ++c) {
+          if (c >= m) break;
+          VT s = (VT)0;
+#pragma unroll
+          for (int j = 0; j < MAXM; ++j)
+            if (j < m) s += qr[j] * sh.Ys[j * MAXM + c];
+          P.Q[(size_t)c * ld + row] = s;
+        }
+        P.Q[(size_t)kn * ld + row] = xl;
+        if (kn != m) P.Q[(size_t)m * ld + row] = xl;
+      }
+    }
+    k = kn;
+    ++restart;
+    if (!bar.sync()) return;
+  }
+  if (rank == 0 && tid == 0) {
+    P.ctl[2] = restart;
+    P.ctl[3] = breakdowns;
+    P.ctl[4] = steps;
+    if (restart == 0) P.ctl[0] = 0;
+  }
+}
+
+// ---------------------------------------------------------------- host side
+
+static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+
+size_t lanczos_workspace_bytes(int n, int ld, int m, int prec, int nctas) {
+  (void)n; (void)m;
+  const size_t vt = (prec == 64) ? 8 : 4;
+  size_t b = align256(2 * (size_t)ld * vt);
+  b += align256((size_t)3 * nctas * MP1 * sizeof(double));
+  b += align256((size_t)MAXM * MAXM * sizeof(double));
+  b += 256;  // barrier counters
+  return b;
+}
+
+int lanczos_lanes(int n, long long nnz) {
+  const double avg = n > 0 ? (double)nnz / n : 1.0;
+  int L = 1;
+  while (L < 32 && L * 2 <= avg * 0.75 + 1) L *= 2;
+  return L;
+}
+
+int lanczos_team_size(const DeviceInfo& di, int n, int prec) {
+  const int occ = (prec == 64) ? di.lanczos_occ64 : di.lanczos_occ32;
+  const int maxc = di.sm_count * (occ > 0 ? occ : 1);
+  const int tiles = (n + LZ_BLOCK - 1) / LZ_BLOCK;
+  // a few tiles per CTA keeps the barrier population small for mid sizes
+  int want = tiles;
+  if (want > maxc) want = maxc;
+  if (want < 1) want = 1;
+  return want;
+}
+
+template <typename VT>
+static int run_typed(const DeviceInfo& di, const LanczosProblem* probs, int count,
+                     cudaStream_t stream) {
+  const int occ = (sizeof(VT) == 8) ? di.lanczos_occ64 : di.lanczos_occ32;
+  const int maxc = di.sm_count * (occ > 0 ? occ : 1);
+  for (int base = 0; base < count; base += MAX_TEAMS) {
+    const int cnt = (count - base < MAX_TEAMS) ? (count - base) : MAX_TEAMS;
+    TeamBatch<VT> batch;
+    batch.count = cnt;
+    int total = 0;
+    std::vector<int> want(cnt);
+    for (int i = 0; i < cnt; ++i) {
+      want[i] = lanczos_team_size(di, probs[base + i].n, sizeof(VT) == 8 ? 64 : 32);
+      total += want[i];
+    }
+    if (total > maxc) {
+      // shrink teams proportionally so that every CTA is co-resident
+      int tot2 = 0;
+      for (int i = 0; i < cnt; ++i) {
+        want[i] = (int)((long long)want[i] * maxc / total);
+        if (want[i] < 1) want[i] = 1;
+        tot2 += want[i];
+      }
+      if (tot2 > maxc) {
+        set_error("lanczos: %d problems need more co-resident CTAs (%d) than the device holds (%d)",
+                  cnt, tot2, maxc);
+        return -3;
+      }
+      total = tot2;
+    }
+    int first = 0;
+    for (int i = 0; i < cnt; ++i) {
+      const LanczosProblem& p = probs[base + i];
+      if (p.m > MAXM || p.m < 1 || p.n < 1 || p.ld < p.n) {
+        set_error("lanczos: unsupported sizes n=%d ld=%d m=%d (m must be in [1, %d])", p.n,
+                  p.ld, p.m, MAXM);
+        return -2;
+      }
+      TeamDesc<VT>& t = batch.t[i];
+      t.n = p.n; t.ld = p.ld; t.m = p.m; t.num_desired = p.num_desired;
+      t.max_restarts = p.max_restarts; t.tol = p.tol;
+      t.lanes = lanczos_lanes(p.n, p.nnz);
+      t.first_cta = first;
+      t.nctas = want[i];
+      t.rowptr = p.rowptr; t.col = p.col; t.val = (const VT*)p.val;
+      t.Q = (VT*)p.Q;
+      char* w = (char*)p.work;
+      t.vbuf = (VT*)w; w += align256(2 * (size_t)p.ld * sizeof(VT));
+      t.part = (double*)w; w += align256((size_t)3 * want[i] * MP1 * sizeof(double));
+      t.Ybuf = (double*)w; w += align256((size_t)MAXM * MAXM * sizeof(double));
+      t.bar = (unsigned int*)w;
+      t.alpha = p.alpha; t.beta = p.beta; t.ctl = p.ctl; t.status = p.status;
+      first += want[i];
+      if (cudaMemsetAsync(t.bar, 0, 2 * sizeof(unsigned int), stream) != cudaSuccess ||
+          cudaMemsetAsync(p.ctl, 0, 8 * sizeof(int), stream) != cudaSuccess) {
+        set_error("lanczos: memset failed");
+        return -4;
+      }
+    }
+    void* args[] = {(void*)&batch};
+    cudaError_t e = cudaLaunchCooperativeKernel((const void*)lanczos_team_kernel<VT>,
+                                                dim3(total), dim3(LZ_BLOCK), args, 0, stream);
+    if (e != cudaSuccess) {
+      set_error("lanczos: cooperative launch of %d CTAs failed: %s", total,
+                cudaGetErrorString(e));
+      return -5;
+    }
+  }
+  return 0;
+}
+
+int lanczos_run(const DeviceInfo& di, const LanczosProblem* probs, int count, int prec,
+                cudaStream_t stream) {
+  if (prec == 64) return run_typed<double>(di, probs, count, stream);
+  if (prec == 32) return run_typed<float>(di, probs, count, stream);
+  set_error("lanczos: precision must be 32 or 64");
+  return -2;
+}
+
+int lanczos_occupancy(int prec) {
+  int occ = 0;
+  if (prec == 64)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lanczos_team_kernel<double>, LZ_BLOCK, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lanczos_team_kernel<float>, LZ_BLOCK, 0);
+  return occ;
+}
+
+}  // namespace usbs
