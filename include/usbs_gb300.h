@@ -100,6 +100,92 @@ int usbs_eigsh_smallest(int n, long long nnz, const int* rowptr, const int* col,
                         double tolerance, int precision, void* Q, int ldq, double* eigenvalues,
                         int* info, void* workspace, size_t workspace_bytes, void* stream);
 
+/* ------------------------------------------------------------------ usbs()
+ * One SDP instance, resident in device memory.  Field meanings follow the
+ * reference's SDPState (utils/common.py:11-26) after scale_sdp_state. */
+typedef struct usbs_problem {
+  int n;                    /* order of X (C is n x n) */
+  int m;                    /* number of constraints (len(b)) */
+  long long nnz;            /* entries of the union pattern */
+  int num_triples;
+  const int* rowptr;        /* [n+1] union pattern */
+  const int* col;           /* [nnz] */
+  const double* c_val;      /* [nnz] C on the union pattern */
+  const int* slot_ptr;      /* [nnz+1] */
+  const int* slot_tid;      /* [num_triples] */
+  const int* t_con;         /* [num_triples] caller order */
+  const double* t_a0;       /* [num_triples] caller order */
+  const int* con_ptr;       /* [m+1] triples sorted by constraint */
+  const int* t_row;
+  const int* t_col;
+  const double* t_a;
+  const int* row_ptr;       /* [n+1] triples sorted by row */
+  const int* r_con;
+  const int* r_col;
+  const double* r_a;
+  const double* b;          /* [m] */
+  const double* b_ineq_mask;/* [m] 1.0 for "<=" rows */
+  const double* scale_a;    /* [m] SCALE_A */
+  double scale_c, scale_x;  /* SCALE_C, SCALE_X */
+  double b_norm;            /* || (b / SCALE_A) / SCALE_X ||_2 (host-computed) */
+  int has_ineq;             /* any b_ineq_mask != 0 */
+} usbs_problem;
+
+/* Solver settings: the arguments of usbs() (solver/usbs.py:436-459). */
+typedef struct usbs_params {
+  double trace_ub, trace_factor, rho, beta;
+  int k_curr, k_past;       /* k = k_curr + k_past <= 12 */
+  int max_iters;
+  double max_time;          /* seconds of wall clock */
+  double obj_gap_eps, infeas_gap_eps, max_infeas_eps;
+  int lanczos_inner_iterations;  /* <= 32 */
+  int lanczos_max_restarts;
+  double subprob_eps;
+  int subprob_max_iters;
+  double cond_exp_base;     /* in [1, 2] */
+  int precision;            /* 64: FP64 everywhere; 32: FP32 Lanczos + FP64 rest */
+  int sketch_mode;          /* 0: Nystrom sketch P = X Omega, 1: dense X, 2: diag(X) only */
+  int sketch_dim;           /* columns of Omega (mode 0) */
+} usbs_params;
+
+/* Iterate state (device arrays, column-major with leading dimension ld) and
+ * host-side scalars.  y, z, P, X are read as the starting point and hold the
+ * result on return; V receives the final bundle basis. */
+typedef struct usbs_state {
+  int ld;                   /* n rounded up to a multiple of 32 */
+  double* y;                /* [m] */
+  double* z;                /* [m] */
+  double* V;                /* [ld x (k_curr + k_past)] */
+  double* P;                /* mode 0: [ld x sketch_dim]; mode 2: [n] */
+  double* Omega;            /* mode 0: [ld x sketch_dim] */
+  double* X;                /* mode 1: [n x n] row-major */
+  const double* q0;         /* [n] unit Lanczos start vector (solver/usbs.py:691-692) */
+  double* trace;            /* optional [trace_capacity x 20] per-iteration record */
+  int trace_capacity;
+  double tr_X, primal_obj;  /* in: starting values; out: final values */
+  /* outputs */
+  int iterations;
+  double obj_gap, infeas_gap, max_infeas, obj_ub, pen_dual_obj, elapsed;
+  int status;               /* device status bits (see usbs_eigsh_smallest) */
+} usbs_state;
+
+/* Called on the host at every condition check (after the device has caught
+ * up), before the stop decision: the place for the reference's callback_fn
+ * (solver/usbs.py:505-512). */
+typedef void (*usbs_cond_callback)(void* user, int t);
+
+/* Workspace bytes for usbs_solve (host call). */
+size_t usbs_solve_workspace_bytes(const usbs_problem* problem, const usbs_params* params);
+
+/* usbs() (solver/usbs.py:436-789): initial eigsh for the bundle, then at most
+ * max_iters outer iterations while the reference's stop condition holds
+ * (obj_gap, infeas_gap, max_infeas above their eps and time < max_time),
+ * checking it on the cond_exp_base schedule (utils/loop.py:80-115).
+ * Synchronous: returns when the loop has stopped. */
+int usbs_solve(const usbs_problem* problem, const usbs_params* params, usbs_state* state,
+               void* workspace, size_t workspace_bytes, usbs_cond_callback callback,
+               void* callback_user, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

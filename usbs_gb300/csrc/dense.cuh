@@ -18,7 +18,7 @@ namespace usbs {
 // warp.  On return w[0..n-1] holds the eigenvalues in ascending order and
 // Z (row-major, ldz) the eigenvectors as columns.  A is destroyed.  Returns
 // false if the QR iteration did not converge in 30 n sweeps.  n <= 32.
-__device__ bool warp_syev(double* A, int lda, int n, double* w, double* Z, int ldz) {
+__device__ inline bool warp_syev(double* A, int lda, int n, double* w, double* Z, int ldz) {
   const int lane = threadIdx.x & 31;
   // Z = I
   for (int j = 0; j < n; ++j)
@@ -157,7 +157,7 @@ __device__ bool warp_syev(double* A, int lda, int n, double* w, double* Z, int l
 // pivoting, executed by the whole CTA.  A and b are destroyed; x overwrites b.
 // `red` needs >= 2*blockDim/32 doubles and ints for the pivot search.
 // Returns false (uniformly) if a pivot is exactly zero.
-__device__ bool block_lu_solve(double* A, int lda, double* b, int n, double* redv, int* redi) {
+__device__ inline bool block_lu_solve(double* A, int lda, double* b, int n, double* redv, int* redi) {
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5;
   const int nw = nt >> 5;
   __shared__ int s_piv;
@@ -221,7 +221,7 @@ __device__ bool block_lu_solve(double* A, int lda, double* b, int n, double* red
 
 // Inverse of the n x n matrix A (row-major lda) by one warp: Gauss-Jordan with
 // partial pivoting.  Ainv (row-major ldi) receives the result; A is destroyed.
-__device__ bool warp_inverse(double* A, int lda, int n, double* Ainv, int ldi) {
+__device__ inline bool warp_inverse(double* A, int lda, int n, double* Ainv, int ldi) {
   const int lane = threadIdx.x & 31;
   for (int i = 0; i < n; ++i)
     if (lane < n) Ainv[i * ldi + lane] = (i == lane) ? 1.0 : 0.0;

@@ -57,12 +57,14 @@ __global__ void csr_spmv_kernel(int n, const int* __restrict__ rowptr, const int
   const int lanes_total = gridDim.x * blockDim.x;
   const int gid = blockIdx.x * blockDim.x + threadIdx.x;
   const int lig = gid % L;
+  const int lane = threadIdx.x & 31;
+  const unsigned gmask = (L == 32) ? 0xffffffffu : (((1u << L) - 1u) << (lane & ~(L - 1)));
   for (int row = gid / L; row < n; row += lanes_total / L) {
     VT s = (VT)0;
     const int e = rowptr[row + 1];
     for (int p = rowptr[row] + lig; p < e; p += L) s += val[p] * x[col[p]];
 #pragma unroll
-    for (int o = L >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    for (int o = L >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(gmask, s, o, L);
     if (lig == 0) y[row] = s;
   }
 }

@@ -1,0 +1,226 @@
+"""usbs() on the GB300: the reference's solver call surface over the C ABI.
+
+``usbs(sdp_state, n, m, trace_ub, trace_factor, rho, beta, k_curr, k_past,
+max_iters, max_time, obj_gap_eps, infeas_gap_eps, max_infeas_eps,
+lanczos_inner_iterations, lanczos_max_restarts, subprob_eps, subprob_max_iters,
+cond_exp_base, callback_fn, callback_static_args, callback_nonstatic_args)``
+keeps the signature of solver/usbs.py:436-459 and returns an SDPState.  The
+whole iteration runs on the device (libusbs_gb300 ``usbs_solve``); Python only
+prepares the problem layout once and reads the result.
+
+Extra keyword arguments: ``q0`` (Lanczos start vector; the reference draws it
+from ``PRNGKey(0)``), ``precision`` (64 = FP64 parity path, 32 = FP32 Lanczos
+with FP64 subproblems, gaps and Rayleigh refinement), ``device``,
+``return_trace`` (per-iteration record), ``problem`` (a prepared
+:class:`DeviceProblem`, to skip the host layout step).
+"""
+import ctypes
+
+import numpy as np
+import scipy.sparse as sp
+
+from . import _lib
+from .problem import DeviceProblem, layout
+from .rng import default_q0
+from .state import SDPState
+
+P = ctypes.c_void_p
+
+
+class UsbsProblem(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int), ("m", ctypes.c_int), ("nnz", ctypes.c_longlong),
+                ("num_triples", ctypes.c_int)] + \
+        [(f, P) for f in ("rowptr", "col", "c_val", "slot_ptr", "slot_tid", "t_con", "t_a0",
+                          "con_ptr", "t_row", "t_col", "t_a", "row_ptr", "r_con", "r_col", "r_a",
+                          "b", "b_ineq_mask", "scale_a")] + \
+        [("scale_c", ctypes.c_double), ("scale_x", ctypes.c_double), ("b_norm", ctypes.c_double),
+         ("has_ineq", ctypes.c_int)]
+
+
+class UsbsParams(ctypes.Structure):
+    _fields_ = [("trace_ub", ctypes.c_double), ("trace_factor", ctypes.c_double),
+                ("rho", ctypes.c_double), ("beta", ctypes.c_double), ("k_curr", ctypes.c_int),
+                ("k_past", ctypes.c_int), ("max_iters", ctypes.c_int),
+                ("max_time", ctypes.c_double), ("obj_gap_eps", ctypes.c_double),
+                ("infeas_gap_eps", ctypes.c_double), ("max_infeas_eps", ctypes.c_double),
+                ("lanczos_inner_iterations", ctypes.c_int), ("lanczos_max_restarts", ctypes.c_int),
+                ("subprob_eps", ctypes.c_double), ("subprob_max_iters", ctypes.c_int),
+                ("cond_exp_base", ctypes.c_double), ("precision", ctypes.c_int),
+                ("sketch_mode", ctypes.c_int), ("sketch_dim", ctypes.c_int)]
+
+
+class UsbsState(ctypes.Structure):
+    _fields_ = [("ld", ctypes.c_int)] + [(f, P) for f in ("y", "z", "V", "P", "Omega", "X", "q0",
+                                                          "trace")] + \
+        [("trace_capacity", ctypes.c_int), ("tr_X", ctypes.c_double),
+         ("primal_obj", ctypes.c_double), ("iterations", ctypes.c_int),
+         ("obj_gap", ctypes.c_double), ("infeas_gap", ctypes.c_double),
+         ("max_infeas", ctypes.c_double), ("obj_ub", ctypes.c_double),
+         ("pen_dual_obj", ctypes.c_double), ("elapsed", ctypes.c_double),
+         ("status", ctypes.c_int)]
+
+
+CALLBACK = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int)
+
+TRACE_FIELDS = ["t", "primal_obj", "obj_ub", "obj_gap", "infeas_gap", "max_infeas",
+                "pen_dual_obj", "cand_pen_dual_obj", "lb_spec_est", "cand_eig0", "descent", "eta",
+                "trS", "tr_X", "quad_iters", "lb_iters", "bar_primal_obj", "tr_X_bar"]
+TRACE_WIDTH = 20
+
+
+def _sigs(lib):
+    lib.usbs_solve_workspace_bytes.restype = ctypes.c_size_t
+    lib.usbs_solve_workspace_bytes.argtypes = [ctypes.POINTER(UsbsProblem),
+                                               ctypes.POINTER(UsbsParams)]
+    lib.usbs_solve.restype = ctypes.c_int
+    lib.usbs_solve.argtypes = [ctypes.POINTER(UsbsProblem), ctypes.POINTER(UsbsParams),
+                               ctypes.POINTER(UsbsState), P, ctypes.c_size_t, CALLBACK, P, P]
+
+
+def _ptr(t):
+    return int(t.data_ptr()) if t is not None else None
+
+
+class DeviceInstance:
+    """Problem layout + constraint vectors of one SDP, resident on one device."""
+
+    def __init__(self, sdp_state, device):
+        import torch
+        self.device = torch.device(device)
+        A_idx = np.asarray(_host(sdp_state.A_indices))
+        b = np.asarray(_host(sdp_state.b), dtype=np.float64)
+        self.problem = DeviceProblem(layout(sp.csr_matrix(sdp_state.C), _host(sdp_state.A_data),
+                                            A_idx, m=b.shape[0]), device)
+        mask = np.asarray(_host(sdp_state.b_ineq_mask), dtype=np.float64)
+        SA = np.broadcast_to(np.asarray(_host(sdp_state.SCALE_A), dtype=np.float64),
+                             b.shape).copy()
+        self.b = torch.as_tensor(b, device=self.device)
+        self.mask = torch.as_tensor(mask, device=self.device)
+        self.scale_a = torch.as_tensor(SA, device=self.device)
+        self.scale_c = float(sdp_state.SCALE_C)
+        self.scale_x = float(sdp_state.SCALE_X)
+        self.b_norm = float(np.linalg.norm((b / SA) / self.scale_x))
+        self.has_ineq = bool(np.any(mask != 0))
+
+    def c_struct(self):
+        p = self.problem
+        s = UsbsProblem()
+        s.n, s.m, s.nnz, s.num_triples = p.n, p.m, p.nnz, p.num_triples
+        for f in ("rowptr", "col", "c_val", "slot_ptr", "slot_tid", "t_con", "t_a0", "con_ptr",
+                  "t_row", "t_col", "t_a", "row_ptr", "r_con", "r_col", "r_a"):
+            setattr(s, f, _ptr(getattr(p, f)))
+        s.b, s.b_ineq_mask, s.scale_a = _ptr(self.b), _ptr(self.mask), _ptr(self.scale_a)
+        s.scale_c, s.scale_x, s.b_norm, s.has_ineq = (self.scale_c, self.scale_x, self.b_norm,
+                                                      int(self.has_ineq))
+        return s
+
+
+def _host(x):
+    if x is None:
+        return None
+    if hasattr(x, "detach"):
+        return x.detach().cpu().numpy()
+    return x
+
+
+def _dev_cols(x, rows, ld, cols, device, dtype):
+    """Column-major (cols x ld) device tensor from an (rows, cols) array."""
+    import torch
+    out = torch.zeros((cols, ld), dtype=dtype, device=device)
+    if x is not None:
+        xt = x if isinstance(x, torch.Tensor) else torch.as_tensor(np.asarray(x))
+        out[:, :rows] = xt.to(device=device, dtype=dtype).reshape(rows, cols).t()
+    return out
+
+
+def usbs(sdp_state, n, m, trace_ub, trace_factor, rho, beta, k_curr, k_past, max_iters, max_time,
+         obj_gap_eps, infeas_gap_eps, max_infeas_eps, lanczos_inner_iterations,
+         lanczos_max_restarts, subprob_eps, subprob_max_iters, cond_exp_base=1.0,
+         callback_fn=None, callback_static_args=None, callback_nonstatic_args=None, *, q0=None,
+         precision=64, device="cuda", return_trace=False, return_info=False, instance=None,
+         stream=None):
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("usbs_gb300.usbs needs a CUDA device (GB300); none is visible")
+    lib = _lib.load()
+    _sigs(lib)
+    dev = torch.device(device)
+    inst = instance if instance is not None else DeviceInstance(sdp_state, dev)
+    k = k_curr + k_past
+    ld = (n + 31) // 32 * 32
+    f64 = torch.float64
+    y = torch.as_tensor(np.asarray(_host(sdp_state.y), dtype=np.float64), device=dev).clone()
+    z = torch.as_tensor(np.asarray(_host(sdp_state.z), dtype=np.float64), device=dev).clone()
+    V = torch.zeros((k, ld), dtype=f64, device=dev)
+    if sdp_state.X is not None:
+        mode, sdim = 1, 0
+        X = torch.as_tensor(np.asarray(_host(sdp_state.X), dtype=np.float64), device=dev).clone()
+        Pm = Om = None
+    elif sdp_state.Omega is not None:
+        mode = 0
+        sdim = int(np.asarray(_host(sdp_state.Omega)).shape[1])
+        Om = _dev_cols(_host(sdp_state.Omega), n, ld, sdim, dev, f64)
+        Pm = _dev_cols(_host(sdp_state.P), n, ld, sdim, dev, f64)
+        X = None
+    else:
+        mode, sdim = 2, 0
+        Pm = torch.zeros(ld, dtype=f64, device=dev)
+        if sdp_state.P is not None:
+            Pm[:n] = torch.as_tensor(np.asarray(_host(sdp_state.P), dtype=np.float64).reshape(-1))
+        Om = X = None
+    q0 = default_q0(n) if q0 is None else np.asarray(_host(q0), dtype=np.float64)
+    q0t = torch.as_tensor(q0, dtype=f64, device=dev)
+    trace = torch.zeros((max(max_iters, 1), TRACE_WIDTH), dtype=f64, device=dev) \
+        if return_trace else None
+
+    prm = UsbsParams()
+    prm.trace_ub, prm.trace_factor, prm.rho, prm.beta = trace_ub, trace_factor, rho, beta
+    prm.k_curr, prm.k_past, prm.max_iters = k_curr, k_past, int(max_iters)
+    prm.max_time = float(max_time)
+    prm.obj_gap_eps, prm.infeas_gap_eps, prm.max_infeas_eps = (obj_gap_eps, infeas_gap_eps,
+                                                               max_infeas_eps)
+    prm.lanczos_inner_iterations = int(lanczos_inner_iterations)
+    prm.lanczos_max_restarts = int(lanczos_max_restarts)
+    prm.subprob_eps, prm.subprob_max_iters = subprob_eps, int(subprob_max_iters)
+    prm.cond_exp_base = float(cond_exp_base)
+    prm.precision, prm.sketch_mode, prm.sketch_dim = int(precision), mode, sdim
+    pst = UsbsState()
+    pst.ld = ld
+    pst.y, pst.z, pst.V = _ptr(y), _ptr(z), _ptr(V)
+    pst.P, pst.Omega, pst.X, pst.q0, pst.trace = _ptr(Pm), _ptr(Om), _ptr(X), _ptr(q0t), _ptr(trace)
+    pst.trace_capacity = int(max_iters) if return_trace else 0
+    pst.tr_X, pst.primal_obj = float(sdp_state.tr_X), float(sdp_state.primal_obj)
+    prob = inst.c_struct()
+    need = int(lib.usbs_solve_workspace_bytes(ctypes.byref(prob), ctypes.byref(prm)))
+    ws = torch.empty(need, dtype=torch.uint8, device=dev)
+    cb_val = {}
+
+    def _cb(_user, t):
+        if callback_fn is not None and Om is not None:
+            cb_val[t] = callback_fn(Pm[:, :n].t(), Om[:, :n].t(), callback_static_args,
+                                    callback_nonstatic_args)
+
+    ccb = CALLBACK(_cb)
+    st = stream if stream is not None else torch.cuda.current_stream(dev)
+    rc = lib.usbs_solve(ctypes.byref(prob), ctypes.byref(prm), ctypes.byref(pst), _ptr(ws), need,
+                        ccb, None, int(st.cuda_stream))
+    _lib.check(rc, "usbs_solve")
+    if pst.status & 1:
+        raise RuntimeError("usbs_solve: a device barrier timed out")
+    out = SDPState(C=sdp_state.C, A_indices=sdp_state.A_indices, A_data=sdp_state.A_data,
+                   b=sdp_state.b, b_ineq_mask=sdp_state.b_ineq_mask,
+                   X=X, P=(Pm[:, :n].t() if mode == 0 else (Pm[:n] if mode == 2 else None)),
+                   Omega=sdp_state.Omega, y=y, z=z, tr_X=pst.tr_X, primal_obj=pst.primal_obj,
+                   SCALE_C=sdp_state.SCALE_C, SCALE_X=sdp_state.SCALE_X,
+                   SCALE_A=sdp_state.SCALE_A)
+    info = dict(iterations=pst.iterations, obj_gap=pst.obj_gap, infeas_gap=pst.infeas_gap,
+                max_infeas=pst.max_infeas, obj_ub=pst.obj_ub, pen_dual_obj=pst.pen_dual_obj,
+                elapsed=pst.elapsed, status=pst.status, callback_vals=cb_val,
+                V=V[:, :n].t())
+    if return_trace:
+        tr = trace[:pst.iterations].cpu().numpy()
+        recs = [{f: float(r[i]) for i, f in enumerate(TRACE_FIELDS)} for r in tr]
+        return out, recs, info
+    if return_info:
+        return out, info
+    return out
