@@ -62,8 +62,13 @@ def _subspace_gap(A, B):
     return float(np.sqrt(max(0.0, 1.0 - s.min() ** 2)))
 
 
-@pytest.mark.parametrize("name,nd", [("er", 11), ("torus", 10)])
-def test_eigsh_fp64_matches_oracle(cuda, name, nd):
+@pytest.mark.parametrize("name,nd,restarts,tol", [("er", 5, 200, 1e-9), ("torus", 4, 300, 1e-9),
+                                                  ("er", 11, 10, 1e-7)])
+def test_eigsh_fp64_matches_oracle(cuda, name, nd, restarts, tol):
+    """Converged Ritz pairs agree to round-off.  With the reference's default
+    budget (10 restarts, tol 1e-7) the trailing Ritz vectors are not converged;
+    those directions depend on summation order in any two FP64 implementations,
+    so only the converged ones are held to round-off there."""
     from usbs_gb300 import api
     from usbs_gb300.problem import DeviceProblem, layout
     Wg = wl.er_graph(800, 19176, 0) if name == "er" else wl.torus_graph(30, 1)
@@ -72,20 +77,24 @@ def test_eigsh_fp64_matches_oracle(cuda, name, nd):
     prob = DeviceProblem(layout(st.C, st.A_data, st.A_indices, m=n), cuda)
     y = np.random.default_rng(2).standard_normal(n) * 0.5
     q0 = orng.default_q0(n)
-    trace = []
     ov, oV, ost = olz.eigsh_smallest(n, (-st.C).tocsr(), st.A_data, st.A_indices, y, q0, nd, 32,
-                                     10, 1e-7, trace=trace)
-    gv, gV, info = api.eigsh_smallest(n, prob, None, None, y, q0, nd, 32, 10, 1e-7, c_scale=-1.0,
-                                      precision=64, return_info=True)
+                                     restarts, tol)
+    gv, gV, info = api.eigsh_smallest(n, prob, None, None, y, q0, nd, 32, restarts, tol,
+                                      c_scale=-1.0, precision=64, return_info=True)
     gv, gV = _np(gv), _np(gV)
     assert info.status == 0
-    assert info.restarts == ost["restart"]
-    np.testing.assert_allclose(gv, ov, rtol=1e-9, atol=1e-9 * np.abs(ov).max())
-    # eigenvectors: compare the invariant quantities (column signs are free)
-    for j in range(nd):
-        c = abs(gV[:, j] @ oV[:, j])
-        assert c > 1 - 1e-7, (j, c)
+    assert info.restarts == ost["restart"] and info.num_converged == ost["nconv"]
+    nc = min(nd, ost["nconv"])
+    np.testing.assert_allclose(gv[:nc], ov[:nc], rtol=1e-9, atol=1e-9 * np.abs(ov).max())
+    for j in range(nc):
+        assert abs(gV[:, j] @ oV[:, j]) > 1 - 1e-12, j
+    # unconverged tail: still Ritz values of the same operator to the residual level
+    assert np.abs(gv - ov).max() <= 1e-4 * np.abs(ov).max()
     np.testing.assert_allclose(gV.T @ gV, np.eye(nd), atol=1e-10)
+    # residuals: ||Op v - theta v|| small for the converged pairs
+    Op = (-st.C).toarray() + np.diag(y)
+    r = np.linalg.norm(Op @ gV[:, :nc] - gV[:, :nc] * gv[None, :nc], axis=0)
+    assert r.max() < 10 * tol + 1e-9
 
 
 def test_eigsh_fp32_close_to_oracle(cuda):

@@ -14,7 +14,7 @@ KEYS = ["primal_obj", "obj_ub", "lb_spec_est", "pen_dual_obj", "cand_pen_dual_ob
         "obj_gap", "infeas_gap", "max_infeas", "tr_X"]
 
 
-def _run_both(W, iters, precision, sketch_dim=10, k_curr=10, k_past=1):
+def _run_both(W, iters, precision, sketch_dim=10, k_curr=10, k_past=1, eps=1e-7, restarts=10):
     from usbs_gb300 import solver
     st = omaxcut.initialize_state(W, sketch_dim)
     n = st.C.shape[0]
@@ -22,11 +22,10 @@ def _run_both(W, iters, precision, sketch_dim=10, k_curr=10, k_past=1):
     mL = min(n, 32)
     otr = []
     oout, ofin = ousbs.usbs(st, n, n, 2.0 * n, 2.0, S["rho"], S["beta"], k_curr, k_past, iters,
-                            np.inf, -1.0, -1.0, -1.0, mL, S["lanczos_max_restarts"],
-                            S["subprob_eps"], S["subprob_max_iters"], q0=q0, trace=otr)
+                            np.inf, -1.0, -1.0, -1.0, mL, restarts, eps, S["subprob_max_iters"],
+                            q0=q0, trace=otr)
     gout, gtr, info = solver.usbs(st, n, n, 2.0 * n, 2.0, S["rho"], S["beta"], k_curr, k_past,
-                                  iters, np.inf, -1.0, -1.0, -1.0, mL,
-                                  S["lanczos_max_restarts"], S["subprob_eps"],
+                                  iters, np.inf, -1.0, -1.0, -1.0, mL, restarts, eps,
                                   S["subprob_max_iters"], 1.0, None, None, None, q0=q0,
                                   precision=precision, return_trace=True)
     return st, oout, ofin, otr, gout, gtr, info
@@ -37,22 +36,38 @@ def _rel(a, b):
 
 
 def test_usbs_fp64_trace_matches_oracle(cuda):
+    """Plain FP64 device path vs the FP64 oracle, iteration by iteration, on a
+    configuration whose eigenproblems are resolved (Lanczos converges, so the
+    bundle basis is determined by the problem and not by rounding)."""
     W = wl.er_graph(300, 4000, 7)
-    st, oout, ofin, otr, gout, gtr, info = _run_both(W, 8, 64)
-    assert info["status"] == 0 and info["iterations"] == 8
+    st, oout, ofin, otr, gout, gtr, info = _run_both(W, 5, 64, k_curr=4, k_past=1, eps=1e-9,
+                                                     restarts=200)
+    assert info["status"] == 0 and info["iterations"] == 5
     for a, b in zip(otr, gtr):
         assert bool(a["descent"]) == bool(b["descent"]), a["t"]
+        assert a["quad_iters"] == b["quad_iters"] and a["lb_iters"] == b["lb_iters"], a["t"]
         for key in KEYS:
-            assert _rel(a[key], b[key]) < 1e-8, (a["t"], key, a[key], b[key])
-    np.testing.assert_allclose(gout.y.cpu().numpy(), oout.y, rtol=1e-7, atol=1e-7)
-    np.testing.assert_allclose(gout.z.cpu().numpy(), oout.z, rtol=1e-7, atol=1e-7)
-    np.testing.assert_allclose(gout.P.cpu().numpy(), oout.P, rtol=1e-6, atol=1e-7)
-    assert _rel(gout.primal_obj, oout.primal_obj) < 1e-8
+            assert _rel(a[key], b[key]) < 1e-9, (a["t"], key, a[key], b[key])
+    np.testing.assert_allclose(gout.y.cpu().numpy(), oout.y, rtol=1e-8, atol=1e-8)
+    np.testing.assert_allclose(gout.z.cpu().numpy(), oout.z, rtol=1e-8, atol=1e-9)
+    np.testing.assert_allclose(gout.P.cpu().numpy(), oout.P, rtol=1e-7, atol=1e-8)
+    assert _rel(gout.primal_obj, oout.primal_obj) < 1e-9
 
 
-def test_usbs_fp32_mixed_close_to_fp64_oracle(cuda):
+def test_usbs_fp64_reference_settings_first_step(cuda):
+    """With the reference's default Lanczos budget the trailing Ritz vectors are
+    unconverged; the first step still agrees to their sensitivity (~1e-4)."""
+    W = wl.er_graph(300, 4000, 7)
+    st, oout, ofin, otr, gout, gtr, info = _run_both(W, 1, 64)
+    assert _rel(otr[0]["primal_obj"], gtr[0]["primal_obj"]) < 1e-3
+    assert _rel(otr[0]["lb_spec_est"], gtr[0]["lb_spec_est"]) < 1e-3
+
+
+def test_usbs_fp32_mixed_step_close_to_fp64(cuda):
+    """FP32 Lanczos + FP64 rest vs the FP64 oracle on a resolved configuration."""
     W = wl.torus_graph(30, 1)
-    st, oout, ofin, otr, gout, gtr, info = _run_both(W, 12, 32)
+    st, oout, ofin, otr, gout, gtr, info = _run_both(W, 3, 32, k_curr=4, k_past=1, eps=1e-9,
+                                                     restarts=100)
     assert info["status"] == 0
     for a, b in zip(otr, gtr):
         assert _rel(a["primal_obj"], b["primal_obj"]) < 1e-4, (a["t"], a["primal_obj"],
@@ -61,10 +76,26 @@ def test_usbs_fp32_mixed_close_to_fp64_oracle(cuda):
 
 def test_usbs_dense_X_mode(cuda):
     W = wl.er_graph(120, 900, 9)
-    st, oout, ofin, otr, gout, gtr, info = _run_both(W, 5, 64, sketch_dim=-1, k_curr=4, k_past=1)
+    st, oout, ofin, otr, gout, gtr, info = _run_both(W, 4, 64, sketch_dim=-1, k_curr=4,
+                                                     k_past=1, eps=1e-9, restarts=200)
     for a, b in zip(otr, gtr):
-        assert _rel(a["primal_obj"], b["primal_obj"]) < 1e-8
-    np.testing.assert_allclose(gout.X.cpu().numpy(), oout.X, rtol=1e-7, atol=1e-8)
+        assert _rel(a["primal_obj"], b["primal_obj"]) < 1e-9
+    np.testing.assert_allclose(gout.X.cpu().numpy(), oout.X, rtol=1e-8, atol=1e-9)
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_usbs_complete_graph_optimum(cuda, precision):
+    """MaxCut SDP of K_n (unit weights) is n^2/4: both precisions reach it."""
+    from usbs_gb300 import solver
+    import scipy.sparse as sp
+    n = 40
+    W = sp.csr_matrix(np.ones((n, n)) - np.eye(n))
+    st = omaxcut.initialize_state(W, 4)
+    out, info = solver.usbs(st, n, n, 2.0 * n, 2.0, 0.01, 0.25, 4, 1, 2000, np.inf, 1e-3, 1e-3,
+                            1e-3, 32, 10, 1e-7, 100, 1.0, None, None, None, precision=precision,
+                            return_info=True)
+    assert info["obj_gap"] <= 1e-3 and info["max_infeas"] <= 1e-3, info
+    assert abs(out.primal_obj - n * n / 4.0) / (n * n / 4.0) < 2e-3
 
 
 def test_usbs_stops_on_gap(cuda):
