@@ -153,6 +153,183 @@ __device__ inline bool warp_syev(double* A, int lda, int n, double* w, double* Z
   return true;
 }
 
+// Cyclic parallel Jacobi eigensolver (float) for a symmetric n x n matrix by
+// one warp: n/2 disjoint rotations per round in round-robin ("chess
+// tournament") order, Rutishauser's rotation formulas, sweeps until the
+// off-diagonal Frobenius norm is below 4 eps ||A||_F.  A (row-major lda) is
+// destroyed; w receives the eigenvalues ascending, Z (row-major ldz) the
+// eigenvectors as columns.  n <= 32.  Returns false if 20 sweeps do not converge.
+__device__ inline bool warp_jacobi_f32(float* A, int lda, int n, float* w, float* Z, int ldz,
+                                       int* pidx, float* rc, float* rs) {
+  const int lane = threadIdx.x & 31;
+  const int M = (n + 1) & ~1;  // even order; a padding index couples to nothing
+  for (int i = 0; i < M; ++i)
+    if (lane < M) Z[i * ldz + lane] = (i == lane) ? 1.0f : 0.0f;
+  if (M > n && lane < M) { A[n * lda + lane] = 0.0f; A[lane * lda + n] = 0.0f; }
+  __syncwarp();
+  float fro = 0.0f;
+  for (int i = 0; i < n; ++i) {
+    const float a = (lane < n) ? A[i * lda + lane] : 0.0f;
+    fro += a * a;
+  }
+  fro = warp_sum(fro);
+  const float tol2 = fro * (4.0f * 1.2e-7f) * (4.0f * 1.2e-7f);
+  bool ok = false;
+  const int half = M >> 1;
+  for (int sweep = 0; sweep < 20; ++sweep) {
+    float off = 0.0f;
+    for (int i = 0; i < n; ++i) {
+      const float a = (lane < n && lane != i) ? A[i * lda + lane] : 0.0f;
+      off += a * a;
+    }
+    off = warp_sum(off);
+    if (off <= tol2) { ok = true; break; }
+    for (int r = 0; r < M - 1; ++r) {
+      if (lane < half) {
+        int p, q;
+        if (lane == 0) { p = 0; q = 1 + r % (M - 1); }
+        else {
+          p = 1 + (r + lane) % (M - 1);
+          q = 1 + (r - lane + M - 1) % (M - 1);
+        }
+        if (p > q) { const int t = p; p = q; q = t; }
+        const float apq = A[p * lda + q];
+        float c = 1.0f, s = 0.0f;
+        if (apq != 0.0f) {
+          const float theta = (A[q * lda + q] - A[p * lda + p]) / (2.0f * apq);
+          const float t = copysignf(1.0f, theta) / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
+          c = rsqrtf(t * t + 1.0f);
+          s = t * c;
+        }
+        pidx[2 * lane] = p;
+        pidx[2 * lane + 1] = q;
+        rc[lane] = c;
+        rs[lane] = s;
+      }
+      __syncwarp();
+      // rows: (J^T A)
+      for (int e = lane; e < half * M; e += 32) {
+        const int pr = e / M, j = e - pr * M;
+        const int p = pidx[2 * pr], q = pidx[2 * pr + 1];
+        const float c = rc[pr], s = rs[pr];
+        const float ap = A[p * lda + j], aq = A[q * lda + j];
+        A[p * lda + j] = c * ap - s * aq;
+        A[q * lda + j] = s * ap + c * aq;
+      }
+      __syncwarp();
+      // columns: (. J) and eigenvectors Z J
+      for (int e = lane; e < half * M; e += 32) {
+        const int pr = e / M, j = e - pr * M;
+        const int p = pidx[2 * pr], q = pidx[2 * pr + 1];
+        const float c = rc[pr], s = rs[pr];
+        const float ap = A[j * lda + p], aq = A[j * lda + q];
+        A[j * lda + p] = c * ap - s * aq;
+        A[j * lda + q] = s * ap + c * aq;
+        const float zp = Z[j * ldz + p], zq = Z[j * ldz + q];
+        Z[j * ldz + p] = c * zp - s * zq;
+        Z[j * ldz + q] = s * zp + c * zq;
+      }
+      __syncwarp();
+    }
+  }
+  // eigenvalues from the diagonal, sorted ascending with their vectors
+  for (int i = lane; i < n; i += 32) w[i] = A[i * lda + i];
+  __syncwarp();
+  for (int i = 0; i < n - 1; ++i) {
+    int kmin = i;
+    float vmin = w[i];
+    for (int j = i + 1; j < n; ++j)
+      if (w[j] < vmin) { vmin = w[j]; kmin = j; }
+    if (kmin != i) {
+      const float wi = w[i];
+      __syncwarp();
+      if (lane < n) {
+        const float t = Z[lane * ldz + i];
+        Z[lane * ldz + i] = Z[lane * ldz + kmin];
+        Z[lane * ldz + kmin] = t;
+      }
+      if (lane == 0) { w[kmin] = wi; w[i] = vmin; }
+      __syncwarp();
+    }
+  }
+  return ok;
+}
+
+// One step of the iterative refinement of a symmetric eigen-decomposition of
+// Ogita & Aishima ("Iterative refinement for symmetric eigenvalue
+// decomposition", Japan J. Indust. Appl. Math. 35, 2018), FP64, whole CTA.
+//   R = I - X^T X,  S = X^T A X,  lam_i = S_ii / (1 - R_ii),
+//   E_ij = (S_ij + lam_j R_ij) / (lam_j - lam_i)  if |lam_i - lam_j| > delta,
+//          R_ij / 2                                 otherwise,
+//   X <- X + X E.
+// A, X, R, S, W: n x n row-major with leading dimension ld (shared memory);
+// A is multiplied as a dense matrix.  lam receives the refined eigenvalues.
+__device__ inline void cta_refine_eig(const double* A, double* X, double* R, double* S,
+                                      double* W, double* lam, double* red, int n, int ld) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  // W = A X
+  for (int e = tid; e < n * n; e += nt) {
+    const int i = e / n, j = e - i * n;
+    double v = 0.0;
+    for (int l = 0; l < n; ++l) {
+      const double a = A[i * ld + l];
+      if (a != 0.0) v += a * X[l * ld + j];
+    }
+    W[i * ld + j] = v;
+  }
+  __syncthreads();
+  // R = I - X^T X,  S = X^T W
+  for (int e = tid; e < n * n; e += nt) {
+    const int i = e / n, j = e - i * n;
+    double r = 0.0, s = 0.0;
+    for (int l = 0; l < n; ++l) {
+      r += X[l * ld + i] * X[l * ld + j];
+      s += X[l * ld + i] * W[l * ld + j];
+    }
+    R[i * ld + j] = ((i == j) ? 1.0 : 0.0) - r;
+    S[i * ld + j] = s;
+  }
+  __syncthreads();
+  if (tid < n) lam[tid] = S[tid * ld + tid] / (1.0 - R[tid * ld + tid]);
+  __syncthreads();
+  // delta = 2 (||S - diag(lam)||_F + ||A||_F ||R||_F)
+  double sa = 0.0, aa = 0.0, rr = 0.0;
+  for (int e = tid; e < n * n; e += nt) {
+    const int i = e / n, j = e - i * n;
+    const double d = S[i * ld + j] - ((i == j) ? lam[i] : 0.0);
+    sa += d * d;
+    aa += A[i * ld + j] * A[i * ld + j];
+    rr += R[i * ld + j] * R[i * ld + j];
+  }
+  sa = block_sum(sa, red);
+  __syncthreads();
+  aa = block_sum(aa, red);
+  __syncthreads();
+  rr = block_sum(rr, red);
+  const double delta = 2.0 * (sqrt(sa) + sqrt(aa) * sqrt(rr));
+  // E into W
+  for (int e = tid; e < n * n; e += nt) {
+    const int i = e / n, j = e - i * n;
+    const double dl = lam[j] - lam[i];
+    W[i * ld + j] = (fabs(dl) > delta) ? (S[i * ld + j] + lam[j] * R[i * ld + j]) / dl
+                                       : 0.5 * R[i * ld + j];
+  }
+  __syncthreads();
+  // X <- X + X E   (result into S, then copied back)
+  for (int e = tid; e < n * n; e += nt) {
+    const int i = e / n, j = e - i * n;
+    double v = 0.0;
+    for (int l = 0; l < n; ++l) v += X[i * ld + l] * W[l * ld + j];
+    S[i * ld + j] = X[i * ld + j] + v;
+  }
+  __syncthreads();
+  for (int e = tid; e < n * n; e += nt) {
+    const int i = e / n, j = e - i * n;
+    X[i * ld + j] = S[i * ld + j];
+  }
+  __syncthreads();
+}
+
 // Solve A x = b (n x n, row-major lda, in shared memory) by LU with partial
 // pivoting, executed by the whole CTA.  A and b are destroyed; x overwrites b.
 // `red` needs >= 2*blockDim/32 doubles and ints for the pivot search.

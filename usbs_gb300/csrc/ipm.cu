@@ -73,88 +73,171 @@ __device__ __forceinline__ double symkron(const double* T, const double* X, int 
   return 0.5 * wa * wb * acc;
 }
 
-// Cholesky positive-definiteness test of A + s dA (k x k, lower triangle)
-__device__ bool pd_test(const double* A, const double* dA, double s, int k) {
-  double L[IPM_MAXS];
+// Positive-definiteness test of A + s dA (k x k, lower triangle) by LDL^T
+// without pivoting: PD iff every pivot is positive (equivalent to Cholesky
+// succeeding, i.e. to the smallest eigenvalue being > 0, up to round-off at the
+// boundary).  One reciprocal per column, no square roots.
+__device__ __forceinline__ bool pd_test(const double* A, const double* dA, double s, int k) {
+  double L[IPM_MAXS];   // packed lower triangle, unit diagonal implied; L[jj] holds d_j
   for (int j = 0; j < k; ++j) {
+    const int rj = j * (j + 1) / 2;
     double d = A[j * k + j] + s * dA[j * k + j];
-    for (int p = 0; p < j; ++p) d -= L[j * (j + 1) / 2 + p] * L[j * (j + 1) / 2 + p];
+    for (int p = 0; p < j; ++p) d -= L[rj + p] * L[rj + p] * L[p * (p + 1) / 2 + p];
     if (!(d > 0.0)) return false;
-    const double ljj = sqrt(d);
-    L[j * (j + 1) / 2 + j] = ljj;
+    L[rj + j] = d;
+    const double inv = 1.0 / d;
     for (int i = j + 1; i < k; ++i) {
+      const int ri = i * (i + 1) / 2;
       double v = A[i * k + j] + s * dA[i * k + j];
-      for (int p = 0; p < j; ++p) v -= L[i * (i + 1) / 2 + p] * L[j * (j + 1) / 2 + p];
-      L[i * (i + 1) / 2 + j] = v / ljj;
+      for (int p = 0; p < j; ++p) v -= L[ri + p] * L[rj + p] * L[p * (p + 1) / 2 + p];
+      L[ri + j] = v * inv;
     }
   }
   return true;
 }
 
+struct IpmScal {
+  double eta, zeta, omega, mu, step, trS, k1, k2, den, ze, F2, d_eta, d_omega, d_zeta, st, cS,
+      cT, q22, h2, t1, t2, t3, t4;
+  int cont, it;
+};
+
+// sum_a x[a] y[a] by one warp (lane 0 holds the result)
+__device__ __forceinline__ double wdot(const double* x, const double* y, int s) {
+  double v = 0.0;
+  for (int a = threadIdx.x & 31; a < s; a += 32) v += x[a] * y[a];
+  return warp_sum(v);
+}
+
+// LU with partial pivoting and solve, whole CTA: warps over rows, lanes over
+// columns; multipliers formed once (lane 0) and broadcast through shared memory.
+__device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* redv, int* redi,
+                             int* piv_out, int* ok_out) {
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+  if (tid == 0) *ok_out = 1;
+  for (int j = 0; j < n; ++j) {
+    if (wid == 0) {
+      double best = -1.0;
+      int bi = j;
+      for (int i = j + lane; i < n; i += 32) {
+        const double a = fabs(A[i * lda + j]);
+        if (a > best) { best = a; bi = i; }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
+      }
+      if (lane == 0) {
+        *piv_out = bi;
+        if (best == 0.0) *ok_out = 0;
+        redv[0] = (best == 0.0) ? 1.0 : 1.0 / A[bi * lda + j];
+      }
+    }
+    __syncthreads();
+    const int piv = *piv_out;
+    if (piv != j) {
+      for (int c = tid; c < n; c += blockDim.x) {
+        const double t = A[j * lda + c];
+        A[j * lda + c] = A[piv * lda + c];
+        A[piv * lda + c] = t;
+      }
+      if (tid == 0) { const double t = b[j]; b[j] = b[piv]; b[piv] = t; }
+      __syncthreads();
+    }
+    const double inv = redv[0];
+    const double bj = b[j];
+    for (int i = j + 1 + wid; i < n; i += nw) {
+      if (lane == 0) {
+        const double l = A[i * lda + j] * inv;
+        A[i * lda + j] = l;
+        b[i] -= l * bj;
+      }
+      __syncwarp();
+      const double l = A[i * lda + j];
+      for (int c = j + 1 + lane; c < n; c += 32) A[i * lda + c] -= l * A[j * lda + c];
+    }
+    __syncthreads();
+  }
+  for (int j = n - 1; j >= 0; --j) {
+    if (tid == 0) b[j] = b[j] / A[j * lda + j];
+    __syncthreads();
+    const double bj = b[j];
+    for (int i = tid; i < j; i += blockDim.x) b[i] -= A[i * lda + j] * bj;
+    __syncthreads();
+  }
+  (void)redi;
+}
+
 __global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ IpmArgs A) {
   extern __shared__ double dyn[];
   __shared__ IpmShared sh;
-  __shared__ double s_red[IPM_BLOCK / 32];
+  __shared__ IpmScal sc;
+  __shared__ double grid[256];
+  __shared__ int s_piv, s_ok;
   if (A.skip && *A.skip) return;
-  const int k = A.k, s = k * (k + 1) / 2, tid = threadIdx.x;
+  const int k = A.k, s = k * (k + 1) / 2, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int nw = IPM_BLOCK / 32;
   double* Q11 = dyn;            // s*s (mode 0)
   double* coeff = dyn + s * s;  // s*s
   double* sm = A.smalls;
-  // svec index maps (np.tril_indices order)
   if (tid == 0) {
     int a = 0;
     for (int b = 0; b < k; ++b)
       for (int c = 0; c <= b; ++c) { sh.bi[a] = b; sh.ci[a] = c; ++a; }
   }
+  const int ngrid = A.ipm_grid;
+  for (int j = tid; j < ngrid && j < 256; j += IPM_BLOCK) grid[j] = pow(0.9, (double)j);
   __syncthreads();
   const double tr = A.trace_ub;
   const double tXb_raw = sm[A.o_sc + SC_TRXBAR];
   const double tX = (tXb_raw > 0.0) ? tXb_raw : tr;
   const double bpo = sm[A.o_sc + SC_BPO];
-  double q22 = 0.0, h2 = 0.0;
   for (int a = tid; a < s; a += IPM_BLOCK) sh.sI[a] = (sh.bi[a] == sh.ci[a]) ? 1.0 : 0.0;
   if (A.mode == 0) {
     const double rho = A.rho;
     const double* QB = sm + A.o_QB;
-    for (int e = tid; e < s * s; e += IPM_BLOCK) Q11[e] = (tr * tr / rho) * QB[e];
+    const double qs = tr * tr / rho;
+    for (int e = tid; e < s * s; e += IPM_BLOCK) Q11[e] = qs * QB[e];
     const double* GZ = sm + A.o_GZ;
     const double* GYmC = sm + A.o_GYmC;
     const double* GB = sm + A.o_GB;
+    const double q12s = tr * tr / (rho * tX);
     for (int a = tid; a < s; a += IPM_BLOCK) {
       const int b = sh.bi[a], c = sh.ci[a];
-      sh.q12[a] = (tr * tr / (rho * tX)) * svec_of(GZ, k, b, c);
+      sh.q12[a] = q12s * svec_of(GZ, k, b, c);
       // svec(V^T (A*(y) - C - A*(b - ups)/rho) V)
-      double gy = svec_of(GYmC, k, b, c);
-      double gb = svec_of(GB, k, b, c);
-      sh.h1[a] = tr * (gy - gb / rho);
+      sh.h1[a] = tr * (svec_of(GYmC, k, b, c) - svec_of(GB, k, b, c) / rho);
     }
-    q22 = (tr * tr / (rho * tX * tX)) * sm[A.o_sc + SC_ZZ];
-    h2 = (tr / tX) * (sm[A.o_sc + SC_ZY] - bpo - sm[A.o_sc + SC_ZBMU] / rho);
+    if (tid == 0) {
+      sc.q22 = (tr * tr / (rho * tX * tX)) * sm[A.o_sc + SC_ZZ];
+      sc.h2 = (tr / tX) * (sm[A.o_sc + SC_ZY] - bpo - sm[A.o_sc + SC_ZBMU] / rho);
+    }
   } else {
     const double* GYC = sm + A.o_GYC;  // V^T (A*(y_cand) - C) V
     for (int a = tid; a < s; a += IPM_BLOCK) {
       sh.h1[a] = tr * svec_of(GYC, k, sh.bi[a], sh.ci[a]);   // g_1
       sh.q12[a] = 0.0;
     }
-    h2 = (tr / tX) * (sm[A.o_sc + SC_ZYC] - bpo);           // g_2
+    if (tid == 0) { sc.q22 = 0.0; sc.h2 = (tr / tX) * (sm[A.o_sc + SC_ZYC] - bpo); }   // g_2
   }
-  __syncthreads();
   // ---- initial point ----
-  double eta;
   if (A.mode == 0) {
-    eta = (tX / tr) * sm[A.o_sc + SC_ETA_SUB];
     const double* S0 = sm + A.o_Ssub;
     for (int e = tid; e < k * k; e += IPM_BLOCK) sh.S[e] = S0[e] / tr;
+    if (tid == 0) sc.eta = (tX / tr) * sm[A.o_sc + SC_ETA_SUB];
   } else {
-    eta = (bpo == 0.0) ? 0.00001 : 0.99 * (1.0 / (k + 1.0));
     for (int e = tid; e < k * k; e += IPM_BLOCK) {
       const int r = e / k, c = e - r * k;
       sh.S[e] = (r == c) ? 0.99 * (1.0 / (k + 1.0)) : 0.0;
     }
+    if (tid == 0) sc.eta = (bpo == 0.0) ? 0.00001 : 0.99 * (1.0 / (k + 1.0));
   }
   __syncthreads();
   for (int a = tid; a < s; a += IPM_BLOCK) sh.sS[a] = svec_of(sh.S, k, sh.bi[a], sh.ci[a]);
   __syncthreads();
+  const double q22 = sc.q22, h2 = sc.h2;
+  double eta = sc.eta;
   // T_svec -> sh.ord (temporary)
   for (int a = tid; a < s; a += IPM_BLOCK) {
     if (A.mode == 0) {
@@ -165,170 +248,248 @@ __global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ 
       sh.ord[a] = sh.h1[a];
     }
   }
+  if (wid == 0) {
+    const double d = wdot(sh.q12, sh.sS, s);
+    if (lane == 0) sc.zeta = (A.mode == 0) ? (d + eta * q22 + h2) : h2;
+  }
   __syncthreads();
-  double zeta = (A.mode == 0) ? (dot_s(sh.q12, sh.sS, s) + eta * q22 + h2) : h2;
   svec_inv_to(sh.ord, k, s, sh.bi, sh.ci, sh.T);
   __syncthreads();
-  double vmax = zeta, vmin = zeta;
-  for (int b = 0; b < k; ++b) { vmax = fmax(vmax, sh.T[b * k + b]); vmin = fmin(vmin, sh.T[b * k + b]); }
-  double width = vmax - vmin;
-  width = (width < 100.0) ? 100.0 : width;
-  double omega = -1.01 * vmin;
-  omega = (omega < width) ? width : omega;
-  __syncthreads();
-  if (tid < k) sh.T[tid * k + tid] += omega;
-  zeta += omega;
+  if (tid == 0) {
+    double zeta = sc.zeta, vmax = zeta, vmin = zeta;
+    for (int b = 0; b < k; ++b) { vmax = fmax(vmax, sh.T[b * k + b]); vmin = fmin(vmin, sh.T[b * k + b]); }
+    double width = vmax - vmin;
+    width = (width < 100.0) ? 100.0 : width;
+    double omega = -1.01 * vmin;
+    omega = (omega < width) ? width : omega;
+    for (int b = 0; b < k; ++b) sh.T[b * k + b] += omega;
+    sc.zeta = zeta + omega;
+    sc.omega = omega;
+    double trS = 0.0;
+    for (int b = 0; b < k; ++b) trS += sh.S[b * k + b];
+    sc.trS = trS;
+    sc.step = 1.0;
+    sc.it = 0;
+  }
   __syncthreads();
   for (int a = tid; a < s; a += IPM_BLOCK) sh.sT[a] = svec_of(sh.T, k, sh.bi[a], sh.ci[a]);
   __syncthreads();
-  double trS = 0.0;
-  for (int b = 0; b < k; ++b) trS += sh.S[b * k + b];
-  double mu = (dot_s(sh.sS, sh.sT, s) + eta * zeta + omega * (1 - trS - eta)) / (2 * k + 4.0);
-  double step = 1.0;
-  int it = 0;
+  if (wid == 0) {
+    const double d = wdot(sh.sS, sh.sT, s);
+    if (lane == 0)
+      sc.mu = (d + sc.eta * sc.zeta + sc.omega * (1 - sc.trS - sc.eta)) / (2 * k + 4.0);
+  }
+  __syncthreads();
   const int maxit = A.max_iters;
   const double eps = A.eps;
-  while (it < maxit) {
-    const bool cont = (A.mode == 0) ? (mu > eps && step > eps * eps) : (mu > eps);
-    if (!cont) break;
+  while (true) {
+    if (tid == 0) {
+      const bool cont = (sc.it < maxit) &&
+          ((A.mode == 0) ? (sc.mu > eps && sc.step > eps * eps) : (sc.mu > eps));
+      sc.cont = cont;
+      if (cont) {
+        sc.k1 = (1 - sc.trS - sc.eta) / sc.omega;
+        sc.k2 = sc.zeta / sc.eta + q22;
+        sc.den = sc.k1 * sc.k2 + 1;
+        sc.ze = sc.zeta / sc.eta;
+      }
+    }
+    __syncthreads();
+    if (!sc.cont) break;
+    const double mu = sc.mu, eta_ = sc.eta, zeta = sc.zeta, omega = sc.omega, tIS = sc.trS;
+    const double k1 = sc.k1, k2 = sc.k2, den = sc.den, ze = sc.ze;
     // ---- Newton system ----
-    const double tIS = trS;
-    const double k1 = (1 - tIS - eta) / omega;
-    const double k2 = zeta / eta + q22;
-    double F2 = 0.0;
     if (A.mode == 0) {
       for (int a = tid; a < s; a += IPM_BLOCK) {
         double v = 0.0;
         for (int b = 0; b < s; ++b) v += Q11[a * s + b] * sh.sS[b];
-        double f = v + eta * sh.q12[a] + sh.h1[a];
+        const double f = v + eta_ * sh.q12[a] + sh.h1[a];
         sh.F1[a] = f + (-sh.sT[a] + omega * sh.sI[a]);
       }
-      F2 = dot_s(sh.q12, sh.sS, s) + eta * q22 + h2;
-      F2 = F2 + (-zeta + omega);
+      if (wid == 1) {
+        const double d = wdot(sh.q12, sh.sS, s);
+        if (lane == 0) {
+          double F2 = d + eta_ * q22 + h2;
+          sc.F2 = F2 + (-zeta + omega);
+        }
+      }
     }
-    // S^-1 by warp 0
-    if (tid < 32) {
-      for (int e = tid; e < k * k; e += 32) sh.wk[e] = sh.S[e];
+    if (wid == 0) {   // S^-1
+      for (int e = lane; e < k * k; e += 32) sh.wk[e] = sh.S[e];
       __syncwarp();
-      bool ok = warp_inverse(sh.wk, k, k, sh.Si, k);
-      if (!ok && tid == 0) atomicOr(A.status, ST_SMALL_DENSE_FAIL);
+      const bool okinv = warp_inverse(sh.wk, k, k, sh.Si, k);
+      if (!okinv && lane == 0) atomicOr(A.status, ST_SMALL_DENSE_FAIL);
     }
     __syncthreads();
+    const double F2 = (A.mode == 0) ? sc.F2 : 0.0;
     for (int a = tid; a < s; a += IPM_BLOCK) sh.sSi[a] = svec_of(sh.Si, k, sh.bi[a], sh.ci[a]);
-    const double den = k1 * k2 + 1;
-    const double ze = zeta / eta;
-    for (int e = tid; e < s * s; e += IPM_BLOCK) {
-      const int a = e / s, a2 = e - a * s;
-      double v = symkron(sh.T, sh.Si, k, sh.bi[a], sh.ci[a], sh.bi[a2], sh.ci[a2]);
-      if (A.mode == 0) {
-        v = Q11[e] + v;
-        v -= (sh.q12[a] * (k1 * sh.q12[a2] + sh.sI[a2]) + sh.sI[a] * (sh.q12[a2] - k2 * sh.sI[a2])) / den;
-      } else {
-        v += (ze / (k1 * ze + 1)) * (sh.sI[a] * sh.sI[a2]);
+    // coefficient matrix (symmetric: lower triangle, mirrored)
+    const double lbc = (A.mode == 1) ? (ze / (k1 * ze + 1)) : 0.0;
+    for (int a = wid; a < s; a += nw) {
+      const int b = sh.bi[a], c = sh.ci[a];
+      for (int a2 = lane; a2 <= a; a2 += 32) {
+        double v = symkron(sh.T, sh.Si, k, b, c, sh.bi[a2], sh.ci[a2]);
+        if (A.mode == 0) {
+          v = Q11[a * s + a2] + v;
+          v -= (sh.q12[a] * (k1 * sh.q12[a2] + sh.sI[a2]) + sh.sI[a] * (sh.q12[a2] - k2 * sh.sI[a2])) / den;
+        } else {
+          v += lbc * (sh.sI[a] * sh.sI[a2]);
+        }
+        coeff[a * s + a2] = v;
+        coeff[a2 * s + a] = v;
       }
-      coeff[e] = v;
+    }
+    if (tid == 0) {
+      if (A.mode == 0) {
+        sc.t1 = (mu / omega + tIS + eta_ - 1 + k1 * (F2 - mu / eta_ + zeta)) / den;
+        sc.t2 = (F2 - mu / eta_ + zeta - k2 * (mu / omega + tIS + eta_ - 1)) / den;
+      } else {
+        sc.t1 = ze * (-k1 * (mu / eta_ - h2 - omega) + mu / omega + tIS + eta_ - 1) / (-k1 * ze - 1);
+        sc.t2 = h2 - mu / eta_;
+      }
     }
     __syncthreads();
     for (int a = tid; a < s; a += IPM_BLOCK) {
       double o;
       if (A.mode == 0) {
         o = -sh.F1[a] + mu * sh.sSi[a] - sh.sT[a];
-        o += ((mu / omega + tIS + eta - 1 + k1 * (F2 - mu / eta + zeta)) / den) * sh.q12[a];
-        o += ((F2 - mu / eta + zeta - k2 * (mu / omega + tIS + eta - 1)) / den) * sh.sI[a];
+        o += sc.t1 * sh.q12[a];
+        o += sc.t2 * sh.sI[a];
       } else {
-        o = ze * (-k1 * (mu / eta - h2 - omega) + mu / omega + tIS + eta - 1) / (-k1 * ze - 1) * sh.sI[a];
-        o += (h2 - mu / eta) * sh.sI[a] - sh.h1[a];
+        o = sc.t1 * sh.sI[a];
+        o += sc.t2 * sh.sI[a] - sh.h1[a];
         o += mu * sh.sSi[a];
       }
       sh.ord[a] = o;
     }
     __syncthreads();
-    if (!block_lu_solve(coeff, s, sh.ord, s, sh.redv, sh.redi)) {
-      if (tid == 0) atomicOr(A.status, ST_SMALL_DENSE_FAIL);
-    }
+    ipm_lu_solve(coeff, s, sh.ord, s, sh.redv, sh.redi, &s_piv, &s_ok);
+    if (tid == 0 && !s_ok) atomicOr(A.status, ST_SMALL_DENSE_FAIL);
     // sh.ord now holds dsS
-    double d_eta, d_omega, d_zeta;
-    if (A.mode == 0) {
-      double t1 = 0.0;
-      for (int a = threadIdx.x & 31; a < s; a += 32) t1 += (k1 * sh.q12[a] + sh.sI[a]) * sh.ord[a];
+    if (wid == 0) {
+      double t1 = 0.0, t2 = 0.0, t3 = 0.0;
+      for (int a = lane; a < s; a += 32) {
+        const double x = sh.ord[a];
+        if (A.mode == 0) {
+          t1 += (k1 * sh.q12[a] + sh.sI[a]) * x;
+          t2 += (sh.q12[a] - k2 * sh.sI[a]) * x;
+          t3 += sh.q12[a] * x;
+        } else {
+          t1 += sh.sI[a] * x;
+        }
+      }
       t1 = warp_sum(t1);
-      d_eta = (-t1 - (mu / omega) - tIS - eta + 1 + k1 * (-F2 + mu / eta - zeta)) / den;
-      double t2 = 0.0;
-      for (int a = threadIdx.x & 31; a < s; a += 32) t2 += (sh.q12[a] - k2 * sh.sI[a]) * sh.ord[a];
-      t2 = warp_sum(t2);
-      d_omega = (-F2 + mu / eta - zeta + k2 * (mu / omega + tIS + eta - 1) - t2) / den;
-      for (int a = tid; a < s; a += IPM_BLOCK) {
+      if (A.mode == 0) { t2 = warp_sum(t2); t3 = warp_sum(t3); }
+      if (lane == 0) {
+        double d_eta, d_omega, d_zeta;
+        if (A.mode == 0) {
+          d_eta = (-t1 - (mu / omega) - tIS - eta_ + 1 + k1 * (-F2 + mu / eta_ - zeta)) / den;
+          d_omega = (-F2 + mu / eta_ - zeta + k2 * (mu / omega + tIS + eta_ - 1) - t2) / den;
+          d_zeta = t3 + d_eta * q22 + d_omega + F2;
+        } else {
+          d_eta = (t1 - k1 * (mu / eta_ - h2 - omega) + mu / omega + tIS + eta_ - 1) / (-k1 * ze - 1);
+          d_omega = -ze * d_eta + mu / eta_;
+          d_omega = d_omega + (-h2 - omega);
+          d_zeta = d_omega - zeta + h2 + omega;
+        }
+        sc.d_eta = d_eta; sc.d_omega = d_omega; sc.d_zeta = d_zeta;
+        // step size from the linear variables (solver/usbs.py:128-132)
+        const double r = nanmin2(nanmin2(d_eta / eta_, d_zeta / zeta), d_omega / omega);
+        double st = -1.0 / r;
+        if (!isnan(st) && st > 1.0) st = 1.0;
+        sc.st = 0.99 * ((st <= 0.0) ? 1.0 : st);
+      }
+    }
+    __syncthreads();
+    const double d_eta = sc.d_eta, d_omega = sc.d_omega;
+    for (int a = tid; a < s; a += IPM_BLOCK) {
+      if (A.mode == 0) {
         double v = 0.0;
         for (int b = 0; b < s; ++b) v += Q11[a * s + b] * sh.ord[b];
         sh.dsT[a] = v + d_eta * sh.q12[a] + d_omega * sh.sI[a] + sh.F1[a];
-      }
-      d_zeta = dot_s(sh.q12, sh.ord, s) + d_eta * q22 + d_omega + F2;
-    } else {
-      const double tI = dot_s(sh.sI, sh.ord, s);
-      d_eta = (tI - k1 * (mu / eta - h2 - omega) + mu / omega + tIS + eta - 1) / (-k1 * ze - 1);
-      d_omega = -ze * d_eta + mu / eta;
-      d_omega = d_omega + (-h2 - omega);
-      for (int a = tid; a < s; a += IPM_BLOCK)
+      } else {
         sh.dsT[a] = d_omega * sh.sI[a] - sh.sT[a] + sh.h1[a] + omega * sh.sI[a];
-      d_zeta = d_omega - zeta + h2 + omega;
+      }
     }
     __syncthreads();
     svec_inv_to(sh.ord, k, s, sh.bi, sh.ci, sh.dS);
     svec_inv_to(sh.dsT, k, s, sh.bi, sh.ci, sh.dT);
     __syncthreads();
-    // ---- step size ----
-    double r = nanmin2(nanmin2(d_eta / eta, d_zeta / zeta), d_omega / omega);
-    double st = -1.0 / r;
-    if (!isnan(st) && st > 1.0) st = 1.0;
-    st = 0.99 * ((st <= 0.0) ? 1.0 : st);
-    double cS = 0.0, cT = 0.0;
-    for (int j = tid; j < A.ipm_grid; j += IPM_BLOCK) {
-      const double a = pow(0.9, (double)j);
-      if (pd_test(sh.S, sh.dS, a, k)) cS = fmax(cS, a);
-      if (pd_test(sh.T, sh.dT, a, k)) cT = fmax(cT, a);
+    // ---- line search over the grid 0.9^j (solver/usbs.py:134-154): the largest
+    // grid step keeping S (lanes 0-15) and T (lanes 16-31) positive definite is the
+    // first positive-definite grid index; batches of 16 with early exit ----
+    if (wid == 0) {
+      const int half = lane >> 4, sub = lane & 15;
+      const double* M = half ? sh.T : sh.S;
+      const double* dM = half ? sh.dT : sh.dS;
+      int firstS = -1, firstT = -1;
+      for (int base = 0; base < ngrid && (firstS < 0 || firstT < 0); base += 16) {
+        const int j = base + sub;
+        const bool need = half ? (firstT < 0) : (firstS < 0);
+        bool pd = false;
+        if (need && j < ngrid) {
+          const double a = (j < 256) ? grid[j] : pow(0.9, (double)j);
+          pd = pd_test(M, dM, a, k);
+        }
+        const unsigned bal = __ballot_sync(0xffffffffu, pd);
+        const unsigned bs = bal & 0xffffu, bt = bal >> 16;
+        if (firstS < 0 && bs) firstS = base + __ffs(bs) - 1;
+        if (firstT < 0 && bt) firstT = base + __ffs(bt) - 1;
+      }
+      if (lane == 0) {
+        const double cS = (firstS < 0) ? 0.0 : (firstS < 256 ? grid[firstS] : pow(0.9, (double)firstS));
+        const double cT = (firstT < 0) ? 0.0 : (firstT < 256 ? grid[firstT] : pow(0.9, (double)firstT));
+        const double cand = (cS < cT) ? cS : cT;
+        double st = sc.st;
+        st = (st < cand) ? st : cand;
+        sc.st = st;
+        sc.eta = eta_ + st * d_eta;
+        sc.zeta = zeta + st * sc.d_zeta;
+        sc.omega = omega + st * d_omega;
+      }
     }
-    cS = block_max(cS, s_red);
     __syncthreads();
-    cT = block_max(cT, s_red);
-    const double cand = (cS < cT) ? cS : cT;
-    st = (st < cand) ? st : cand;
-    __syncthreads();
-    // ---- update ----
+    const double st = sc.st;
     for (int e = tid; e < k * k; e += IPM_BLOCK) {
       sh.S[e] = sh.S[e] + st * sh.dS[e];
       sh.T[e] = sh.T[e] + st * sh.dT[e];
     }
-    eta = eta + st * d_eta;
-    zeta = zeta + st * d_zeta;
-    omega = omega + st * d_omega;
     __syncthreads();
     for (int a = tid; a < s; a += IPM_BLOCK) {
       sh.sS[a] = svec_of(sh.S, k, sh.bi[a], sh.ci[a]);
       sh.sT[a] = svec_of(sh.T, k, sh.bi[a], sh.ci[a]);
     }
     __syncthreads();
-    trS = 0.0;
-    for (int b = 0; b < k; ++b) trS += sh.S[b * k + b];
-    double mun = (dot_s(sh.sS, sh.sT, s) + eta * zeta + omega * (1 - trS - eta)) / (2 * k + 4.0);
-    mun *= (st > 0.2) ? (0.5 - 0.4 * st * st) : 1.0;
-    if (!(isnan(mun) || mun <= mu)) mun = mu;
-    mu = mun;
-    step = st;
-    ++it;
+    if (wid == 0) {
+      const double d = wdot(sh.sS, sh.sT, s);
+      if (lane == 0) {
+        double trS = 0.0;
+        for (int b = 0; b < k; ++b) trS += sh.S[b * k + b];
+        double mun = (d + sc.eta * sc.zeta + sc.omega * (1 - trS - sc.eta)) / (2 * k + 4.0);
+        mun *= (st > 0.2) ? (0.5 - 0.4 * st * st) : 1.0;
+        if (!(isnan(mun) || mun <= mu)) mun = mu;
+        sc.mu = mun;
+        sc.trS = trS;
+        sc.step = st;
+        sc.it = sc.it + 1;
+      }
+    }
     __syncthreads();
   }
   // ---- outputs ----
   if (A.mode == 0) {
     for (int e = tid; e < k * k; e += IPM_BLOCK) sm[A.o_Sout + e] = tr * sh.S[e];
     if (tid == 0) {
-      sm[A.o_sc + SC_ETA] = (tr / tX) * eta;
-      sm[A.o_sc + SC_QITERS] = it;
+      sm[A.o_sc + SC_ETA] = (tr / tX) * sc.eta;
+      sm[A.o_sc + SC_QITERS] = sc.it;
     }
   } else {
-    const double g1S = dot_s(sh.h1, sh.sS, s);
-    if (tid == 0) {
-      sm[A.o_sc + SC_LB] = sm[A.o_sc + SC_BYC] - g1S - eta * h2;
-      sm[A.o_sc + SC_LITERS] = it;
+    if (wid == 0) {
+      const double g1S = wdot(sh.h1, sh.sS, s);
+      if (lane == 0) {
+        sm[A.o_sc + SC_LB] = sm[A.o_sc + SC_BYC] - g1S - sc.eta * h2;
+        sm[A.o_sc + SC_LITERS] = sc.it;
+      }
     }
   }
 }

@@ -57,15 +57,27 @@ struct TeamBatch {
 
 template <typename VT>
 struct LzShared {
-  double ys[LZ_BLOCK];
-  double wred[LZ_NW][MP1];
+  union {
+    struct {                     // Lanczos step phases
+      double ys[LZ_BLOCK];
+      double wred[LZ_NW][MP1];
+    } st;
+    struct {                     // restart on CTA 0 (T, X, R, S, W row-major, ld MP1)
+      double T[MAXM * MP1];
+      double X[MAXM * MP1];
+      double R[MAXM * MP1];      // float copy of T during the Jacobi sweeps
+      double S[MAXM * MP1];      // float eigenvectors during the Jacobi sweeps
+      double W[MAXM * MP1];
+    } rs;
+    VT Ys[MAXM * MAXM];          // saved Ritz vectors, every CTA, after the restart barrier
+  } u;
   double h[MP1];
   double alpha[MAXM];
   double beta[MAXM];
-  double T[MAXM * MP1];
-  double Z[MAXM * MP1];
   double ritz[MAXM];
-  VT Ys[MAXM * MAXM];
+  double red[LZ_NW];
+  float wf[MAXM], rc[MAXM / 2], rsn[MAXM / 2];
+  int pidx[MAXM];
   int order[MAXM];
   int k_next, nconv;
 };
@@ -79,14 +91,14 @@ __device__ __forceinline__ void block_reduce_cols(const AT* acc, int nv, LzShare
   for (int c = 0; c < MP1; ++c) {
     if (c < nv) {
       double v = warp_sum((double)acc[c]);
-      if (lane == 0) sh.wred[wid][c] = v;
+      if (lane == 0) sh.u.st.wred[wid][c] = v;
     }
   }
   __syncthreads();
   for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) {
     double s = 0.0;
 #pragma unroll
-    for (int w = 0; w < LZ_NW; ++w) s += sh.wred[w][c];
+    for (int w = 0; w < LZ_NW; ++w) s += sh.u.st.wred[w][c];
     out[c] = s;
   }
 }
@@ -129,12 +141,12 @@ __device__ void phase_spmv(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0, int 
           s += (AT)P.val[p] * (AT)__ldcg(xsrc + P.col[p]);
       }
       for (int o = L >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lig == 0) sh.ys[rl] = (double)s;
+      if (lig == 0) sh.u.st.ys[rl] = (double)s;
     }
     __syncthreads();
     const int row = base + tid;
     if (row < P.n) {
-      const VT y = (VT)sh.ys[tid] * xscale;
+      const VT y = (VT)sh.u.st.ys[tid] * xscale;
       vout[row] = y;
       VT xn = (VT)0;
       if (wq) {
@@ -237,6 +249,10 @@ __device__ void phase_update_norm(const TeamDesc<VT>& P, LzShared<VT>& sh, int t
 template <typename VT>
 __device__ void restart_select(const TeamDesc<VT>& P, LzShared<VT>& sh, int k) {
   const int m = P.m, tid = threadIdx.x;
+  double* T = sh.u.rs.T;
+  double* X = sh.u.rs.X;
+  float* Tf = (float*)sh.u.rs.R;
+  float* Zf = (float*)sh.u.rs.S;
   for (int e = tid; e < m * m; e += LZ_BLOCK) {
     const int r = e / m, c = e - r * m;
     double v = 0.0;
@@ -245,19 +261,56 @@ __device__ void restart_select(const TeamDesc<VT>& P, LzShared<VT>& sh, int k) {
     else if (r == k && c < k) v = sh.beta[c];
     else if (c == r + 1 && r >= k) v = sh.beta[r];
     else if (r == c + 1 && c >= k) v = sh.beta[c];
-    sh.T[r * MP1 + c] = v;
+    T[r * MP1 + c] = v;
+    Tf[r * MP1 + c] = (float)v;
   }
   __syncthreads();
+  // eigh(T) (solver/lanczos.py:203): FP32 parallel Jacobi by warp 0 ...
   if (tid < 32) {
-    bool ok = warp_syev(sh.T, MP1, m, sh.ritz, sh.Z, MP1);
+    bool ok = warp_jacobi_f32(Tf, MP1, m, sh.wf, Zf, MP1, sh.pidx, sh.rc, sh.rsn);
     if (!ok && tid == 0) atomicOr(P.status, ST_SMALL_DENSE_FAIL);
   }
   __syncthreads();
+  for (int e = tid; e < m * m; e += LZ_BLOCK) {
+    const int r = e / m, c = e - r * m;
+    X[r * MP1 + c] = (double)Zf[r * MP1 + c];
+  }
+  if (tid < m) sh.ritz[tid] = (double)sh.wf[tid];
+  __syncthreads();
+  if (sizeof(VT) == 8) {
+    // ... refined to FP64 accuracy by two Ogita-Aishima steps, then re-sorted
+    cta_refine_eig(T, X, sh.u.rs.R, sh.u.rs.S, sh.u.rs.W, sh.ritz, sh.red, m, MP1);
+    cta_refine_eig(T, X, sh.u.rs.R, sh.u.rs.S, sh.u.rs.W, sh.ritz, sh.red, m, MP1);
+    if (tid == 0) {
+      for (int i = 0; i < m; ++i) sh.order[i] = i;
+      for (int i = 0; i < m - 1; ++i) {
+        int kmin = i;
+        for (int j = i + 1; j < m; ++j)
+          if (sh.ritz[sh.order[j]] < sh.ritz[sh.order[kmin]]) kmin = j;
+        const int t = sh.order[i]; sh.order[i] = sh.order[kmin]; sh.order[kmin] = t;
+      }
+    }
+    __syncthreads();
+    double* Sx = sh.u.rs.S;
+    for (int e = tid; e < m * m; e += LZ_BLOCK) {
+      const int r = e / m, c = e - r * m;
+      Sx[r * MP1 + c] = X[r * MP1 + sh.order[c]];
+    }
+    double rv = (tid < m) ? sh.ritz[sh.order[tid]] : 0.0;
+    __syncthreads();
+    for (int e = tid; e < m * m; e += LZ_BLOCK) {
+      const int r = e / m, c = e - r * m;
+      X[r * MP1 + c] = Sx[r * MP1 + c];
+    }
+    if (tid < m) sh.ritz[tid] = rv;
+    __syncthreads();
+  }
+  const double* Z = X;
   if (tid == 0) {
     const double bl = sh.beta[m - 1];
     int nconv = m;
     for (int c = 0; c < m; ++c) {
-      if (!(bl * fabs(sh.Z[(m - 1) * MP1 + c]) < P.tol)) { nconv = c; break; }
+      if (!(bl * fabs(Z[(m - 1) * MP1 + c]) < P.tol)) { nconv = c; break; }
     }
     const int delta = min(m - P.num_desired, 2 * (m - nconv) / 5);
     const double lt = sh.ritz[min(nconv, m - 1)];
@@ -286,13 +339,13 @@ __device__ void restart_select(const TeamDesc<VT>& P, LzShared<VT>& sh, int k) {
   const double bl = sh.beta[m - 1];
   for (int e = tid; e < m * m; e += LZ_BLOCK) {
     const int j = e / m, c = e - j * m;
-    P.Ybuf[j * m + c] = sh.Z[j * MP1 + sh.order[c]];
+    P.Ybuf[j * m + c] = Z[j * MP1 + sh.order[c]];
   }
   __syncthreads();
   if (tid < m) {
     const int c = tid;
     const double a = (c < kn) ? sh.ritz[sh.order[c]] : 0.0;
-    const double b = (c < kn) ? bl * sh.Z[(m - 1) * MP1 + sh.order[c]] : 0.0;
+    const double b = (c < kn) ? bl * Z[(m - 1) * MP1 + sh.order[c]] : 0.0;
     sh.alpha[c] = a;
     sh.beta[c] = b;
     P.alpha[c] = a;
@@ -302,6 +355,7 @@ __device__ void restart_select(const TeamDesc<VT>& P, LzShared<VT>& sh, int k) {
     P.ctl[0] = kn;
     P.ctl[1] = sh.nconv;
   }
+  __syncthreads();
 }
 
 template <typename VT>
@@ -408,7 +462,7 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
     nconv = __ldcg(P.ctl + 1);
     for (int e = tid; e < m * MAXM; e += LZ_BLOCK) {
       const int j = e / MAXM, c = e - j * MAXM;
-      sh.Ys[e] = (c < kn) ? (VT)__ldcg(P.Ybuf + j * m + c) : (VT)0;
+      sh.u.Ys[e] = (c < kn) ? (VT)__ldcg(P.Ybuf + j * m + c) : (VT)0;
     }
     __syncthreads();
     const VT* last = stepped ? (P.vbuf + (size_t)prev * ld) : (P.Q + (size_t)m * ld);
@@ -425,7 +479,7 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
           VT s = (VT)0;
 #pragma unroll
           for (int j = 0; j < MAXM; ++j)
-            if (j < m) s += qr[j] * sh.Ys[j * MAXM + c];
+            if (j < m) s += qr[j] * sh.u.Ys[j * MAXM + c];
           P.Q[(size_t)c * ld + row] = s;
         }
         P.Q[(size_t)kn * ld + row] = xl;
