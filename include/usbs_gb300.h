@@ -162,6 +162,7 @@ typedef struct usbs_state {
   const double* q0;         /* [n] unit Lanczos start vector (solver/usbs.py:691-692) */
   double* trace;            /* optional [trace_capacity x 20] per-iteration record */
   int trace_capacity;
+  double* debug;            /* optional [8192]: IPM histories of iteration 0 and phase cycles */
   double tr_X, primal_obj;  /* in: starting values; out: final values */
   /* outputs */
   int iterations;

@@ -34,7 +34,7 @@ def _sym_kron(U, T, S_inv):
     return 0.5 * U @ (np.kron(T, S_inv) + np.kron(S_inv, T)) @ U.T
 
 
-def _step_and_mu(st, dS, d_eta, dT, d_zeta, d_omega, k, ipm_max_iters, svec_I, U):
+def _step_and_mu(st, dS, d_eta, dT, d_zeta, d_omega, k, ipm_max_iters, svec_I, U, hist=None):
     numers = np.array([st.eta, st.zeta, st.omega])
     denoms = np.array([d_eta, d_zeta, d_omega])
     with np.errstate(divide="ignore", invalid="ignore"):
@@ -51,6 +51,8 @@ def _step_and_mu(st, dS, d_eta, dT, d_zeta, d_omega, k, ipm_max_iters, svec_I, U
             + omega_n * (1 - svec_I @ svec(U, S_n) - eta_n)) / (2 * k + 4.0)
     mu_n *= (0.5 - 0.4 * step ** 2) if step > 0.2 else 1.0
     mu_n = min(mu_n, st.mu)
+    if hist is not None:
+        hist.append((mu_n, step, eta_n, zeta_n, omega_n, d_eta, d_omega, np.trace(S_n)))
     return IPMState(st.i + 1, S_n, eta_n, T_n, zeta_n, omega_n, mu_n, step)
 
 
@@ -116,7 +118,7 @@ def solve_quad_subprob_ipm(U, k, trace_ub, consts, eta_init, S_init, ipm_eps, ip
         dsT = Q_11 @ dsS + d_eta * q_12 + d_omega * svec_I + F_1
         d_zeta = q_12 @ dsS + d_eta * q_22 + d_omega + F_2
         return _step_and_mu(st, svec_inv(U, dsS, k), d_eta, svec_inv(U, dsT, k), d_zeta, d_omega,
-                            k, ipm_max_iters, svec_I, U)
+                            k, ipm_max_iters, svec_I, U, None if info is None else info.get("qhist"))
 
     init = IPMState(0, S0, eta0, T0, zeta0, omega0, mu0, 1.0)
     fin = while_loop(lambda s: (s.mu > ipm_eps) and (s.step_size > ipm_eps ** 2), body, init,

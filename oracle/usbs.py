@@ -91,7 +91,7 @@ def usbs(sdp_state, n, m, trace_ub, trace_factor, rho, beta, k_curr, k_past, max
             or st["max_infeas"] > max_infeas_eps))
 
     def body(st):
-        info = {}
+        info = {"qhist": []}
         V = st["V"]
         CV = C @ V
         eta, S, ups_n, G_C = solve_step_subprob(

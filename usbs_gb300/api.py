@@ -134,10 +134,12 @@ class EigshInfo:
     def __init__(self, raw):
         self.k_saved, self.num_converged, self.restarts, self.breakdowns, self.matvecs, \
             self.status = (int(v) for v in raw[:6])
+        self.restart_kcycles, self.total_kcycles = int(raw[6]), int(raw[7])
 
     def __repr__(self):
         return (f"EigshInfo(restarts={self.restarts}, converged={self.num_converged}, "
-                f"matvecs={self.matvecs}, breakdowns={self.breakdowns}, status={self.status})")
+                f"matvecs={self.matvecs}, breakdowns={self.breakdowns}, status={self.status}, "
+                f"restart_kcycles={self.restart_kcycles}, total_kcycles={self.total_kcycles})")
 
 
 def eigsh_smallest(n, C, A_data, A_indices, adjoint_left_vec, q0, num_desired, inner_iterations,

@@ -156,13 +156,17 @@ __device__ inline bool warp_syev(double* A, int lda, int n, double* w, double* Z
 // Cyclic parallel Jacobi eigensolver (float) for a symmetric n x n matrix by
 // one warp: n/2 disjoint rotations per round in round-robin ("chess
 // tournament") order, Rutishauser's rotation formulas, sweeps until the
-// off-diagonal Frobenius norm is below 4 eps ||A||_F.  A (row-major lda) is
-// destroyed; w receives the eigenvalues ascending, Z (row-major ldz) the
-// eigenvectors as columns.  n <= 32.  Returns false if 20 sweeps do not converge.
+// off-diagonal Frobenius norm is below 4 eps ||A||_F.  A (row-major lda >= M)
+// is destroyed; w receives the eigenvalues ascending, Z (row-major ldz >= M)
+// the eigenvectors as columns.  n <= 32, M = n rounded up to even.  Lane j owns
+// column j in the row phase and row j in the column phase, so no index
+// arithmetic is needed inside a round.  Returns false if 20 sweeps do not
+// converge.  pidx needs 2*16 ints, rc/rs 16 floats each.
 __device__ inline bool warp_jacobi_f32(float* A, int lda, int n, float* w, float* Z, int ldz,
                                        int* pidx, float* rc, float* rs) {
   const int lane = threadIdx.x & 31;
   const int M = (n + 1) & ~1;  // even order; a padding index couples to nothing
+  const int half = M >> 1;
   for (int i = 0; i < M; ++i)
     if (lane < M) Z[i * ldz + lane] = (i == lane) ? 1.0f : 0.0f;
   if (M > n && lane < M) { A[n * lda + lane] = 0.0f; A[lane * lda + n] = 0.0f; }
@@ -175,7 +179,6 @@ __device__ inline bool warp_jacobi_f32(float* A, int lda, int n, float* w, float
   fro = warp_sum(fro);
   const float tol2 = fro * (4.0f * 1.2e-7f) * (4.0f * 1.2e-7f);
   bool ok = false;
-  const int half = M >> 1;
   for (int sweep = 0; sweep < 20; ++sweep) {
     float off = 0.0f;
     for (int i = 0; i < n; ++i) {
@@ -187,47 +190,49 @@ __device__ inline bool warp_jacobi_f32(float* A, int lda, int n, float* w, float
     for (int r = 0; r < M - 1; ++r) {
       if (lane < half) {
         int p, q;
-        if (lane == 0) { p = 0; q = 1 + r % (M - 1); }
+        if (lane == 0) { p = 0; q = 1 + r; }
         else {
-          p = 1 + (r + lane) % (M - 1);
-          q = 1 + (r - lane + M - 1) % (M - 1);
+          p = r + lane; p = (p >= M - 1) ? p - (M - 1) : p; p += 1;
+          q = r - lane + M - 1; q = (q >= M - 1) ? q - (M - 1) : q; q += 1;
         }
         if (p > q) { const int t = p; p = q; q = t; }
         const float apq = A[p * lda + q];
-        float c = 1.0f, s = 0.0f;
+        float c = 1.0f, sn = 0.0f;
         if (apq != 0.0f) {
           const float theta = (A[q * lda + q] - A[p * lda + p]) / (2.0f * apq);
           const float t = copysignf(1.0f, theta) / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
           c = rsqrtf(t * t + 1.0f);
-          s = t * c;
+          sn = t * c;
         }
         pidx[2 * lane] = p;
         pidx[2 * lane + 1] = q;
         rc[lane] = c;
-        rs[lane] = s;
+        rs[lane] = sn;
       }
       __syncwarp();
-      // rows: (J^T A)
-      for (int e = lane; e < half * M; e += 32) {
-        const int pr = e / M, j = e - pr * M;
-        const int p = pidx[2 * pr], q = pidx[2 * pr + 1];
-        const float c = rc[pr], s = rs[pr];
-        const float ap = A[p * lda + j], aq = A[q * lda + j];
-        A[p * lda + j] = c * ap - s * aq;
-        A[q * lda + j] = s * ap + c * aq;
+      if (lane < M) {
+        // rows (J^T A): lane = column
+        for (int pr = 0; pr < half; ++pr) {
+          const int p = pidx[2 * pr], q = pidx[2 * pr + 1];
+          const float c = rc[pr], sn = rs[pr];
+          const float ap = A[p * lda + lane], aq = A[q * lda + lane];
+          A[p * lda + lane] = c * ap - sn * aq;
+          A[q * lda + lane] = sn * ap + c * aq;
+        }
       }
       __syncwarp();
-      // columns: (. J) and eigenvectors Z J
-      for (int e = lane; e < half * M; e += 32) {
-        const int pr = e / M, j = e - pr * M;
-        const int p = pidx[2 * pr], q = pidx[2 * pr + 1];
-        const float c = rc[pr], s = rs[pr];
-        const float ap = A[j * lda + p], aq = A[j * lda + q];
-        A[j * lda + p] = c * ap - s * aq;
-        A[j * lda + q] = s * ap + c * aq;
-        const float zp = Z[j * ldz + p], zq = Z[j * ldz + q];
-        Z[j * ldz + p] = c * zp - s * zq;
-        Z[j * ldz + q] = s * zp + c * zq;
+      if (lane < M) {
+        // columns (A J) and Z J: lane = row
+        for (int pr = 0; pr < half; ++pr) {
+          const int p = pidx[2 * pr], q = pidx[2 * pr + 1];
+          const float c = rc[pr], sn = rs[pr];
+          const float ap = A[lane * lda + p], aq = A[lane * lda + q];
+          A[lane * lda + p] = c * ap - sn * aq;
+          A[lane * lda + q] = sn * ap + c * aq;
+          const float zp = Z[lane * ldz + p], zq = Z[lane * ldz + q];
+          Z[lane * ldz + p] = c * zp - sn * zq;
+          Z[lane * ldz + q] = sn * zp + c * zq;
+        }
       }
       __syncwarp();
     }

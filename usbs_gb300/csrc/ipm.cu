@@ -35,6 +35,7 @@ struct IpmShared {
   double dS[IPM_MAXK * IPM_MAXK], dT[IPM_MAXK * IPM_MAXK], wk[IPM_MAXK * IPM_MAXK];
   double redv[IPM_BLOCK / 32];
   int redi[IPM_BLOCK / 32];
+  double lcol[IPM_MAXS];
 };
 
 // sum_a x[a] y[a], computed redundantly by every warp (identical in all threads)
@@ -109,9 +110,11 @@ __device__ __forceinline__ double wdot(const double* x, const double* y, int s) 
   return warp_sum(v);
 }
 
-// LU with partial pivoting and solve, whole CTA: warps over rows, lanes over
-// columns; multipliers formed once (lane 0) and broadcast through shared memory.
-__device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* redv, int* redi,
+// LU with partial pivoting and solve, whole CTA (G&VL Alg. 3.4.1).  Per column:
+// warp 0 finds the pivot, the rows are swapped, the multipliers of all rows are
+// formed in parallel (one thread per row) into `lcol`, then the trailing update
+// runs with warps over rows and lanes over columns.
+__device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* redv, double* lcol,
                              int* piv_out, int* ok_out) {
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
   if (tid == 0) *ok_out = 1;
@@ -147,14 +150,16 @@ __device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* redv,
     }
     const double inv = redv[0];
     const double bj = b[j];
+    for (int i = j + 1 + tid; i < n; i += blockDim.x) {
+      const double l = A[i * lda + j] * inv;
+      A[i * lda + j] = l;
+      lcol[i] = l;
+      b[i] -= l * bj;
+    }
+    __syncthreads();
+#pragma unroll 4
     for (int i = j + 1 + wid; i < n; i += nw) {
-      if (lane == 0) {
-        const double l = A[i * lda + j] * inv;
-        A[i * lda + j] = l;
-        b[i] -= l * bj;
-      }
-      __syncwarp();
-      const double l = A[i * lda + j];
+      const double l = lcol[i];
       for (int c = j + 1 + lane; c < n; c += 32) A[i * lda + c] -= l * A[j * lda + c];
     }
     __syncthreads();
@@ -166,7 +171,6 @@ __device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* redv,
     for (int i = tid; i < j; i += blockDim.x) b[i] -= A[i * lda + j] * bj;
     __syncthreads();
   }
-  (void)redi;
 }
 
 __global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ IpmArgs A) {
@@ -282,7 +286,9 @@ __global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ 
   __syncthreads();
   const int maxit = A.max_iters;
   const double eps = A.eps;
+  long long ph0 = 0, ph1 = 0, ph2 = 0, ph3 = 0, tclk = 0;
   while (true) {
+    if (tid == 0) tclk = clock64();
     if (tid == 0) {
       const bool cont = (sc.it < maxit) &&
           ((A.mode == 0) ? (sc.mu > eps && sc.step > eps * eps) : (sc.mu > eps));
@@ -323,11 +329,13 @@ __global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ 
     __syncthreads();
     const double F2 = (A.mode == 0) ? sc.F2 : 0.0;
     for (int a = tid; a < s; a += IPM_BLOCK) sh.sSi[a] = svec_of(sh.Si, k, sh.bi[a], sh.ci[a]);
-    // coefficient matrix (symmetric: lower triangle, mirrored)
+    // coefficient matrix, every entry computed (S^-1 is not exactly symmetric in
+    // floating point; mirroring one triangle measurably degrades the Newton
+    // steps once the system is ill-conditioned near the end of the IPM)
     const double lbc = (A.mode == 1) ? (ze / (k1 * ze + 1)) : 0.0;
     for (int a = wid; a < s; a += nw) {
       const int b = sh.bi[a], c = sh.ci[a];
-      for (int a2 = lane; a2 <= a; a2 += 32) {
+      for (int a2 = lane; a2 < s; a2 += 32) {
         double v = symkron(sh.T, sh.Si, k, b, c, sh.bi[a2], sh.ci[a2]);
         if (A.mode == 0) {
           v = Q11[a * s + a2] + v;
@@ -336,7 +344,6 @@ __global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ 
           v += lbc * (sh.sI[a] * sh.sI[a2]);
         }
         coeff[a * s + a2] = v;
-        coeff[a2 * s + a] = v;
       }
     }
     if (tid == 0) {
@@ -363,7 +370,9 @@ __global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ 
       sh.ord[a] = o;
     }
     __syncthreads();
-    ipm_lu_solve(coeff, s, sh.ord, s, sh.redv, sh.redi, &s_piv, &s_ok);
+    if (tid == 0) { const long long c = clock64(); ph0 += c - tclk; tclk = c; }
+    ipm_lu_solve(coeff, s, sh.ord, s, sh.redv, sh.lcol, &s_piv, &s_ok);
+    if (tid == 0) { const long long c = clock64(); ph1 += c - tclk; tclk = c; }
     if (tid == 0 && !s_ok) atomicOr(A.status, ST_SMALL_DENSE_FAIL);
     // sh.ord now holds dsS
     if (wid == 0) {
@@ -449,6 +458,7 @@ __global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ 
       }
     }
     __syncthreads();
+    if (tid == 0) { const long long c = clock64(); ph2 += c - tclk; tclk = c; }
     const double st = sc.st;
     for (int e = tid; e < k * k; e += IPM_BLOCK) {
       sh.S[e] = sh.S[e] + st * sh.dS[e];
@@ -468,6 +478,11 @@ __global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ 
         double mun = (d + sc.eta * sc.zeta + sc.omega * (1 - trS - sc.eta)) / (2 * k + 4.0);
         mun *= (st > 0.2) ? (0.5 - 0.4 * st * st) : 1.0;
         if (!(isnan(mun) || mun <= mu)) mun = mu;
+        if (A.dbg && sc.it < 128) {
+          double* d = A.dbg + sc.it * 8;
+          d[0] = mun; d[1] = st; d[2] = sc.eta; d[3] = sc.zeta; d[4] = sc.omega;
+          d[5] = sc.d_eta; d[6] = sc.d_omega; d[7] = trS;
+        }
         sc.mu = mun;
         sc.trS = trS;
         sc.step = st;
@@ -475,6 +490,11 @@ __global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ 
       }
     }
     __syncthreads();
+    if (tid == 0) { const long long c = clock64(); ph3 += c - tclk; }
+  }
+  if (tid == 0 && A.prof) {
+    A.prof[0] += (double)ph0; A.prof[1] += (double)ph1; A.prof[2] += (double)ph2;
+    A.prof[3] += (double)ph3;
   }
   // ---- outputs ----
   if (A.mode == 0) {

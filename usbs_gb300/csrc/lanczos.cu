@@ -82,10 +82,12 @@ struct LzShared {
   int k_next, nconv;
 };
 
-// acc[c] (c < nv) summed over the CTA, written to out[c]
+// acc[c] (c < nv) summed over the CTA, written to out[c * R] (column-major
+// [column][cta] partial layout, so the team reduction reads each column in one
+// coalesced load)
 template <typename VT, typename AT>
 __device__ __forceinline__ void block_reduce_cols(const AT* acc, int nv, LzShared<VT>& sh,
-                                                  double* out) {
+                                                  double* out, int R) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
   for (int c = 0; c < MP1; ++c) {
@@ -99,20 +101,31 @@ __device__ __forceinline__ void block_reduce_cols(const AT* acc, int nv, LzShare
     double s = 0.0;
 #pragma unroll
     for (int w = 0; w < LZ_NW; ++w) s += sh.u.st.wred[w][c];
-    out[c] = s;
+    out[(size_t)c * R] = s;
   }
 }
 
-// h[c] = sum over the team's CTAs of part_pass[r][c], identical order in every CTA
+// h[c] = sum over the team's CTAs of part_pass[c][r], identical order in every
+// CTA.  Warp w owns columns w, w+8, ...; all its loads are issued before the
+// warp sums.
+constexpr int CPW = (MP1 + LZ_NW - 1) / LZ_NW;
 template <typename VT>
 __device__ __forceinline__ void reduce_part(const double* part_pass, int R, int nv,
                                             LzShared<VT>& sh) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  for (int c = wid; c < nv; c += LZ_NW) {
-    double s = 0.0;
-    for (int r = lane; r < R; r += 32) s += __ldcg(part_pass + (size_t)r * MP1 + c);
-    s = warp_sum(s);
-    if (lane == 0) sh.h[c] = s;
+  double acc[CPW];
+#pragma unroll
+  for (int j = 0; j < CPW; ++j) {
+    acc[j] = 0.0;
+    const int c = wid + j * LZ_NW;
+    if (c < nv)
+      for (int r = lane; r < R; r += 32) acc[j] += __ldcg(part_pass + (size_t)c * R + r);
+  }
+#pragma unroll
+  for (int j = 0; j < CPW; ++j) {
+    const int c = wid + j * LZ_NW;
+    const double s = warp_sum(acc[j]);
+    if (lane == 0 && c < nv) sh.h[c] = s;
   }
   __syncthreads();
 }
@@ -163,7 +176,7 @@ __device__ void phase_spmv(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0, int 
     }
     __syncthreads();
   }
-  block_reduce_cols(acc, i + 1, sh, part_out);
+  block_reduce_cols(acc, i + 1, sh, part_out, P.nctas);
 }
 
 // Breakdown pass a: buf = hash_normal(key) for own rows, acc[c] = Q[:, c] . buf (c < nv)
@@ -185,7 +198,7 @@ __device__ void phase_random(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0, in
         if (c < nv) acc[c] += (AT)P.Q[(size_t)c * ld + row] * (AT)r;
     }
   }
-  block_reduce_cols(acc, nv, sh, part_out);
+  block_reduce_cols(acc, nv, sh, part_out, P.nctas);
 }
 
 // Phase B: buf -= Q h (c < nv); acc[c] = Q[:, c] . buf
@@ -216,7 +229,7 @@ __device__ void phase_update_dot(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0
         if (c < nv) acc[c] += (AT)qr[c] * (AT)q1;
     }
   }
-  block_reduce_cols(acc, nv, sh, part_out);
+  block_reduce_cols(acc, nv, sh, part_out, P.nctas);
 }
 
 // Phase C: buf -= Q h (c < nv); part_out[0] = sum buf^2 over own rows
@@ -240,7 +253,7 @@ __device__ void phase_update_norm(const TeamDesc<VT>& P, LzShared<VT>& sh, int t
   }
   AT one[MP1];
   one[0] = nrm;
-  block_reduce_cols(one, 1, sh, part_out);
+  block_reduce_cols(one, 1, sh, part_out, P.nctas);
 }
 
 // CTA 0 of a team: projected eigenproblem and thick-restart selection
@@ -374,11 +387,13 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
   const int ntiles = (n + LZ_BLOCK - 1) / LZ_BLOCK;
   const int t0 = (int)((long long)ntiles * rank / R);
   const int t1 = (int)((long long)ntiles * (rank + 1) / R);
+  // [pass][column][cta] partial sums
   double* part0 = P.part;
   double* part1 = P.part + (size_t)R * MP1;
   double* part2 = P.part + (size_t)2 * R * MP1;
 
   int k = 0, nconv = 0, restart = 0, breakdowns = 0, steps = 0;
+  long long clk_start = clock64(), clk_restart = 0;
   if (rank == 0 && tid < MAXM) { sh.alpha[tid] = 0.0; sh.beta[tid] = 0.0; }
   __syncthreads();
   int prev = 0;          // vbuf slot holding the latest unnormalised vector
@@ -401,13 +416,13 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
           // against Q[:, :i] (solver/lanczos.py:107-117)
           ++breakdowns;
           VT* buf = P.vbuf + (size_t)prev * ld;
-          phase_random(P, sh, t0, t1, i, (uint64_t)i, buf, part0 + (size_t)rank * MP1);
+          phase_random(P, sh, t0, t1, i, (uint64_t)i, buf, part0 + rank);
           if (!bar.sync()) return;
           reduce_part(part0, R, i, sh);
-          phase_update_dot(P, sh, t0, t1, i, buf, part1 + (size_t)rank * MP1);
+          phase_update_dot(P, sh, t0, t1, i, buf, part1 + rank);
           if (!bar.sync()) return;
           reduce_part(part1, R, i, sh);
-          phase_update_norm(P, sh, t0, t1, i, buf, part2 + (size_t)rank * MP1);
+          phase_update_norm(P, sh, t0, t1, i, buf, part2 + rank);
           if (!bar.sync()) return;
           reduce_part(part2, R, 1, sh);
           invb = (VT)(1.0 / sqrt(sh.h[0]));
@@ -418,15 +433,15 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
         wq = true;
       }
       VT* vout = P.vbuf + (size_t)cur * ld;
-      phase_spmv(P, sh, t0, t1, i, xsrc, invb, wq, vout, part0 + (size_t)rank * MP1);
+      phase_spmv(P, sh, t0, t1, i, xsrc, invb, wq, vout, part0 + rank);
       if (!bar.sync()) return;
       reduce_part(part0, R, i + 1, sh);
       const double h1i = sh.h[i];
-      phase_update_dot(P, sh, t0, t1, i + 1, vout, part1 + (size_t)rank * MP1);
+      phase_update_dot(P, sh, t0, t1, i + 1, vout, part1 + rank);
       if (!bar.sync()) return;
       reduce_part(part1, R, i + 1, sh);
       if (rank == 0 && tid == 0) sh.alpha[i] = h1i + sh.h[i];
-      phase_update_norm(P, sh, t0, t1, i + 1, vout, part2 + (size_t)rank * MP1);
+      phase_update_norm(P, sh, t0, t1, i + 1, vout, part2 + rank);
       if (!bar.sync()) return;
       prev = cur;
       cur ^= 1;
@@ -441,13 +456,13 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
       if (b < 1e-15) {
         ++breakdowns;
         VT* buf = P.vbuf + (size_t)prev * ld;
-        phase_random(P, sh, t0, t1, m, (uint64_t)m, buf, part0 + (size_t)rank * MP1);
+        phase_random(P, sh, t0, t1, m, (uint64_t)m, buf, part0 + rank);
         if (!bar.sync()) return;
         reduce_part(part0, R, m, sh);
-        phase_update_dot(P, sh, t0, t1, m, buf, part1 + (size_t)rank * MP1);
+        phase_update_dot(P, sh, t0, t1, m, buf, part1 + rank);
         if (!bar.sync()) return;
         reduce_part(part1, R, m, sh);
-        phase_update_norm(P, sh, t0, t1, m, buf, part2 + (size_t)rank * MP1);
+        phase_update_norm(P, sh, t0, t1, m, buf, part2 + rank);
         if (!bar.sync()) return;
         reduce_part(part2, R, 1, sh);
         invb = (VT)(1.0 / sqrt(sh.h[0]));
@@ -456,7 +471,11 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
       }
     }
     __syncthreads();
-    if (rank == 0) restart_select(P, sh, k);
+    if (rank == 0) {
+      const long long c0 = clock64();
+      restart_select(P, sh, k);
+      clk_restart += clock64() - c0;
+    }
     if (!bar.sync()) return;
     const int kn = __ldcg(P.ctl + 0);
     nconv = __ldcg(P.ctl + 1);
@@ -494,6 +513,8 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
     P.ctl[2] = restart;
     P.ctl[3] = breakdowns;
     P.ctl[4] = steps;
+    P.ctl[6] = (int)(clk_restart >> 10);
+    P.ctl[7] = (int)((clock64() - clk_start) >> 10);
     if (restart == 0) P.ctl[0] = 0;
   }
 }

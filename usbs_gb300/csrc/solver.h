@@ -60,6 +60,8 @@ struct IpmArgs {
   int o_sc, o_QB, o_GZ, o_GYmC, o_GB, o_GYC, o_Ssub, o_Sout;
   int* status;
   const int* skip;     // non-zero: instance inactive, kernel returns
+  double* dbg;         // optional: per-iteration history, 8 doubles per IPM iteration
+  double* prof;        // optional: clock64 cycles per phase (4 doubles, accumulated)
 };
 
 struct EigSArgs {

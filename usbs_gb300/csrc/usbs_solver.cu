@@ -766,8 +766,12 @@ struct Solver {
     a.o_sc = L.o_sc; a.o_QB = L.o_QB; a.o_GZ = L.o_GZ; a.o_GYmC = L.o_GYmC; a.o_GB = L.o_GB;
     a.o_GYC = L.o_GYC; a.o_Ssub = L.o_Ssub; a.o_Sout = L.o_Sout; a.status = L.status;
     a.skip = nullptr;
+    a.dbg = nullptr;
+    a.prof = S->debug ? S->debug + 4096 + 8 * mode : nullptr;
+    if (S->debug && cur_t == 0) a.dbg = S->debug + 1024 * mode;
     return a;
   }
+  int cur_t = 0;
   int run_ipm(int mode) { return launch_ipm(ipm_args(mode), st); }
   int read_scalars(double* out, int first, int count) {
     if (cudaMemcpyAsync(out, L.smalls + L.o_sc + first, count * sizeof(double),
@@ -784,6 +788,7 @@ struct Solver {
 };
 
 static int body(Solver& X, int t) {
+  X.cur_t = t;
   Layout& L = X.L;
   const usbs_problem* P = X.P;
   const usbs_params* Pa = X.Pa;

@@ -52,7 +52,7 @@ class UsbsParams(ctypes.Structure):
 class UsbsState(ctypes.Structure):
     _fields_ = [("ld", ctypes.c_int)] + [(f, P) for f in ("y", "z", "V", "P", "Omega", "X", "q0",
                                                           "trace")] + \
-        [("trace_capacity", ctypes.c_int), ("tr_X", ctypes.c_double),
+        [("trace_capacity", ctypes.c_int), ("debug", P), ("tr_X", ctypes.c_double),
          ("primal_obj", ctypes.c_double), ("iterations", ctypes.c_int),
          ("obj_gap", ctypes.c_double), ("infeas_gap", ctypes.c_double),
          ("max_infeas", ctypes.c_double), ("obj_ub", ctypes.c_double),
@@ -138,7 +138,7 @@ def usbs(sdp_state, n, m, trace_ub, trace_factor, rho, beta, k_curr, k_past, max
          lanczos_max_restarts, subprob_eps, subprob_max_iters, cond_exp_base=1.0,
          callback_fn=None, callback_static_args=None, callback_nonstatic_args=None, *, q0=None,
          precision=64, device="cuda", return_trace=False, return_info=False, instance=None,
-         stream=None):
+         stream=None, debug=None):
     import torch
     if not torch.cuda.is_available():
         raise RuntimeError("usbs_gb300.usbs needs a CUDA device (GB300); none is visible")
@@ -189,6 +189,7 @@ def usbs(sdp_state, n, m, trace_ub, trace_factor, rho, beta, k_curr, k_past, max
     pst.y, pst.z, pst.V = _ptr(y), _ptr(z), _ptr(V)
     pst.P, pst.Omega, pst.X, pst.q0, pst.trace = _ptr(Pm), _ptr(Om), _ptr(X), _ptr(q0t), _ptr(trace)
     pst.trace_capacity = int(max_iters) if return_trace else 0
+    pst.debug = _ptr(debug)
     pst.tr_X, pst.primal_obj = float(sdp_state.tr_X), float(sdp_state.primal_obj)
     prob = inst.c_struct()
     need = int(lib.usbs_solve_workspace_bytes(ctypes.byref(prob), ctypes.byref(prm)))
