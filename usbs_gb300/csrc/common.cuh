@@ -36,6 +36,26 @@ __device__ __forceinline__ double warp_max(double v) {
   return v;
 }
 
+// Reduce-scatter of 32 per-lane columns across a warp: on return lane l holds
+// the warp-wide sum of column l.  Butterfly with halving payload: 16+8+4+2+1
+// shuffle-adds per lane instead of 32 x 5 for 32 separate warp sums.  x is
+// consumed.  All 32 lanes must call it.
+template <typename T>
+__device__ __forceinline__ T warp_reduce_scatter32(T* x) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int h = 16; h >= 1; h >>= 1) {
+    const bool up = (lane & h) != 0;
+#pragma unroll
+    for (int j = 0; j < h; ++j) {
+      const T send = up ? x[j] : x[j + h];
+      const T keep = up ? x[j + h] : x[j];
+      x[j] = keep + __shfl_xor_sync(0xffffffffu, send, h);
+    }
+  }
+  return x[0];
+}
+
 // Sum of one double per thread over the block; result returned to every thread.
 // `red` needs blockDim.x/32 doubles of shared memory.
 __device__ __forceinline__ double block_sum(double v, double* red) {

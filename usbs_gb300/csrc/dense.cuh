@@ -154,41 +154,41 @@ __device__ inline bool warp_syev(double* A, int lda, int n, double* w, double* Z
 }
 
 // Cyclic parallel Jacobi eigensolver (float) for a symmetric n x n matrix by
-// one warp: n/2 disjoint rotations per round in round-robin ("chess
+// one warp, always run at order 32 (indices >= n are padding that couples to
+// nothing): 16 disjoint rotations per round in round-robin ("chess
 // tournament") order, Rutishauser's rotation formulas, sweeps until the
-// off-diagonal Frobenius norm is below 4 eps ||A||_F.  A (row-major lda >= M)
-// is destroyed; w receives the eigenvalues ascending, Z (row-major ldz >= M)
-// the eigenvectors as columns.  n <= 32, M = n rounded up to even.  Lane j owns
-// column j in the row phase and row j in the column phase, so no index
-// arithmetic is needed inside a round.  Returns false if 20 sweeps do not
-// converge.  pidx needs 2*16 ints, rc/rs 16 floats each.
+// off-diagonal Frobenius norm is below 4 eps ||A||_F.  A (row-major lda >= 32)
+// is destroyed; w receives the eigenvalues ascending, Z (row-major ldz >= 32)
+// the eigenvectors as columns.  Lane j owns column j in the row phase and row j
+// in the column phase; every loop has a fixed trip count.  Returns false if 20
+// sweeps do not converge.  pidx needs 32 ints, rc/rs 16 floats each.
 __device__ inline bool warp_jacobi_f32(float* A, int lda, int n, float* w, float* Z, int ldz,
                                        int* pidx, float* rc, float* rs) {
   const int lane = threadIdx.x & 31;
-  const int M = (n + 1) & ~1;  // even order; a padding index couples to nothing
-  const int half = M >> 1;
-  for (int i = 0; i < M; ++i)
-    if (lane < M) Z[i * ldz + lane] = (i == lane) ? 1.0f : 0.0f;
-  if (M > n && lane < M) { A[n * lda + lane] = 0.0f; A[lane * lda + n] = 0.0f; }
+  constexpr int M = 32, H = 16;
+#pragma unroll 4
+  for (int i = 0; i < M; ++i) {
+    Z[i * ldz + lane] = (i == lane) ? 1.0f : 0.0f;
+    if (i >= n || lane >= n) A[i * lda + lane] = 0.0f;
+  }
   __syncwarp();
   float fro = 0.0f;
-  for (int i = 0; i < n; ++i) {
-    const float a = (lane < n) ? A[i * lda + lane] : 0.0f;
-    fro += a * a;
-  }
+#pragma unroll 4
+  for (int i = 0; i < M; ++i) { const float a = A[i * lda + lane]; fro += a * a; }
   fro = warp_sum(fro);
   const float tol2 = fro * (4.0f * 1.2e-7f) * (4.0f * 1.2e-7f);
   bool ok = false;
   for (int sweep = 0; sweep < 20; ++sweep) {
     float off = 0.0f;
-    for (int i = 0; i < n; ++i) {
-      const float a = (lane < n && lane != i) ? A[i * lda + lane] : 0.0f;
+#pragma unroll 4
+    for (int i = 0; i < M; ++i) {
+      const float a = (lane != i) ? A[i * lda + lane] : 0.0f;
       off += a * a;
     }
     off = warp_sum(off);
     if (off <= tol2) { ok = true; break; }
     for (int r = 0; r < M - 1; ++r) {
-      if (lane < half) {
+      if (lane < H) {
         int p, q;
         if (lane == 0) { p = 0; q = 1 + r; }
         else {
@@ -210,35 +210,33 @@ __device__ inline bool warp_jacobi_f32(float* A, int lda, int n, float* w, float
         rs[lane] = sn;
       }
       __syncwarp();
-      if (lane < M) {
-        // rows (J^T A): lane = column
-        for (int pr = 0; pr < half; ++pr) {
-          const int p = pidx[2 * pr], q = pidx[2 * pr + 1];
-          const float c = rc[pr], sn = rs[pr];
-          const float ap = A[p * lda + lane], aq = A[q * lda + lane];
-          A[p * lda + lane] = c * ap - sn * aq;
-          A[q * lda + lane] = sn * ap + c * aq;
-        }
+      // rows (J^T A): lane = column
+#pragma unroll
+      for (int pr = 0; pr < H; ++pr) {
+        const int p = pidx[2 * pr], q = pidx[2 * pr + 1];
+        const float c = rc[pr], sn = rs[pr];
+        const float ap = A[p * lda + lane], aq = A[q * lda + lane];
+        A[p * lda + lane] = c * ap - sn * aq;
+        A[q * lda + lane] = sn * ap + c * aq;
       }
       __syncwarp();
-      if (lane < M) {
-        // columns (A J) and Z J: lane = row
-        for (int pr = 0; pr < half; ++pr) {
-          const int p = pidx[2 * pr], q = pidx[2 * pr + 1];
-          const float c = rc[pr], sn = rs[pr];
-          const float ap = A[lane * lda + p], aq = A[lane * lda + q];
-          A[lane * lda + p] = c * ap - sn * aq;
-          A[lane * lda + q] = sn * ap + c * aq;
-          const float zp = Z[lane * ldz + p], zq = Z[lane * ldz + q];
-          Z[lane * ldz + p] = c * zp - sn * zq;
-          Z[lane * ldz + q] = sn * zp + c * zq;
-        }
+      // columns (A J) and Z J: lane = row
+#pragma unroll
+      for (int pr = 0; pr < H; ++pr) {
+        const int p = pidx[2 * pr], q = pidx[2 * pr + 1];
+        const float c = rc[pr], sn = rs[pr];
+        const float ap = A[lane * lda + p], aq = A[lane * lda + q];
+        A[lane * lda + p] = c * ap - sn * aq;
+        A[lane * lda + q] = sn * ap + c * aq;
+        const float zp = Z[lane * ldz + p], zq = Z[lane * ldz + q];
+        Z[lane * ldz + p] = c * zp - sn * zq;
+        Z[lane * ldz + q] = sn * zp + c * zq;
       }
       __syncwarp();
     }
   }
   // eigenvalues from the diagonal, sorted ascending with their vectors
-  for (int i = lane; i < n; i += 32) w[i] = A[i * lda + i];
+  if (lane < n) w[lane] = A[lane * lda + lane];
   __syncwarp();
   for (int i = 0; i < n - 1; ++i) {
     int kmin = i;

@@ -84,17 +84,20 @@ struct LzShared {
 
 // acc[c] (c < nv) summed over the CTA, written to out[c * R] (column-major
 // [column][cta] partial layout, so the team reduction reads each column in one
-// coalesced load)
+// coalesced load).  Columns 0..31 are reduced across each warp by one
+// butterfly reduce-scatter (lane c ends with column c), column 32 by a warp sum.
 template <typename VT, typename AT>
-__device__ __forceinline__ void block_reduce_cols(const AT* acc, int nv, LzShared<VT>& sh,
-                                                  double* out, int R) {
+__device__ __forceinline__ void block_reduce_cols(AT* acc, int nv, LzShared<VT>& sh, double* out,
+                                                  int R) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-  for (int c = 0; c < MP1; ++c) {
-    if (c < nv) {
-      double v = warp_sum((double)acc[c]);
-      if (lane == 0) sh.u.st.wred[wid][c] = v;
-    }
+  if (nv == 1) {
+    const AT v = warp_sum(acc[0]);
+    if (lane == 0) sh.u.st.wred[wid][0] = (double)v;
+  } else {
+    const AT extra = (nv > 32) ? warp_sum(acc[32]) : (AT)0;
+    const AT v = warp_reduce_scatter32(acc);
+    sh.u.st.wred[wid][lane] = (double)v;
+    if (lane == 0 && nv > 32) sh.u.st.wred[wid][32] = (double)extra;
   }
   __syncthreads();
   for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) {
@@ -106,26 +109,34 @@ __device__ __forceinline__ void block_reduce_cols(const AT* acc, int nv, LzShare
 }
 
 // h[c] = sum over the team's CTAs of part_pass[c][r], identical order in every
-// CTA.  Warp w owns columns w, w+8, ...; all its loads are issued before the
-// warp sums.
-constexpr int CPW = (MP1 + LZ_NW - 1) / LZ_NW;
+// CTA.  Warp 0 issues all loads (lane l takes CTAs l, l+32, ...), then one
+// butterfly reduce-scatter leaves column c in lane c.
 template <typename VT>
 __device__ __forceinline__ void reduce_part(const double* part_pass, int R, int nv,
                                             LzShared<VT>& sh) {
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  double acc[CPW];
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x < 32) {
+    if (nv == 1) {
+      double a = 0.0;
+      for (int r = lane; r < R; r += 32) a += __ldcg(part_pass + r);
+      a = warp_sum(a);
+      if (lane == 0) sh.h[0] = a;
+    } else {
+      double acc[32];
 #pragma unroll
-  for (int j = 0; j < CPW; ++j) {
-    acc[j] = 0.0;
-    const int c = wid + j * LZ_NW;
-    if (c < nv)
-      for (int r = lane; r < R; r += 32) acc[j] += __ldcg(part_pass + (size_t)c * R + r);
-  }
+      for (int c = 0; c < 32; ++c) acc[c] = 0.0;
+      double extra = 0.0;
+      for (int r = lane; r < R; r += 32) {
 #pragma unroll
-  for (int j = 0; j < CPW; ++j) {
-    const int c = wid + j * LZ_NW;
-    const double s = warp_sum(acc[j]);
-    if (lane == 0 && c < nv) sh.h[c] = s;
+        for (int c = 0; c < 32; ++c)
+          if (c < nv) acc[c] += __ldcg(part_pass + (size_t)c * R + r);
+        if (nv > 32) extra += __ldcg(part_pass + (size_t)32 * R + r);
+      }
+      extra = warp_sum(extra);
+      const double v = warp_reduce_scatter32(acc);
+      if (lane < nv) sh.h[lane] = v;
+      if (lane == 0 && nv > 32) sh.h[32] = extra;
+    }
   }
   __syncthreads();
 }
@@ -542,10 +553,12 @@ int lanczos_lanes(int n, long long nnz) {
 
 int lanczos_team_size(const DeviceInfo& di, int n, int prec) {
   const int occ = (prec == 64) ? di.lanczos_occ64 : di.lanczos_occ32;
-  const int maxc = di.sm_count * (occ > 0 ? occ : 1);
+  // two SMs stay free for the single-CTA kernels that run beside the team
+  const int maxc = (di.sm_count > 4 ? di.sm_count - 2 : di.sm_count) * (occ > 0 ? occ : 1);
   const int tiles = (n + LZ_BLOCK - 1) / LZ_BLOCK;
-  // a few tiles per CTA keeps the barrier population small for mid sizes
-  int want = tiles;
+  // at least 4 tiles per CTA: small problems are latency bound, and every
+  // extra CTA costs barrier arrivals and partial sums on each phase
+  int want = (tiles + 3) / 4;
   if (want > maxc) want = maxc;
   if (want < 1) want = 1;
   return want;
@@ -555,7 +568,7 @@ template <typename VT>
 static int run_typed(const DeviceInfo& di, const LanczosProblem* probs, int count,
                      cudaStream_t stream) {
   const int occ = (sizeof(VT) == 8) ? di.lanczos_occ64 : di.lanczos_occ32;
-  const int maxc = di.sm_count * (occ > 0 ? occ : 1);
+  const int maxc = (di.sm_count > 4 ? di.sm_count - 2 : di.sm_count) * (occ > 0 ? occ : 1);
   for (int base = 0; base < count; base += MAX_TEAMS) {
     const int cnt = (count - base < MAX_TEAMS) ? (count - base) : MAX_TEAMS;
     TeamBatch<VT> batch;

@@ -606,8 +606,8 @@ struct Layout {
   int o_QB, o_GC, o_GYmC, o_GZ, o_GB, o_GYC, o_VtO, o_Sout, o_Ssub, o_W, o_Splus, o_Scplus,
       o_Wpast, o_M, o_Mc, o_G, o_Rinv, o_GR1, o_GR2, o_GR, o_sc, n_smalls;
   // buffers
-  double *smalls, *CV, *Vn, *op64, *bmu, *AF, *AFc, *ycand, *zbar, *ups, *Pm, *gpart, *mpart,
-      *Pbar, *Xbar, *alpha, *beta;
+  double *smalls, *CV, *CV2, *Vn, *op64, *op64b, *bmu, *AF, *AFc, *ycand, *zbar, *ups, *Pm,
+      *gpart, *gpart2, *mpart, *Pbar, *Xbar, *alpha, *beta;
   void *opL, *Q, *lz_work, *q0L;
   unsigned int* counters;
   int* status;
@@ -638,13 +638,16 @@ static int plan(const usbs_problem* P, const usbs_params* Pa, const DeviceInfo& 
   L.n_smalls = o;
   L.smalls = ar.take<double>(L.n_smalls);
   L.CV = ar.take<double>((size_t)L.ld * L.k);
+  L.CV2 = ar.take<double>((size_t)L.ld * L.k);
   L.Vn = ar.take<double>((size_t)L.ld * L.k);
   L.op64 = ar.take<double>((size_t)(P->nnz > 0 ? P->nnz : 1));
+  L.op64b = ar.take<double>((size_t)(P->nnz > 0 ? P->nnz : 1));
   L.opL = (Pa->precision == 64) ? (void*)L.op64 : (void*)ar.take<float>((size_t)(P->nnz > 0 ? P->nnz : 1));
   L.bmu = ar.take<double>(L.m); L.AF = ar.take<double>(L.m); L.AFc = ar.take<double>(L.m);
   L.ycand = ar.take<double>(L.m); L.zbar = ar.take<double>(L.m); L.ups = ar.take<double>(L.m);
   L.Pm = ar.take<double>((size_t)L.m * L.s);
   L.gpart = ar.take<double>((size_t)L.grid_gram * L.s * L.s);
+  L.gpart2 = ar.take<double>((size_t)L.grid_gram * L.k * L.k);
   L.mpart = ar.take<double>((size_t)L.grid_red * 8);
   L.Pbar = (Pa->sketch_mode == 0) ? ar.take<double>((size_t)L.ld * L.ssk)
            : (Pa->sketch_mode == 2) ? ar.take<double>(L.ld) : nullptr;
@@ -683,13 +686,20 @@ struct Solver {
   cudaStream_t st;
   int lanes;
   unsigned int* ctr_gram;
+  unsigned int* ctr_gram2;
   unsigned int* ctr_m;
   int gram_ctr_next = 0;
 
-  int gram(const double* X, int ldx, int kx, const double* Y, int ldy, int ky, int n, double* out) {
+  cudaStream_t st2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  int gram(const double* X, int ldx, int kx, const double* Y, int ldy, int ky, int n, double* out,
+           int side = 0) {
     GramArgs a;
     a.n = n; a.kx = kx; a.ky = ky; a.ldx = ldx; a.ldy = ldy; a.X = X; a.Y = Y;
-    a.partial = L.gpart; a.counter = ctr_gram; a.out = out; a.skip = nullptr;
+    a.partial = side ? L.gpart2 : L.gpart;
+    a.counter = side ? ctr_gram2 : ctr_gram;
+    a.out = out; a.skip = nullptr;
+    cudaStream_t st = side ? st2 : this->st;
     int blocks = (n + GR_ROWS - 1) / GR_ROWS;
     if (blocks > L.grid_gram) blocks = L.grid_gram;
     if (blocks < 1) blocks = 1;
@@ -698,7 +708,8 @@ struct Solver {
     else gram_kernel<(IPM_MAXS * IPM_MAXS + RED_BLOCK - 1) / RED_BLOCK><<<blocks, RED_BLOCK, 0, st>>>(a);
     return kerr("gram");
   }
-  int spmm(const double* val, const double* X, int k, double* Y) {
+  int spmm(const double* val, const double* X, int k, double* Y, int side = 0) {
+    cudaStream_t st = side ? st2 : this->st;
     int blocks = (int)(((long long)L.n * lanes + 255) / 256);
     if (blocks > di.sm_count * 8) blocks = di.sm_count * 8;
     if (blocks < 1) blocks = 1;
@@ -706,19 +717,21 @@ struct Solver {
                                         nullptr);
     return kerr("spmm");
   }
-  int assemble(double c_scale, const double* w, void* out, int prec) {
+  int assemble(double c_scale, const double* w, void* out, int prec, int side = 0) {
     return assemble_operator((int)P->nnz, P->c_val, c_scale, P->slot_ptr, P->slot_tid, P->t_con,
-                             P->t_a0, w, out, prec, st);
+                             P->t_a0, w, out, prec, side ? st2 : st);
   }
-  // V^T (c_scale C + A*(w)) V -> smalls[o]
-  int proj(double c_scale, const double* w, const double* V, int o) {
+  // V^T (c_scale C + A*(w)) V -> smalls[o]   (side 1: second stream and its own scratch)
+  int proj(double c_scale, const double* w, const double* V, int o, int side = 0) {
     const double* val = P->c_val;
+    double* op = side ? L.op64b : L.op64;
+    double* cv = side ? L.CV2 : L.CV;
     if (w || c_scale != 1.0) {
-      CK(assemble(c_scale, w, L.op64, 64));
-      val = L.op64;
+      CK(assemble(c_scale, w, op, 64, side));
+      val = op;
     }
-    CK(spmm(val, V, L.k, L.CV));
-    return gram(V, L.ld, L.k, L.CV, L.ld, L.k, L.n, L.smalls + o);
+    CK(spmm(val, V, L.k, cv, side));
+    return gram(V, L.ld, L.k, cv, L.ld, L.k, L.n, L.smalls + o, side);
   }
   MvecArgs margs() {
     MvecArgs a;
@@ -877,23 +890,29 @@ static int body(Solver& X, int t) {
     rows_update_kernel<<<X.rgrid(), 256, 0, st>>>(ra);
     CK(kerr("rows_update"));
   }
+  // ---- lower bound (solver/usbs.py:606-621) on a second stream: it needs V and
+  // y_cand only, so it overlaps the Lanczos call below ----
+  if (cudaEventRecord(X.ev_fork, st) != cudaSuccess ||
+      cudaStreamWaitEvent(X.st2, X.ev_fork, 0) != cudaSuccess)
+    return kerr("fork");
+  CK(X.proj(-1.0, L.ycand, V, L.o_GYC, 1));     // V^T (A*(y_cand) - C) V (solver/usbs.py:219-220)
+  CK(launch_ipm(X.ipm_args(1), X.st2));
+  if (cudaEventRecord(X.ev_join, X.st2) != cudaSuccess) return kerr("join record");
   // ---- candidate eigenvectors at y_cand (solver/usbs.py:588-599) ----
   CK(X.lanczos(L.ycand, L.kc));
   CK(X.copy_q_cols(L.kc, L.Vn + (size_t)L.kp * L.ld));
-  // V^T (A*(y_cand) - C) V for the lower bound (solver/usbs.py:219-220)
-  CK(X.proj(-1.0, L.ycand, V, L.o_GYC));
+  if (cudaStreamWaitEvent(st, X.ev_join, 0) != cudaSuccess) return kerr("join");
   int refined = 0;
   if (Pa->precision != 64) {
-    // FP64 Rayleigh quotients of the FP32 Ritz vectors (op64 holds -C + A*(y_cand))
+    // FP64 Rayleigh quotients of the FP32 Ritz vectors (op64b holds -C + A*(y_cand))
     double* Vc = L.Vn + (size_t)L.kp * L.ld;
-    CK(X.spmm(L.op64, Vc, L.kc, L.CV));
+    CK(X.spmm(L.op64b, Vc, L.kc, L.CV));
     CK(X.gram(Vc, L.ld, L.kc, L.CV, L.ld, L.kc, L.n, L.smalls + L.o_GR1));
     CK(X.gram(Vc, L.ld, L.kc, Vc, L.ld, L.kc, L.n, L.smalls + L.o_GR2));
     rayleigh_kernel<<<1, 32, 0, st>>>(L.smalls, L.o_GR1, L.o_GR2, L.o_GR, L.kc, nullptr);
     CK(kerr("rayleigh"));
     refined = 1;
   }
-  CK(X.run_ipm(1));
   {
     PostArgs pa;
     pa.smalls = L.smalls; pa.o_sc = L.o_sc; pa.o_GR = L.o_GR; pa.kc = L.kc; pa.alpha = L.alpha;
@@ -988,7 +1007,20 @@ int usbs_solve(const usbs_problem* P, const usbs_params* Pa, usbs_state* S, void
   cudaStream_t st = X.st;
   X.lanes = lanczos_lanes(L.n, P->nnz);
   X.ctr_gram = L.counters;
+  X.ctr_gram2 = L.counters + 8;
   X.ctr_m = L.counters + 16;
+  if (cudaStreamCreateWithFlags(&X.st2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&X.ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&X.ev_join, cudaEventDisableTiming) != cudaSuccess)
+    return kerr("stream/event create");
+  struct Cleanup {
+    Solver* x;
+    ~Cleanup() {
+      if (x->st2) cudaStreamDestroy(x->st2);
+      if (x->ev_fork) cudaEventDestroy(x->ev_fork);
+      if (x->ev_join) cudaEventDestroy(x->ev_join);
+    }
+  } cleanup{&X};
   cudaMemsetAsync(L.counters, 0, 64 * sizeof(unsigned int), st);
   cudaMemsetAsync(L.status, 0, 16 * sizeof(int), st);
   cudaMemsetAsync(L.smalls, 0, (size_t)L.n_smalls * sizeof(double), st);
