@@ -89,9 +89,12 @@ size_t usbs_eigsh_workspace_bytes(int n, long long nnz, int inner_iterations, in
  *   Q:    ldq x (inner_iterations + 1) column-major (`precision` type, ldq >= n);
  *         on return Q[:, :num_desired] are the eigenvectors;
  *   eigenvalues: num_desired doubles (ascending);
- *   info: 8 ints: [0] saved vectors of the last restart, [1] converged count,
+ *   info: 16 ints: [0] saved vectors of the last restart, [1] converged count,
  *         [2] restarts run, [3] breakdown restarts, [4] operator applications,
- *         [5] status bits (1 barrier timeout, 8 projected eigensolver failure).
+ *         [5] status bits (1 barrier timeout, 8 projected eigensolver failure),
+ *         [6] kilo-cycles in the restarts, [7] kilo-cycles in total,
+ *         [8..12] kilo-cycles of CTA 0 in barrier waits, team reductions and
+ *         the three step phases.
  * Runs as one cooperative kernel; the call is asynchronous. */
 int usbs_eigsh_smallest(int n, long long nnz, const int* rowptr, const int* col,
                         const double* c_val, double c_scale, const int* slot_ptr, const int* slot_tid,

@@ -135,11 +135,13 @@ class EigshInfo:
         self.k_saved, self.num_converged, self.restarts, self.breakdowns, self.matvecs, \
             self.status = (int(v) for v in raw[:6])
         self.restart_kcycles, self.total_kcycles = int(raw[6]), int(raw[7])
+        self.phase_kcycles = [int(v) for v in raw[8:13]]
 
     def __repr__(self):
         return (f"EigshInfo(restarts={self.restarts}, converged={self.num_converged}, "
                 f"matvecs={self.matvecs}, breakdowns={self.breakdowns}, status={self.status}, "
-                f"restart_kcycles={self.restart_kcycles}, total_kcycles={self.total_kcycles})")
+                f"restart_kcycles={self.restart_kcycles}, total_kcycles={self.total_kcycles}, "
+                f"bar/red/A/B/C={self.phase_kcycles})")
 
 
 def eigsh_smallest(n, C, A_data, A_indices, adjoint_left_vec, q0, num_desired, inner_iterations,
@@ -161,7 +163,7 @@ def eigsh_smallest(n, C, A_data, A_indices, adjoint_left_vec, q0, num_desired, i
     ld = (n + 31) // 32 * 32
     Q = torch.empty((inner_iterations + 1, ld), dtype=vt, device=dev)
     evals = torch.empty(num_desired, dtype=torch.float64, device=dev)
-    info = torch.zeros(8, dtype=torch.int32, device=dev)
+    info = torch.zeros(16, dtype=torch.int32, device=dev)
     need = int(lib.usbs_eigsh_workspace_bytes(n, prob.nnz, inner_iterations, precision))
     if workspace is None or workspace.numel() < need:
         workspace = torch.empty(need, dtype=torch.uint8, device=dev)

@@ -153,47 +153,54 @@ __device__ inline bool warp_syev(double* A, int lda, int n, double* w, double* Z
   return true;
 }
 
-// Cyclic parallel Jacobi eigensolver (float) for a symmetric n x n matrix by
-// one warp, always run at order 32 (indices >= n are padding that couples to
-// nothing): 16 disjoint rotations per round in round-robin ("chess
-// tournament") order, Rutishauser's rotation formulas, sweeps until the
-// off-diagonal Frobenius norm is below 4 eps ||A||_F.  A (row-major lda >= 32)
-// is destroyed; w receives the eigenvalues ascending, Z (row-major ldz >= 32)
-// the eigenvectors as columns.  Lane j owns column j in the row phase and row j
-// in the column phase; every loop has a fixed trip count.  Returns false if 20
-// sweeps do not converge.  pidx needs 32 ints, rc/rs 16 floats each.
-__device__ inline bool warp_jacobi_f32(float* A, int lda, int n, float* w, float* Z, int ldz,
-                                       int* pidx, float* rc, float* rs) {
-  const int lane = threadIdx.x & 31;
+// Cyclic parallel Jacobi eigensolver (float) for a symmetric n x n matrix, run
+// by a whole CTA (blockDim a multiple of 32, >= 64) at order 32 (indices >= n
+// are padding that couples to nothing): 16 disjoint rotations per round in
+// round-robin ("chess tournament") order, Rutishauser's rotation formulas,
+// sweeps until the off-diagonal Frobenius norm is below 4 eps ||A||_F.  Each
+// round: threads 0-15 form the rotations, then the 512 row updates and the
+// 1024 column updates (A and Z) are spread over the CTA.  A (row-major,
+// lda >= 32) is destroyed; w receives the eigenvalues ascending, Z (row-major,
+// ldz >= 32) the eigenvectors as columns.  Returns false (uniformly) if 20
+// sweeps do not converge.  pidx needs 32 ints, rc/rs 16 floats, red 32 floats.
+__device__ inline bool cta_jacobi_f32(float* A, int lda, int n, float* w, float* Z, int ldz,
+                                      int* pidx, float* rc, float* rs, float* red) {
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5;
   constexpr int M = 32, H = 16;
-#pragma unroll 4
-  for (int i = 0; i < M; ++i) {
-    Z[i * ldz + lane] = (i == lane) ? 1.0f : 0.0f;
-    if (i >= n || lane >= n) A[i * lda + lane] = 0.0f;
+  for (int e = tid; e < M * M; e += nt) {
+    const int i = e >> 5, j = e & 31;
+    Z[i * ldz + j] = (i == j) ? 1.0f : 0.0f;
+    if (i >= n || j >= n) A[i * lda + j] = 0.0f;
   }
-  __syncwarp();
-  float fro = 0.0f;
-#pragma unroll 4
-  for (int i = 0; i < M; ++i) { const float a = A[i * lda + lane]; fro += a * a; }
-  fro = warp_sum(fro);
-  const float tol2 = fro * (4.0f * 1.2e-7f) * (4.0f * 1.2e-7f);
+  __syncthreads();
+  if (wid == 0) {
+    float fro = 0.0f;
+    for (int i = 0; i < M; ++i) { const float a = A[i * lda + lane]; fro += a * a; }
+    fro = warp_sum(fro);
+    if (lane == 0) red[0] = fro * (4.0f * 1.2e-7f) * (4.0f * 1.2e-7f);
+  }
+  __syncthreads();
+  const float tol2 = red[0];
   bool ok = false;
   for (int sweep = 0; sweep < 20; ++sweep) {
-    float off = 0.0f;
-#pragma unroll 4
-    for (int i = 0; i < M; ++i) {
-      const float a = (lane != i) ? A[i * lda + lane] : 0.0f;
-      off += a * a;
+    if (wid == 0) {
+      float off = 0.0f;
+      for (int i = 0; i < M; ++i) {
+        const float a = (lane != i) ? A[i * lda + lane] : 0.0f;
+        off += a * a;
+      }
+      off = warp_sum(off);
+      if (lane == 0) red[1] = off;
     }
-    off = warp_sum(off);
-    if (off <= tol2) { ok = true; break; }
+    __syncthreads();
+    if (red[1] <= tol2) { ok = true; break; }
     for (int r = 0; r < M - 1; ++r) {
-      if (lane < H) {
+      if (tid < H) {
         int p, q;
-        if (lane == 0) { p = 0; q = 1 + r; }
+        if (tid == 0) { p = 0; q = 1 + r; }
         else {
-          p = r + lane; p = (p >= M - 1) ? p - (M - 1) : p; p += 1;
-          q = r - lane + M - 1; q = (q >= M - 1) ? q - (M - 1) : q; q += 1;
+          p = r + tid; p = (p >= M - 1) ? p - (M - 1) : p; p += 1;
+          q = r - tid + M - 1; q = (q >= M - 1) ? q - (M - 1) : q; q += 1;
         }
         if (p > q) { const int t = p; p = q; q = t; }
         const float apq = A[p * lda + q];
@@ -204,57 +211,59 @@ __device__ inline bool warp_jacobi_f32(float* A, int lda, int n, float* w, float
           c = rsqrtf(t * t + 1.0f);
           sn = t * c;
         }
-        pidx[2 * lane] = p;
-        pidx[2 * lane + 1] = q;
-        rc[lane] = c;
-        rs[lane] = sn;
+        pidx[2 * tid] = p;
+        pidx[2 * tid + 1] = q;
+        rc[tid] = c;
+        rs[tid] = sn;
       }
-      __syncwarp();
-      // rows (J^T A): lane = column
-#pragma unroll
-      for (int pr = 0; pr < H; ++pr) {
+      __syncthreads();
+      // rows (J^T A): element (pair, column)
+      for (int e = tid; e < H * M; e += nt) {
+        const int pr = e >> 5, j = e & 31;
         const int p = pidx[2 * pr], q = pidx[2 * pr + 1];
         const float c = rc[pr], sn = rs[pr];
-        const float ap = A[p * lda + lane], aq = A[q * lda + lane];
-        A[p * lda + lane] = c * ap - sn * aq;
-        A[q * lda + lane] = sn * ap + c * aq;
+        const float ap = A[p * lda + j], aq = A[q * lda + j];
+        A[p * lda + j] = c * ap - sn * aq;
+        A[q * lda + j] = sn * ap + c * aq;
       }
-      __syncwarp();
-      // columns (A J) and Z J: lane = row
-#pragma unroll
-      for (int pr = 0; pr < H; ++pr) {
+      __syncthreads();
+      // columns (A J) and Z J: element (pair, row)
+      for (int e = tid; e < 2 * H * M; e += nt) {
+        const int which = e >> 9, pr = (e >> 5) & 15, j = e & 31;
         const int p = pidx[2 * pr], q = pidx[2 * pr + 1];
         const float c = rc[pr], sn = rs[pr];
-        const float ap = A[lane * lda + p], aq = A[lane * lda + q];
-        A[lane * lda + p] = c * ap - sn * aq;
-        A[lane * lda + q] = sn * ap + c * aq;
-        const float zp = Z[lane * ldz + p], zq = Z[lane * ldz + q];
-        Z[lane * ldz + p] = c * zp - sn * zq;
-        Z[lane * ldz + q] = sn * zp + c * zq;
+        float* B = which ? Z : A;
+        const int ldb = which ? ldz : lda;
+        const float bp = B[j * ldb + p], bq = B[j * ldb + q];
+        B[j * ldb + p] = c * bp - sn * bq;
+        B[j * ldb + q] = sn * bp + c * bq;
       }
-      __syncwarp();
+      __syncthreads();
     }
   }
-  // eigenvalues from the diagonal, sorted ascending with their vectors
-  if (lane < n) w[lane] = A[lane * lda + lane];
-  __syncwarp();
-  for (int i = 0; i < n - 1; ++i) {
-    int kmin = i;
-    float vmin = w[i];
-    for (int j = i + 1; j < n; ++j)
-      if (w[j] < vmin) { vmin = w[j]; kmin = j; }
-    if (kmin != i) {
-      const float wi = w[i];
-      __syncwarp();
-      if (lane < n) {
-        const float t = Z[lane * ldz + i];
-        Z[lane * ldz + i] = Z[lane * ldz + kmin];
-        Z[lane * ldz + kmin] = t;
+  // eigenvalues from the diagonal, sorted ascending with their vectors (warp 0)
+  if (wid == 0) {
+    if (lane < n) w[lane] = A[lane * lda + lane];
+    __syncwarp();
+    for (int i = 0; i < n - 1; ++i) {
+      int kmin = i;
+      float vmin = w[i];
+      for (int j = i + 1; j < n; ++j)
+        if (w[j] < vmin) { vmin = w[j]; kmin = j; }
+      if (kmin != i) {
+        const float wi = w[i];
+        __syncwarp();
+        if (lane < n) {
+          const float t = Z[lane * ldz + i];
+          Z[lane * ldz + i] = Z[lane * ldz + kmin];
+          Z[lane * ldz + kmin] = t;
+        }
+        if (lane == 0) { w[kmin] = wi; w[i] = vmin; }
+        __syncwarp();
       }
-      if (lane == 0) { w[kmin] = wi; w[i] = vmin; }
-      __syncwarp();
     }
   }
+  __syncthreads();
   return ok;
 }
 

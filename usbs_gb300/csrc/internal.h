@@ -31,7 +31,7 @@ struct LanczosProblem {
   void* Q;              // ld x (m+1), column-major
   double* alpha;        // m: Ritz values (alpha_hat) after the last restart
   double* beta;         // m
-  int* ctl;             // 8 ints: k_next, nconv, restarts, breakdowns, steps
+  int* ctl;             // 16 ints: k_next, nconv, restarts, breakdowns, steps, -, cycle counters
   int* status;
   void* work;           // workspace of lanczos_workspace_bytes()
 };

@@ -19,6 +19,7 @@
 // At a restart CTA 0 builds the arrowhead matrix and runs the FP64 warp
 // eigensolver; after a barrier every CTA rotates its rows of Q by the saved
 // Ritz vectors.
+#include <stdlib.h>
 #include <vector>
 #include "common.cuh"
 #include "dense.cuh"
@@ -31,9 +32,11 @@ constexpr int LZ_NW = LZ_BLOCK / 32;
 constexpr int MAX_TEAMS = 48;
 constexpr int MP1 = MAXM + 1;
 
+constexpr int LZ_XS_BYTES = 160 * 1024;   // dynamic shared memory for a staged x
+
 template <typename VT>
 struct TeamDesc {
-  int n, ld, m, num_desired, max_restarts, lanes, first_cta, nctas;
+  int n, ld, m, num_desired, max_restarts, lanes, first_cta, nctas, xsmem;
   double tol;
   const int* rowptr;
   const int* col;
@@ -76,7 +79,7 @@ struct LzShared {
   double beta[MAXM];
   double ritz[MAXM];
   double red[LZ_NW];
-  float wf[MAXM], rc[MAXM / 2], rsn[MAXM / 2];
+  float wf[MAXM], rc[MAXM / 2], rsn[MAXM / 2], redf[32];
   int pidx[MAXM];
   int order[MAXM];
   int k_next, nconv;
@@ -153,6 +156,14 @@ __device__ void phase_spmv(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0, int 
   const int tid = threadIdx.x, L = P.lanes, gpp = LZ_BLOCK / L;
   const int g = tid / L, lig = tid - g * L;
   const size_t ld = (size_t)P.ld;
+  // small vectors: stage x once in shared memory so the gathers skip L2
+  extern __shared__ __align__(16) unsigned char lz_dyn[];
+  VT* xs = (VT*)lz_dyn;
+  const bool use_xs = P.xsmem != 0;
+  if (use_xs) {
+    for (int j = tid; j < P.n; j += LZ_BLOCK) xs[j] = __ldcg(xsrc + j);
+    __syncthreads();
+  }
   for (int tile = t0; tile < t1; ++tile) {
     const int base = tile * LZ_BLOCK;
     for (int pass = 0; pass < L; ++pass) {
@@ -161,8 +172,13 @@ __device__ void phase_spmv(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0, int 
       AT s = (AT)0;
       if (row < P.n) {
         const int pe = P.rowptr[row + 1];
-        for (int p = P.rowptr[row] + lig; p < pe; p += L)
-          s += (AT)P.val[p] * (AT)__ldcg(xsrc + P.col[p]);
+        if (use_xs) {
+          for (int p = P.rowptr[row] + lig; p < pe; p += L)
+            s += (AT)P.val[p] * (AT)xs[P.col[p]];
+        } else {
+          for (int p = P.rowptr[row] + lig; p < pe; p += L)
+            s += (AT)P.val[p] * (AT)__ldcg(xsrc + P.col[p]);
+        }
       }
       for (int o = L >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
       if (lig == 0) sh.u.st.ys[rl] = (double)s;
@@ -289,12 +305,11 @@ __device__ void restart_select(const TeamDesc<VT>& P, LzShared<VT>& sh, int k) {
     Tf[r * MP1 + c] = (float)v;
   }
   __syncthreads();
-  // eigh(T) (solver/lanczos.py:203): FP32 parallel Jacobi by warp 0 ...
-  if (tid < 32) {
-    bool ok = warp_jacobi_f32(Tf, MP1, m, sh.wf, Zf, MP1, sh.pidx, sh.rc, sh.rsn);
+  // eigh(T) (solver/lanczos.py:203): FP32 parallel Jacobi by the CTA ...
+  {
+    const bool ok = cta_jacobi_f32(Tf, MP1, m, sh.wf, Zf, MP1, sh.pidx, sh.rc, sh.rsn, sh.redf);
     if (!ok && tid == 0) atomicOr(P.status, ST_SMALL_DENSE_FAIL);
   }
-  __syncthreads();
   for (int e = tid; e < m * m; e += LZ_BLOCK) {
     const int r = e / m, c = e - r * m;
     X[r * MP1 + c] = (double)Zf[r * MP1 + c];
@@ -405,6 +420,17 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
 
   int k = 0, nconv = 0, restart = 0, breakdowns = 0, steps = 0;
   long long clk_start = clock64(), clk_restart = 0;
+  // rank-0 phase accounting: [0] barrier waits, [1] team reductions, [2..4] phases A..C
+  long long tp[5] = {0, 0, 0, 0, 0}, tmark = clock64();
+  const bool timing = (rank == 0 && tid == 0);
+#define LZ_MARK(slot)                                   \
+  do {                                                  \
+    if (timing) {                                       \
+      const long long _c = clock64();                   \
+      tp[slot] += _c - tmark;                           \
+      tmark = _c;                                       \
+    }                                                   \
+  } while (0)
   if (rank == 0 && tid < MAXM) { sh.alpha[tid] = 0.0; sh.beta[tid] = 0.0; }
   __syncthreads();
   int prev = 0;          // vbuf slot holding the latest unnormalised vector
@@ -444,16 +470,25 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
         wq = true;
       }
       VT* vout = P.vbuf + (size_t)cur * ld;
+      LZ_MARK(1);
       phase_spmv(P, sh, t0, t1, i, xsrc, invb, wq, vout, part0 + rank);
+      LZ_MARK(2);
       if (!bar.sync()) return;
+      LZ_MARK(0);
       reduce_part(part0, R, i + 1, sh);
+      LZ_MARK(1);
       const double h1i = sh.h[i];
       phase_update_dot(P, sh, t0, t1, i + 1, vout, part1 + rank);
+      LZ_MARK(3);
       if (!bar.sync()) return;
+      LZ_MARK(0);
       reduce_part(part1, R, i + 1, sh);
+      LZ_MARK(1);
       if (rank == 0 && tid == 0) sh.alpha[i] = h1i + sh.h[i];
       phase_update_norm(P, sh, t0, t1, i + 1, vout, part2 + rank);
+      LZ_MARK(4);
       if (!bar.sync()) return;
+      LZ_MARK(0);
       prev = cur;
       cur ^= 1;
       ++steps;
@@ -519,6 +554,7 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
     k = kn;
     ++restart;
     if (!bar.sync()) return;
+    if (timing) tmark = clock64();   // restart time is reported separately (ctl[6])
   }
   if (rank == 0 && tid == 0) {
     P.ctl[2] = restart;
@@ -526,6 +562,7 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
     P.ctl[4] = steps;
     P.ctl[6] = (int)(clk_restart >> 10);
     P.ctl[7] = (int)((clock64() - clk_start) >> 10);
+    for (int j = 0; j < 5; ++j) P.ctl[8 + j] = (int)(tp[j] >> 10);
     if (restart == 0) P.ctl[0] = 0;
   }
 }
@@ -559,6 +596,13 @@ int lanczos_team_size(const DeviceInfo& di, int n, int prec) {
   // at least 4 tiles per CTA: small problems are latency bound, and every
   // extra CTA costs barrier arrivals and partial sums on each phase
   int want = (tiles + 3) / 4;
+  // USBS_LANCZOS_CTAS overrides the team size (tuning experiments)
+  static const int forced = [] {
+    const char* e = getenv("USBS_LANCZOS_CTAS");
+    return e ? atoi(e) : 0;
+  }();
+  if (forced > 0) want = forced;
+  if (want > tiles) want = tiles;
   if (want > maxc) want = maxc;
   if (want < 1) want = 1;
   return want;
@@ -595,6 +639,7 @@ static int run_typed(const DeviceInfo& di, const LanczosProblem* probs, int coun
       total = tot2;
     }
     int first = 0;
+    size_t dyn = 0;
     for (int i = 0; i < cnt; ++i) {
       const LanczosProblem& p = probs[base + i];
       if (p.m > MAXM || p.m < 1 || p.n < 1 || p.ld < p.n) {
@@ -606,6 +651,8 @@ static int run_typed(const DeviceInfo& di, const LanczosProblem* probs, int coun
       t.n = p.n; t.ld = p.ld; t.m = p.m; t.num_desired = p.num_desired;
       t.max_restarts = p.max_restarts; t.tol = p.tol;
       t.lanes = lanczos_lanes(p.n, p.nnz);
+      t.xsmem = ((size_t)p.n * sizeof(VT) <= (size_t)LZ_XS_BYTES) ? 1 : 0;
+      if (t.xsmem && (size_t)p.n * sizeof(VT) > dyn) dyn = (size_t)p.n * sizeof(VT);
       t.first_cta = first;
       t.nctas = want[i];
       t.rowptr = p.rowptr; t.col = p.col; t.val = (const VT*)p.val;
@@ -618,14 +665,20 @@ static int run_typed(const DeviceInfo& di, const LanczosProblem* probs, int coun
       t.alpha = p.alpha; t.beta = p.beta; t.ctl = p.ctl; t.status = p.status;
       first += want[i];
       if (cudaMemsetAsync(t.bar, 0, 2 * sizeof(unsigned int), stream) != cudaSuccess ||
-          cudaMemsetAsync(p.ctl, 0, 8 * sizeof(int), stream) != cudaSuccess) {
+          cudaMemsetAsync(p.ctl, 0, 16 * sizeof(int), stream) != cudaSuccess) {
         set_error("lanczos: memset failed");
         return -4;
       }
     }
     void* args[] = {(void*)&batch};
+    static bool attr_set = false;
+    if (!attr_set) {
+      cudaFuncSetAttribute((const void*)lanczos_team_kernel<VT>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, LZ_XS_BYTES);
+      attr_set = true;
+    }
     cudaError_t e = cudaLaunchCooperativeKernel((const void*)lanczos_team_kernel<VT>,
-                                                dim3(total), dim3(LZ_BLOCK), args, 0, stream);
+                                                dim3(total), dim3(LZ_BLOCK), args, dyn, stream);
     if (e != cudaSuccess) {
       set_error("lanczos: cooperative launch of %d CTAs failed: %s", total,
                 cudaGetErrorString(e));
@@ -644,11 +697,19 @@ int lanczos_run(const DeviceInfo& di, const LanczosProblem* probs, int count, in
 }
 
 int lanczos_occupancy(int prec) {
+  // occupancy with the largest staged x, so any launch stays co-resident
   int occ = 0;
-  if (prec == 64)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lanczos_team_kernel<double>, LZ_BLOCK, 0);
-  else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lanczos_team_kernel<float>, LZ_BLOCK, 0);
+  if (prec == 64) {
+    cudaFuncSetAttribute((const void*)lanczos_team_kernel<double>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, LZ_XS_BYTES);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lanczos_team_kernel<double>, LZ_BLOCK,
+                                                  LZ_XS_BYTES);
+  } else {
+    cudaFuncSetAttribute((const void*)lanczos_team_kernel<float>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, LZ_XS_BYTES);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lanczos_team_kernel<float>, LZ_BLOCK,
+                                                  LZ_XS_BYTES);
+  }
   return occ;
 }
 

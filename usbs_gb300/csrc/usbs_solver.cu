@@ -657,8 +657,8 @@ static int plan(const usbs_problem* P, const usbs_params* Pa, const DeviceInfo& 
   L.Q = ar.take<char>((size_t)L.ld * (L.mL + 1) * L.vt);
   L.q0L = ar.take<char>((size_t)L.ld * L.vt);
   L.counters = ar.take<unsigned int>(64);
-  L.status = ar.take<int>(16);
-  L.ctl = L.status + 8;
+  L.status = ar.take<int>(32);
+  L.ctl = L.status + 16;
   L.skip = ar.take<int>(4);
   const int nct = lanczos_team_size(di, L.n, Pa->precision);
   L.lz_work = ar.take<char>(lanczos_workspace_bytes(L.n, L.ld, L.mL, Pa->precision, nct));
@@ -1022,7 +1022,7 @@ int usbs_solve(const usbs_problem* P, const usbs_params* Pa, usbs_state* S, void
     }
   } cleanup{&X};
   cudaMemsetAsync(L.counters, 0, 64 * sizeof(unsigned int), st);
-  cudaMemsetAsync(L.status, 0, 16 * sizeof(int), st);
+  cudaMemsetAsync(L.status, 0, 32 * sizeof(int), st);
   cudaMemsetAsync(L.smalls, 0, (size_t)L.n_smalls * sizeof(double), st);
   cudaMemsetAsync(L.ups, 0, (size_t)L.m * sizeof(double), st);
   cudaMemcpyAsync(L.zbar, S->z, (size_t)L.m * sizeof(double), cudaMemcpyDeviceToDevice, st);
