@@ -110,35 +110,56 @@ __device__ __forceinline__ double wdot(const double* x, const double* y, int s) 
   return warp_sum(v);
 }
 
-// LU with partial pivoting and solve, whole CTA (G&VL Alg. 3.4.1).  Per column:
-// warp 0 finds the pivot, the rows are swapped, the multipliers of all rows are
-// formed in parallel (one thread per row) into `lcol`, then the trailing update
-// runs with warps over rows and lanes over columns.
+// |x| of a double as an integer key: for finite values the ordering of the keys
+// is the ordering of |x|, so pivot comparisons stay off the FP64 pipe.
+__device__ __forceinline__ unsigned long long abs_key(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+}
+
+// LU with partial pivoting and solve, whole CTA (G&VL Alg. 3.4.1).  Warps own
+// rows, lanes own columns.  The trailing update of column j+1 also records,
+// per warp, the largest |a| below the diagonal, so the next pivot is a pick
+// among 8 candidates; multipliers are formed inside each warp.  Two CTA
+// barriers per column.  Ties go to the smaller row index, as in LAPACK.
 __device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* redv, double* lcol,
                              int* piv_out, int* ok_out) {
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
-  if (tid == 0) *ok_out = 1;
-  for (int j = 0; j < n; ++j) {
-    if (wid == 0) {
-      double best = -1.0;
-      int bi = j;
-      for (int i = j + lane; i < n; i += 32) {
-        const double a = fabs(A[i * lda + j]);
-        if (a > best) { best = a; bi = i; }
-      }
-      for (int o = 16; o > 0; o >>= 1) {
-        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
-        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-      }
+  __shared__ unsigned long long cand_key[IPM_BLOCK / 32];
+  __shared__ int cand_row[IPM_BLOCK / 32];
+  (void)lcol;
+  // pivot candidates for column 0
+  {
+    unsigned long long best = 0ull;
+    int bi = 0x7fffffff;
+    for (int i = wid; i < n; i += nw) {
       if (lane == 0) {
-        *piv_out = bi;
-        if (best == 0.0) *ok_out = 0;
-        redv[0] = (best == 0.0) ? 1.0 : 1.0 / A[bi * lda + j];
+        const unsigned long long k = abs_key(A[i * lda]);
+        if (k > best || (k == best && i < bi) || bi == 0x7fffffff) { best = k; bi = i; }
       }
+    }
+    if (lane == 0) { cand_key[wid] = best; cand_row[wid] = bi; }
+  }
+  if (tid == 0) *ok_out = 1;
+  __syncthreads();
+  for (int j = 0; j < n; ++j) {
+    if (tid == 0) {
+      unsigned long long best = 0ull;
+      int bi = 0x7fffffff;
+      for (int w = 0; w < nw; ++w) {
+        const int r = cand_row[w];
+        if (r == 0x7fffffff) continue;
+        const unsigned long long k = cand_key[w];
+        if (bi == 0x7fffffff || k > best || (k == best && r < bi)) { best = k; bi = r; }
+      }
+      if (bi == 0x7fffffff) bi = j;
+      *piv_out = bi;
+      const double pv = A[bi * lda + j];
+      if (pv == 0.0) *ok_out = 0;
+      redv[0] = (pv == 0.0) ? 1.0 : 1.0 / pv;
     }
     __syncthreads();
     const int piv = *piv_out;
+    const double inv = redv[0];
     if (piv != j) {
       for (int c = tid; c < n; c += blockDim.x) {
         const double t = A[j * lda + c];
@@ -148,20 +169,24 @@ __device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* redv,
       if (tid == 0) { const double t = b[j]; b[j] = b[piv]; b[piv] = t; }
       __syncthreads();
     }
-    const double inv = redv[0];
     const double bj = b[j];
-    for (int i = j + 1 + tid; i < n; i += blockDim.x) {
-      const double l = A[i * lda + j] * inv;
-      A[i * lda + j] = l;
-      lcol[i] = l;
-      b[i] -= l * bj;
-    }
-    __syncthreads();
-#pragma unroll 4
+    unsigned long long best = 0ull;
+    int bi = 0x7fffffff;
     for (int i = j + 1 + wid; i < n; i += nw) {
-      const double l = lcol[i];
-      for (int c = j + 1 + lane; c < n; c += 32) A[i * lda + c] -= l * A[j * lda + c];
+      const double l = A[i * lda + j] * inv;
+      __syncwarp();
+      if (lane == 0) { A[i * lda + j] = l; b[i] -= l * bj; }
+      for (int c = j + 1 + lane; c < n; c += 32) {
+        const double v = A[i * lda + c] - l * A[j * lda + c];
+        A[i * lda + c] = v;
+        if (c == j + 1) {
+          const unsigned long long k = abs_key(v);
+          if (bi == 0x7fffffff || k > best) { best = k; bi = i; }
+        }
+      }
     }
+    // lane holding column j+1 is lane 0 of each warp (c = j+1+lane)
+    if (lane == 0) { cand_key[wid] = best; cand_row[wid] = bi; }
     __syncthreads();
   }
   for (int j = n - 1; j >= 0; --j) {
@@ -333,13 +358,14 @@ __global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ 
     // floating point; mirroring one triangle measurably degrades the Newton
     // steps once the system is ill-conditioned near the end of the IPM)
     const double lbc = (A.mode == 1) ? (ze / (k1 * ze + 1)) : 0.0;
+    const double rden = 1.0 / den;
     for (int a = wid; a < s; a += nw) {
       const int b = sh.bi[a], c = sh.ci[a];
       for (int a2 = lane; a2 < s; a2 += 32) {
         double v = symkron(sh.T, sh.Si, k, b, c, sh.bi[a2], sh.ci[a2]);
         if (A.mode == 0) {
           v = Q11[a * s + a2] + v;
-          v -= (sh.q12[a] * (k1 * sh.q12[a2] + sh.sI[a2]) + sh.sI[a] * (sh.q12[a2] - k2 * sh.sI[a2])) / den;
+          v -= (sh.q12[a] * (k1 * sh.q12[a2] + sh.sI[a2]) + sh.sI[a] * (sh.q12[a2] - k2 * sh.sI[a2])) * rden;
         } else {
           v += lbc * (sh.sI[a] * sh.sI[a2]);
         }
