@@ -1,0 +1,366 @@
+"""Benchmark of the USBS hot path on GB300 (one JSON line on rank 0).
+
+Workload (N=1): the 100 x 100 toroidal +-1 spin-glass MaxCut SDP (n = 10,000,
+degree 4), solved with the reference's MaxCut settings (k_curr 10, k_past 1,
+sketch 10, rho 0.01, beta 0.25, trace bound 2n, tolerances 1e-7, 32 Lanczos
+vectors x 10 restarts, IPM <= 100 steps) in the mixed-precision mode (FP32
+Lanczos, FP64 bundle subproblems / gaps / Rayleigh refinement).  Synthetic data
+(seeded generator with the benchmark's shape); no dataset is read.
+
+A step is one ``usbs()`` call from the cold start that runs ``--iters-per-step``
+outer iterations (the stop tolerance is the metric's 1e-4, which this instance
+does not reach within a step, so every step does the same work).  ``value`` is
+outer iterations per second of the whole job (all ranks; each rank solves its
+own instance: replicas, weak scaling).  The 1e-4 solve itself takes thousands of
+iterations on this instance for the reference algorithm as well (see DESIGN),
+so solves/s is not a measurable per-step quantity here.
+
+Extra measurements on the same line: ``roofline`` of the Lanczos team kernel
+(CUDA events around every launch inside the timed region, algorithmic bytes
+from the kernel's own counters), the standalone Lanczos SpMV GB/s on the
+10^6-node random geometric graph, ``cpu_baseline`` (the NumPy oracle on this
+host), ``e2e`` through the public API from pinned host buffers, and SM clocks
+sampled with nvidia-smi during the timed region.
+
+``--impl reference`` times the reference algorithm on the CPU (the oracle
+restatement; JAX is not installed) with the same metric and unit.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+import numpy as np  # noqa: E402
+
+METRIC = "SDP solves/s and p50/p99 latency at 1e-4 rel gap; Lanczos SpMV HBM GB/s"
+UNIT = "USBS outer iterations/s"
+SETTINGS = dict(k_curr=10, k_past=1, sketch_dim=10, rho=0.01, beta=0.25, trace_factor=2.0,
+                subprob_eps=1e-7, subprob_max_iters=100, lanczos_inner_iterations=32,
+                lanczos_max_restarts=10, gap_eps=1e-4)
+
+
+def workload(rank=0):
+    from usbs_gb300 import workloads as wl
+    return wl.torus_graph(100, 1 + 1000 * rank)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms (the recipe's query)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def run_usbs(st, n, iters, inst, device, precision=32, q0=None):
+    from usbs_gb300 import solver
+    S = SETTINGS
+    return solver.usbs(st, n, n, S["trace_factor"] * n * st.SCALE_X, S["trace_factor"], S["rho"],
+                       S["beta"], S["k_curr"], S["k_past"], iters, np.inf, S["gap_eps"],
+                       S["gap_eps"], S["gap_eps"], S["lanczos_inner_iterations"],
+                       S["lanczos_max_restarts"], S["subprob_eps"], S["subprob_max_iters"], 1.0,
+                       None, None, None, q0=q0, precision=precision, device=device,
+                       return_info=True, instance=inst)
+
+
+def cpu_oracle_iterations(st, n, iters):
+    """Oracle (NumPy FP64 restatement) outer iterations; returns (iterations, seconds)."""
+    from oracle import usbs as ousbs
+    S = SETTINGS
+    t0 = time.perf_counter()
+    out, fin = ousbs.usbs(st, n, n, S["trace_factor"] * n * st.SCALE_X, S["trace_factor"],
+                          S["rho"], S["beta"], S["k_curr"], S["k_past"], iters, np.inf,
+                          S["gap_eps"], S["gap_eps"], S["gap_eps"],
+                          S["lanczos_inner_iterations"], S["lanczos_max_restarts"],
+                          S["subprob_eps"], S["subprob_max_iters"])
+    return int(fin["t"]), time.perf_counter() - t0
+
+
+def spmv_gbs(device, reps=20):
+    """Standalone Lanczos operator apply (FP32 CSR SpMV) on the 10^6-node RGG."""
+    import torch
+    from usbs_gb300 import api, workloads as wl
+    from usbs_gb300.problem import DeviceProblem, layout
+    from usbs_gb300.problems import maxcut
+    W = wl.rgg_knn_graph(10 ** 6, 6, 0)
+    st = maxcut.initialize_state(W, 1)
+    n = st.C.shape[0]
+    prob = DeviceProblem(layout(st.C, st.A_data, st.A_indices, m=n), device)
+    x = torch.randn(n, device=device, dtype=torch.float32)
+    w = torch.zeros(n, device=device, dtype=torch.float64)
+    api.operator_apply(prob, -1.0, w, x, precision=32)  # warm-up + assembly
+    lib = api._lib.load()
+    op = torch.empty(prob.nnz, dtype=torch.float32, device=device)
+    lib.usbs_assemble_operator(prob.nnz, api._p(prob.c_val), -1.0, api._p(prob.slot_ptr),
+                               api._p(prob.slot_tid), api._p(prob.t_con), api._p(prob.t_a0),
+                               api._p(w), api._p(op), 32, api._stream())
+    y = torch.empty(n, dtype=torch.float32, device=device)
+    flush = torch.empty(256 * 2 ** 20, dtype=torch.uint8, device=device)
+    ms = []
+    for _ in range(reps):
+        flush.zero_()   # evict L2 (larger than the 129 MB L2)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        lib.usbs_operator_apply(n, prob.nnz, api._p(prob.rowptr), api._p(prob.col), api._p(op),
+                                api._p(x), api._p(y), 32, api._stream())
+        e1.record()
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    nnz = prob.nnz
+    alg = 8.0 * nnz + 4.0 * (n + 1) + 4.0 * n + 4.0 * n
+    t = float(np.median(ms))
+    return {"graph": "rgg n=1e6 k=6", "nnz": int(nnz), "alg_bytes": alg, "ms": t,
+            "gbs": alg / (t * 1e-3) / 1e9}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--iters-per-step", type=int, default=10)
+    ap.add_argument("--cpu-iters", type=int, default=24)
+    ap.add_argument("--no-spmv", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+
+    from usbs_gb300.problems import maxcut
+    S = SETTINGS
+
+    if args.impl == "reference":
+        if rank != 0:
+            return 0
+        W = workload(0)
+        st = maxcut.initialize_state(W, S["sketch_dim"])
+        n = st.C.shape[0]
+        per = max(1, args.cpu_iters // 4)
+        for _ in range(args.warmup):
+            cpu_oracle_iterations(st, n, per)
+        tot_it, tot_s = 0, 0.0
+        for _ in range(args.steps):
+            it, sec = cpu_oracle_iterations(st, n, per)
+            tot_it += it
+            tot_s += sec
+        v = tot_it / tot_s
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": 0,
+                "steps": args.steps, "warmup": args.warmup,
+                "ms_per_step": 1e3 * tot_s / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": "maxcut torus 100x100 +-1 (n=10000), reference settings",
+                           "iters_per_step": per, "settings": S},
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": 1, "kind": "port",
+                                 "sample": f"{args.steps} x {per} outer iterations of the NumPy "
+                                           "oracle restatement (JAX reference not installed)"},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return 0
+
+    import torch
+    import torch.distributed as dist
+    if world > 1:
+        dist.init_process_group("nccl", init_method="env://")
+    device = torch.device(f"cuda:{local}")
+    torch.cuda.set_device(device)
+    from usbs_gb300 import solver
+    from usbs_gb300.problem import DeviceProblem, layout
+    from usbs_gb300.rng import default_q0
+
+    W = workload(rank)
+    st = maxcut.initialize_state(W, S["sketch_dim"])
+    n = st.C.shape[0]
+    q0 = default_q0(n)
+    inst = solver.DeviceInstance(st, device)
+    # device-resident state for the value leg
+    st_dev = st._replace(y=torch.as_tensor(st.y, device=device),
+                         z=torch.as_tensor(st.z, device=device),
+                         P=torch.as_tensor(st.P, device=device),
+                         Omega=torch.as_tensor(st.Omega, device=device))
+    q0_dev = torch.as_tensor(q0, device=device)
+    it_step = args.iters_per_step
+    for _ in range(args.warmup):
+        run_usbs(st_dev, n, it_step, inst, device, q0=q0_dev)
+    torch.cuda.synchronize()
+    if world > 1:
+        dist.barrier()
+    infos = []
+    with ClockSampler(local) as clk:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            out, info = run_usbs(st_dev, n, it_step, inst, device, q0=q0_dev)
+            infos.append(info)
+        e1.record()
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - t0
+    if world > 1:
+        dist.barrier()
+    ms = e0.elapsed_time(e1)
+    iters_done = sum(i["iterations"] for i in infos)
+    t_max = torch.tensor([ms], device=device)
+    it_tot = torch.tensor([float(iters_done)], device=device)
+    if world > 1:
+        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
+        dist.all_reduce(it_tot, op=dist.ReduceOp.SUM)
+    ms_max = float(t_max.item())
+    value = float(it_tot.item()) / (ms_max * 1e-3)
+    lz_ms = sum(i["lanczos_ms"] for i in infos)
+    lz_n = sum(i["lanczos_launches"] for i in infos)
+    lz_bytes = sum(i["lanczos_bytes"] for i in infos)
+    launches = sum(i["kernel_launches"] for i in infos)
+    peak, peak_kind = peaks()
+    achieved = (lz_bytes / max(lz_n, 1)) / ((lz_ms / max(lz_n, 1)) * 1e-3) / 1e9 if lz_n else 0.0
+
+    # e2e: public API from pinned host buffers (problem layout + state in, result out)
+    host = inst.problem.host
+    pinned = {f: torch.from_numpy(np.ascontiguousarray(getattr(host, f))).pin_memory()
+              for f in DeviceProblem.FIELDS}
+    st_pin = st._replace(y=torch.from_numpy(st.y).pin_memory(),
+                         z=torch.from_numpy(st.z).pin_memory(),
+                         P=torch.from_numpy(st.P).pin_memory(),
+                         Omega=torch.from_numpy(st.Omega).pin_memory())
+    for f in ("b", "mask", "scale_a"):
+        pinned[f] = getattr(inst, f).cpu().pin_memory()
+    h2d = sum(t.numel() * t.element_size() for t in pinned.values())
+    h2d += sum(t.numel() * t.element_size() for t in (st_pin.y, st_pin.z, st_pin.P, st_pin.Omega))
+    d2h = 0
+    torch.cuda.synchronize()
+    e2 = torch.cuda.Event(enable_timing=True)
+    e3 = torch.cuda.Event(enable_timing=True)
+    e2.record()
+    e2e_iters = 0
+    for _ in range(args.steps):
+        inst_e = solver.DeviceInstance.__new__(solver.DeviceInstance)
+        inst_e.__dict__.update(inst.__dict__)
+        prob = DeviceProblem.__new__(DeviceProblem)
+        prob.__dict__.update({k: v for k, v in inst.problem.__dict__.items()
+                              if k not in DeviceProblem.FIELDS})
+        for f in DeviceProblem.FIELDS:
+            setattr(prob, f, pinned[f].to(device, non_blocking=True))
+        for f in ("b", "mask", "scale_a"):
+            setattr(inst_e, f, pinned[f].to(device, non_blocking=True))
+        inst_e.problem = prob
+        out, info = run_usbs(st_pin, n, it_step, inst_e, device, q0=q0)
+        y_h, z_h, P_h = out.y.cpu(), out.z.cpu(), out.P.cpu()
+        d2h = (y_h.numel() + z_h.numel() + P_h.numel()) * 8
+        e2e_iters += info["iterations"]
+    e3.record()
+    torch.cuda.synchronize()
+    e2e_ms = e2.elapsed_time(e3)
+    e2e_value = e2e_iters * world / (e2e_ms * 1e-3)
+
+    spmv = None
+    if rank == 0 and not args.no_spmv:
+        try:
+            spmv = spmv_gbs(device)
+            spmv["frac_of_" + peak_kind] = spmv["gbs"] / peak
+        except Exception as exc:  # the main line is still reported
+            spmv = {"error": str(exc)[:200]}
+
+    cpu = None
+    if rank == 0:
+        it, sec = cpu_oracle_iterations(st, n, args.cpu_iters)
+        cpu = {"value": it / sec, "unit": UNIT, "cores": 1, "kind": "port",
+               "sample": f"{it} outer iterations of the NumPy oracle restatement on cfg1 "
+                         f"({sec:.1f} s; JAX reference not installed)"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_max / args.steps, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32 Lanczos / f64 subproblems", "data": "synthetic",
+            "config": {"workload": "maxcut torus 100x100 +-1 (n=10000, nnz=50000), "
+                                   "mixed precision, reference settings",
+                       "iters_per_step": it_step, "settings": S, "parallelism": "replicas",
+                       "l2": "working set ~3 MB stays in the 129 MB L2 (no flush)"},
+            "roofline": {"kernel": "lanczos_team_kernel<float>", "bound": "hbm",
+                         "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "peak_kind": peak_kind,
+                         "launches": lz_n, "ms_per_launch": lz_ms / max(lz_n, 1),
+                         "alg_bytes_per_launch": lz_bytes / max(lz_n, 1), "traffic": None},
+            "lanczos_spmv_rgg1m": spmv,
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
+                    "d2h_bytes_per_step": int(d2h)},
+            "gpu_launches": int(launches),
+            "clocks": clk.summary(),
+            "wall_s": wall,
+        }
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

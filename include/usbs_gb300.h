@@ -94,7 +94,8 @@ size_t usbs_eigsh_workspace_bytes(int n, long long nnz, int inner_iterations, in
  *         [5] status bits (1 barrier timeout, 8 projected eigensolver failure),
  *         [6] kilo-cycles in the restarts, [7] kilo-cycles in total,
  *         [8..12] kilo-cycles of CTA 0 in barrier waits, team reductions and
- *         the three step phases.
+ *         the three step phases, [13] sum over steps of the active basis
+ *         columns, [14] sum over restarts of the saved vectors (for byte counts).
  * Runs as one cooperative kernel; the call is asynchronous. */
 int usbs_eigsh_smallest(int n, long long nnz, const int* rowptr, const int* col,
                         const double* c_val, double c_scale, const int* slot_ptr, const int* slot_tid,
@@ -171,6 +172,11 @@ typedef struct usbs_state {
   int iterations;
   double obj_gap, infeas_gap, max_infeas, obj_ub, pen_dual_obj, elapsed;
   int status;               /* device status bits (see usbs_eigsh_smallest) */
+  /* measurement (outputs): Lanczos launches of the outer loop, their CUDA-event
+   * time on `stream`, their algorithmic bytes, and all kernel launches */
+  int lanczos_launches;
+  double lanczos_ms, lanczos_bytes;
+  long long kernel_launches;
 } usbs_state;
 
 /* Called on the host at every condition check (after the device has caught

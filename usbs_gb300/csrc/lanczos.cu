@@ -418,7 +418,7 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
   double* part1 = P.part + (size_t)R * MP1;
   double* part2 = P.part + (size_t)2 * R * MP1;
 
-  int k = 0, nconv = 0, restart = 0, breakdowns = 0, steps = 0;
+  int k = 0, nconv = 0, restart = 0, breakdowns = 0, steps = 0, sum_nv = 0, sum_kn = 0;
   long long clk_start = clock64(), clk_restart = 0;
   // rank-0 phase accounting: [0] barrier waits, [1] team reductions, [2..4] phases A..C
   long long tp[5] = {0, 0, 0, 0, 0}, tmark = clock64();
@@ -492,6 +492,7 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
       prev = cur;
       cur ^= 1;
       ++steps;
+      sum_nv += i + 1;
     }
     // ---- restart ----
     const bool stepped = (k < m);
@@ -552,6 +553,7 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
       }
     }
     k = kn;
+    sum_kn += kn;
     ++restart;
     if (!bar.sync()) return;
     if (timing) tmark = clock64();   // restart time is reported separately (ctl[6])
@@ -563,6 +565,8 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
     P.ctl[6] = (int)(clk_restart >> 10);
     P.ctl[7] = (int)((clock64() - clk_start) >> 10);
     for (int j = 0; j < 5; ++j) P.ctl[8 + j] = (int)(tp[j] >> 10);
+    P.ctl[13] = sum_nv;
+    P.ctl[14] = sum_kn;
     if (restart == 0) P.ctl[0] = 0;
   }
 }

@@ -691,7 +691,18 @@ struct Solver {
   int gram_ctr_next = 0;
 
   cudaStream_t st2 = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_l0 = nullptr, ev_l1 = nullptr;
+  bool lz_pending = false;
+  long long launches = 0;
+  // algorithmic bytes of one Lanczos launch from its counters (ctl[2], [4], [13], [14])
+  double lanczos_bytes(const int* c) const {
+    const double b = (double)L.vt, n = L.n, nnz = (double)P->nnz;
+    const double steps = c[4], sum_nv = c[13], restarts = c[2], sum_kn = c[14];
+    const double spmv = (4.0 + b) * nnz + 4.0 * (n + 1) + 2.0 * b * n;   // CSR + x + y
+    const double cgs = 3.0 * b * n * sum_nv + 6.0 * b * n * steps;        // 3 Q passes + vectors
+    const double rot = restarts * b * n * L.mL + b * n * (sum_kn + 2.0 * restarts);
+    return steps * spmv + cgs + rot;
+  }
   int gram(const double* X, int ldx, int kx, const double* Y, int ldy, int ky, int n, double* out,
            int side = 0) {
     GramArgs a;
@@ -700,6 +711,7 @@ struct Solver {
     a.counter = side ? ctr_gram2 : ctr_gram;
     a.out = out; a.skip = nullptr;
     cudaStream_t st = side ? st2 : this->st;
+    ++launches;
     int blocks = (n + GR_ROWS - 1) / GR_ROWS;
     if (blocks > L.grid_gram) blocks = L.grid_gram;
     if (blocks < 1) blocks = 1;
@@ -710,6 +722,7 @@ struct Solver {
   }
   int spmm(const double* val, const double* X, int k, double* Y, int side = 0) {
     cudaStream_t st = side ? st2 : this->st;
+    ++launches;
     int blocks = (int)(((long long)L.n * lanes + 255) / 256);
     if (blocks > di.sm_count * 8) blocks = di.sm_count * 8;
     if (blocks < 1) blocks = 1;
@@ -718,6 +731,7 @@ struct Solver {
     return kerr("spmm");
   }
   int assemble(double c_scale, const double* w, void* out, int prec, int side = 0) {
+    ++launches;
     return assemble_operator((int)P->nnz, P->c_val, c_scale, P->slot_ptr, P->slot_tid, P->t_con,
                              P->t_a0, w, out, prec, side ? st2 : st);
   }
@@ -752,19 +766,45 @@ struct Solver {
     return b < 1 ? 1 : b;
   }
   // eigsh on -C + A*(w): leaves num_desired vectors in Q and Ritz values in alpha
-  int lanczos(const double* w, int num_desired) {
+  int lanczos(const double* w, int num_desired, bool timed = false) {
     CK(assemble(-1.0, w, L.opL, Pa->precision));
     if (cudaMemcpyAsync(L.Q, L.q0L, (size_t)L.n * L.vt, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
       return kerr("q0 copy");
+    if (timed) {
+      cudaEventRecord(ev_l0, st);
+      const int rc = lanczos_launch(num_desired);
+      cudaEventRecord(ev_l1, st);
+      lz_pending = true;
+      return rc;
+    }
+    return lanczos_launch(num_desired);
+  }
+  int lanczos_launch(int num_desired) {
     LanczosProblem lp;
     lp.n = L.n; lp.ld = L.ld; lp.m = L.mL; lp.num_desired = num_desired;
     lp.max_restarts = Pa->lanczos_max_restarts; lp.nnz = P->nnz; lp.tol = Pa->subprob_eps;
     lp.rowptr = P->rowptr; lp.col = P->col; lp.val = L.opL; lp.Q = L.Q;
     lp.alpha = L.alpha; lp.beta = L.beta; lp.ctl = L.ctl; lp.status = L.status;
     lp.work = L.lz_work;
+    ++launches;
     return lanczos_run(di, &lp, 1, Pa->precision, st);
   }
+  // after a host sync: fold the last timed launch into the state's counters
+  int collect_lanczos() {
+    if (!lz_pending) return 0;
+    float ms = 0.f;
+    int c[16];
+    if (cudaEventElapsedTime(&ms, ev_l0, ev_l1) != cudaSuccess ||
+        cudaMemcpy(c, L.ctl, sizeof(c), cudaMemcpyDeviceToHost) != cudaSuccess)
+      return kerr("lanczos timing");
+    S->lanczos_ms += ms;
+    S->lanczos_launches += 1;
+    S->lanczos_bytes += lanczos_bytes(c);
+    lz_pending = false;
+    return 0;
+  }
   int copy_q_cols(int cols, double* dst) {
+    ++launches;
     int blocks = rgrid();
     if (Pa->precision == 64)
       copy_cols_kernel<double><<<blocks, 256, 0, st>>>(L.n, cols, (const double*)L.Q, L.ld, dst, L.ld, nullptr);
@@ -785,7 +825,7 @@ struct Solver {
     return a;
   }
   int cur_t = 0;
-  int run_ipm(int mode) { return launch_ipm(ipm_args(mode), st); }
+  int run_ipm(int mode) { ++launches; return launch_ipm(ipm_args(mode), st); }
   int read_scalars(double* out, int first, int count) {
     if (cudaMemcpyAsync(out, L.smalls + L.o_sc + first, count * sizeof(double),
                         cudaMemcpyDeviceToHost, st) != cudaSuccess)
@@ -814,6 +854,7 @@ static int body(Solver& X, int t) {
   CK(X.proj(0.0, L.zbar, V, L.o_GZ));                 // V^T A*(z_bar) V
   {
     MvecArgs ma = X.margs();
+    ++X.launches;
     mvec_pre_kernel<<<X.mgrid(), RED_BLOCK, 0, st>>>(ma, Pa->trace_ub, L.k, 1);
     CK(kerr("mvec_pre"));
   }
@@ -821,6 +862,7 @@ static int body(Solver& X, int t) {
   {
     int blocks = (int)(((long long)L.m * 32 + 255) / 256);
     if (blocks > X.di.sm_count * 16) blocks = X.di.sm_count * 16;
+    ++X.launches;
     svec_project_kernel<<<blocks, 256, 0, st>>>(L.m, P->con_ptr, P->t_row, P->t_col, P->t_a, V,
                                                 L.ld, L.k, L.Pm, L.m, nullptr);
     CK(kerr("svec_project"));
@@ -845,13 +887,16 @@ static int body(Solver& X, int t) {
   const int qblocks = X.mgrid();
   for (int pass = 0; pass < Pa->subprob_max_iters; ++pass) {
     CK(X.run_ipm(0));
+    ++X.launches;
     CK(launch_eigS(ea, st));
+    ++X.launches;
     quadform_kernel<<<qblocks, 256, 0, st>>>(L.m, P->con_ptr, P->t_row, P->t_col, P->t_a, V, L.ld,
                                              L.k, L.smalls + L.o_Splus, L.smalls + L.o_Scplus,
                                              L.AF, L.AFc, nullptr);
     CK(kerr("quadform"));
     if (!P->has_ineq) break;       // upsilon stays 0: the loop ends after one pass
     MvecArgs ma = X.margs();
+    ++X.launches;
     mvec_upsilon_kernel<<<X.mgrid(), RED_BLOCK, 0, st>>>(ma);
     CK(kerr("upsilon"));
     double gap = 0.0;
@@ -863,6 +908,7 @@ static int body(Solver& X, int t) {
       return kerr("S warm start");
     {
       MvecArgs mb = X.margs();
+      ++X.launches;
       mvec_pre_kernel<<<X.mgrid(), RED_BLOCK, 0, st>>>(mb, Pa->trace_ub, L.k, 0);
       CK(kerr("mvec_pre"));
     }
@@ -871,11 +917,13 @@ static int body(Solver& X, int t) {
   // ---- z, y_cand, infeasibility, z_bar (solver/usbs.py:582-583, 638-639, 648-652) ----
   {
     MvecArgs ma = X.margs();
+    ++X.launches;
     mvec_update_kernel<<<X.mgrid(), RED_BLOCK, 0, st>>>(ma);
     CK(kerr("mvec_update"));
   }
   // ---- sketch / X updates and kept directions ----
   if (Pa->sketch_mode == 1) {
+    ++X.launches;
     xmode_kernel<<<X.di.sm_count * 8, 256, 0, st>>>(L.n, L.k, V, L.ld, L.smalls, L.o_sc, L.o_Sout,
                                                     L.o_Scplus, S->X, L.Xbar, nullptr);
     CK(kerr("xmode"));
@@ -887,6 +935,7 @@ static int body(Solver& X, int t) {
     ra.o_sc = L.o_sc; ra.o_M = L.o_M; ra.o_Mc = L.o_Mc; ra.o_Splus = L.o_Splus;
     ra.o_Scplus = L.o_Scplus; ra.o_Wpast = L.o_Wpast; ra.Vn = L.Vn; ra.ldvn = L.ld;
     ra.skip = nullptr;
+    ++X.launches;
     rows_update_kernel<<<X.rgrid(), 256, 0, st>>>(ra);
     CK(kerr("rows_update"));
   }
@@ -896,10 +945,11 @@ static int body(Solver& X, int t) {
       cudaStreamWaitEvent(X.st2, X.ev_fork, 0) != cudaSuccess)
     return kerr("fork");
   CK(X.proj(-1.0, L.ycand, V, L.o_GYC, 1));     // V^T (A*(y_cand) - C) V (solver/usbs.py:219-220)
+  ++X.launches;
   CK(launch_ipm(X.ipm_args(1), X.st2));
   if (cudaEventRecord(X.ev_join, X.st2) != cudaSuccess) return kerr("join record");
   // ---- candidate eigenvectors at y_cand (solver/usbs.py:588-599) ----
-  CK(X.lanczos(L.ycand, L.kc));
+  CK(X.lanczos(L.ycand, L.kc, true));
   CK(X.copy_q_cols(L.kc, L.Vn + (size_t)L.kp * L.ld));
   if (cudaStreamWaitEvent(st, X.ev_join, 0) != cudaSuccess) return kerr("join");
   int refined = 0;
@@ -909,6 +959,7 @@ static int body(Solver& X, int t) {
     CK(X.spmm(L.op64b, Vc, L.kc, L.CV));
     CK(X.gram(Vc, L.ld, L.kc, L.CV, L.ld, L.kc, L.n, L.smalls + L.o_GR1));
     CK(X.gram(Vc, L.ld, L.kc, Vc, L.ld, L.kc, L.n, L.smalls + L.o_GR2));
+    ++X.launches;
     rayleigh_kernel<<<1, 32, 0, st>>>(L.smalls, L.o_GR1, L.o_GR2, L.o_GR, L.kc, nullptr);
     CK(kerr("rayleigh"));
     refined = 1;
@@ -920,9 +971,11 @@ static int body(Solver& X, int t) {
     pa.beta = Pa->beta; pa.scale_c = P->scale_c; pa.scale_x = P->scale_x; pa.bnorm = P->b_norm;
     pa.trace = (S->trace && t < S->trace_capacity) ? S->trace : nullptr;
     pa.t = t; pa.skip = nullptr;
+    ++X.launches;
     post_kernel<<<1, 32, 0, st>>>(pa);
     CK(kerr("post"));
   }
+  ++X.launches;
   descent_copy_kernel<<<X.mgrid(), 256, 0, st>>>(L.m, L.smalls, L.o_sc, S->y, L.ycand, nullptr);
   CK(kerr("descent"));
   // ---- next basis: shifted CholQR3 of [V W_past, cand_vecs] (solver/usbs.py:640-642) ----
@@ -931,7 +984,9 @@ static int body(Solver& X, int t) {
     CholQRArgs ca;
     ca.k = L.k; ca.n = L.n; ca.shifted = (pass == 0); ca.smalls = L.smalls; ca.o_G = L.o_G;
     ca.o_Rinv = L.o_Rinv; ca.status = L.status; ca.skip = nullptr;
+    ++X.launches;
     CK(launch_cholqr(ca, st));
+    ++X.launches;
     rows_rinv_kernel<<<X.rgrid(), 256, 0, st>>>(L.n, L.k, L.Vn, L.ld, L.smalls + L.o_Rinv, nullptr);
     CK(kerr("rinv"));
   }
@@ -1011,14 +1066,20 @@ int usbs_solve(const usbs_problem* P, const usbs_params* Pa, usbs_state* S, void
   X.ctr_m = L.counters + 16;
   if (cudaStreamCreateWithFlags(&X.st2, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreateWithFlags(&X.ev_fork, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&X.ev_join, cudaEventDisableTiming) != cudaSuccess)
+      cudaEventCreateWithFlags(&X.ev_join, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreate(&X.ev_l0) != cudaSuccess || cudaEventCreate(&X.ev_l1) != cudaSuccess)
     return kerr("stream/event create");
+  S->lanczos_launches = 0;
+  S->lanczos_ms = 0.0;
+  S->lanczos_bytes = 0.0;
   struct Cleanup {
     Solver* x;
     ~Cleanup() {
       if (x->st2) cudaStreamDestroy(x->st2);
       if (x->ev_fork) cudaEventDestroy(x->ev_fork);
       if (x->ev_join) cudaEventDestroy(x->ev_join);
+      if (x->ev_l0) cudaEventDestroy(x->ev_l0);
+      if (x->ev_l1) cudaEventDestroy(x->ev_l1);
     }
   } cleanup{&X};
   cudaMemsetAsync(L.counters, 0, 64 * sizeof(unsigned int), st);
@@ -1098,10 +1159,15 @@ int usbs_solve(const usbs_problem* P, const usbs_params* Pa, usbs_state* S, void
   CK(cond(0, &go));
   for (size_t b = 0; b < sched.size() && go; ++b) {
     for (long long j = 0; j < sched[b]; ++j) {
+      if (j > 0) {   // within a block: sync only to collect the previous Lanczos timing
+        if (cudaStreamSynchronize(st) != cudaSuccess) return kerr("iteration");
+        CK(X.collect_lanczos());
+      }
       CK(body(X, t));
       ++t;
     }
     if (cudaStreamSynchronize(st) != cudaSuccess) return kerr("iteration");
+    CK(X.collect_lanczos());
     curr_time = elapsed();
     CK(cond(t, &go));
   }
@@ -1121,6 +1187,7 @@ int usbs_solve(const usbs_problem* P, const usbs_params* Pa, usbs_state* S, void
   S->pen_dual_obj = sc[SC_PEN];
   S->status = status[0];
   S->elapsed = elapsed();
+  S->kernel_launches = X.launches;
   return 0;
 }
 

@@ -57,7 +57,9 @@ class UsbsState(ctypes.Structure):
          ("obj_gap", ctypes.c_double), ("infeas_gap", ctypes.c_double),
          ("max_infeas", ctypes.c_double), ("obj_ub", ctypes.c_double),
          ("pen_dual_obj", ctypes.c_double), ("elapsed", ctypes.c_double),
-         ("status", ctypes.c_int)]
+         ("status", ctypes.c_int), ("lanczos_launches", ctypes.c_int),
+         ("lanczos_ms", ctypes.c_double), ("lanczos_bytes", ctypes.c_double),
+         ("kernel_launches", ctypes.c_longlong)]
 
 
 CALLBACK = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int)
@@ -123,6 +125,14 @@ def _host(x):
     return x
 
 
+def _to_dev(x, device):
+    """float64 tensor on `device` (device tensors are not routed through the host)."""
+    import torch
+    if isinstance(x, torch.Tensor):
+        return x.to(device=device, dtype=torch.float64)
+    return torch.as_tensor(np.asarray(x, dtype=np.float64), device=device)
+
+
 def _dev_cols(x, rows, ld, cols, device, dtype):
     """Column-major (cols x ld) device tensor from an (rows, cols) array."""
     import torch
@@ -149,27 +159,26 @@ def usbs(sdp_state, n, m, trace_ub, trace_factor, rho, beta, k_curr, k_past, max
     k = k_curr + k_past
     ld = (n + 31) // 32 * 32
     f64 = torch.float64
-    y = torch.as_tensor(np.asarray(_host(sdp_state.y), dtype=np.float64), device=dev).clone()
-    z = torch.as_tensor(np.asarray(_host(sdp_state.z), dtype=np.float64), device=dev).clone()
+    y = _to_dev(sdp_state.y, dev).clone()
+    z = _to_dev(sdp_state.z, dev).clone()
     V = torch.zeros((k, ld), dtype=f64, device=dev)
     if sdp_state.X is not None:
         mode, sdim = 1, 0
-        X = torch.as_tensor(np.asarray(_host(sdp_state.X), dtype=np.float64), device=dev).clone()
+        X = _to_dev(sdp_state.X, dev).clone()
         Pm = Om = None
     elif sdp_state.Omega is not None:
         mode = 0
-        sdim = int(np.asarray(_host(sdp_state.Omega)).shape[1])
-        Om = _dev_cols(_host(sdp_state.Omega), n, ld, sdim, dev, f64)
-        Pm = _dev_cols(_host(sdp_state.P), n, ld, sdim, dev, f64)
+        sdim = int(sdp_state.Omega.shape[1])
+        Om = _dev_cols(sdp_state.Omega, n, ld, sdim, dev, f64)
+        Pm = _dev_cols(sdp_state.P, n, ld, sdim, dev, f64)
         X = None
     else:
         mode, sdim = 2, 0
         Pm = torch.zeros(ld, dtype=f64, device=dev)
         if sdp_state.P is not None:
-            Pm[:n] = torch.as_tensor(np.asarray(_host(sdp_state.P), dtype=np.float64).reshape(-1))
+            Pm[:n] = _to_dev(sdp_state.P, dev).reshape(-1)
         Om = X = None
-    q0 = default_q0(n) if q0 is None else np.asarray(_host(q0), dtype=np.float64)
-    q0t = torch.as_tensor(q0, dtype=f64, device=dev)
+    q0t = _to_dev(default_q0(n) if q0 is None else q0, dev)
     trace = torch.zeros((max(max_iters, 1), TRACE_WIDTH), dtype=f64, device=dev) \
         if return_trace else None
 
@@ -217,7 +226,9 @@ def usbs(sdp_state, n, m, trace_ub, trace_factor, rho, beta, k_curr, k_past, max
     info = dict(iterations=pst.iterations, obj_gap=pst.obj_gap, infeas_gap=pst.infeas_gap,
                 max_infeas=pst.max_infeas, obj_ub=pst.obj_ub, pen_dual_obj=pst.pen_dual_obj,
                 elapsed=pst.elapsed, status=pst.status, callback_vals=cb_val,
-                V=V[:, :n].t())
+                V=V[:, :n].t(), lanczos_launches=pst.lanczos_launches,
+                lanczos_ms=pst.lanczos_ms, lanczos_bytes=pst.lanczos_bytes,
+                kernel_launches=pst.kernel_launches)
     if return_trace:
         tr = trace[:pst.iterations].cpu().numpy()
         recs = [{f: float(r[i]) for i, f in enumerate(TRACE_FIELDS)} for r in tr]
