@@ -104,6 +104,36 @@ int usbs_eigsh_smallest(int n, long long nnz, const int* rowptr, const int* col,
                         double tolerance, int precision, void* Q, int ldq, double* eigenvalues,
                         int* info, void* workspace, size_t workspace_bytes, void* stream);
 
+/* Bytes of the library's fixed device scratch for usbs_eigsh_smallest_noalloc. */
+#define USBS_EIGSH_STATIC_SCRATCH_BYTES (16u << 20)
+
+/* usbs_eigsh_smallest without a workspace argument, for callers that cannot
+ * allocate device memory (a JAX/XLA custom call, whose runtime has already
+ * reserved most of HBM, or a serving process with a fixed memory budget).
+ * No counterpart in the reference: its eigsh_smallest allocates through JAX.
+ *  - Allocates nothing: no cudaMalloc/cudaFree, no allocating library call.
+ *    Scratch is a 16 MiB static device array in the library image.
+ *  - The first call on each device looks up that array's address
+ *    (cudaGetSymbolAddress, with that device current) and caches it.  Make
+ *    that first call before any stream capture on the device.
+ *  - Problems whose usbs_eigsh_workspace_bytes() exceeds
+ *    USBS_EIGSH_STATIC_SCRATCH_BYTES are rejected (-2, usbs_last_error()).
+ *    With the usual 32 inner iterations that is about nnz + 2*n above
+ *    2.0e6 (FP64) or 4.0e6 (FP32).
+ *  - The scratch need not start at zero: each call clears its barrier
+ *    counters, info words and Lanczos coefficients on `stream` before use.
+ *  - One scratch per device: calls whose work may overlap in time on the
+ *    same device (different streams or host threads) race.  Calls issued in
+ *    order on one stream are safe.
+ * Arguments, results and asynchrony are those of usbs_eigsh_smallest. */
+int usbs_eigsh_smallest_noalloc(int n, long long nnz, const int* rowptr, const int* col,
+                                const double* c_val, double c_scale, const int* slot_ptr,
+                                const int* slot_tid, const int* t_con, const double* t_a,
+                                const double* adjoint_left_vec, const void* q0, int num_desired,
+                                int inner_iterations, int max_restarts, double tolerance,
+                                int precision, void* Q, int ldq, double* eigenvalues, int* info,
+                                void* stream);
+
 /* ------------------------------------------------------------------ usbs()
  * One SDP instance, resident in device memory.  Field meanings follow the
  * reference's SDPState (utils/common.py:11-26) after scale_sdp_state. */

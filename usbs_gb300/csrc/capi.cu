@@ -46,6 +46,33 @@ int get_device_info(DeviceInfo* out) {
 
 static size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
 
+// Fixed device scratch of usbs_eigsh_smallest_noalloc: part of the module
+// image, so it exists on every device that loads the library and is never
+// allocated or freed at run time.  Its address is looked up once per device.
+static __device__ __align__(256) unsigned char g_eigsh_scratch[USBS_EIGSH_STATIC_SCRATCH_BYTES];
+static void* g_eigsh_scratch_addr[64];
+static std::mutex g_eigsh_scratch_mu;
+
+static int eigsh_static_scratch(void** out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) { set_error("cudaGetDevice: %s", cudaGetErrorString(e)); return -5; }
+  if (dev < 0 || dev >= 64) { set_error("device index %d out of range", dev); return -2; }
+  std::lock_guard<std::mutex> lk(g_eigsh_scratch_mu);
+  if (!g_eigsh_scratch_addr[dev]) {
+    void* p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_eigsh_scratch);
+    if (e != cudaSuccess || !p) {
+      set_error("eigsh_noalloc: cudaGetSymbolAddress of the static scratch on device %d: %s", dev,
+                cudaGetErrorString(e));
+      return -5;
+    }
+    g_eigsh_scratch_addr[dev] = p;
+  }
+  *out = g_eigsh_scratch_addr[dev];
+  return 0;
+}
+
 }  // namespace usbs
 
 using namespace usbs;
@@ -180,6 +207,35 @@ int usbs_eigsh_smallest(int n, long long nnz, const int* rowptr, const int* col,
     return -5;
   }
   return 0;
+}
+
+int usbs_eigsh_smallest_noalloc(int n, long long nnz, const int* rowptr, const int* col,
+                                const double* c_val, double c_scale, const int* slot_ptr,
+                                const int* slot_tid, const int* t_con, const double* t_a,
+                                const double* adjoint_left_vec, const void* q0, int num_desired,
+                                int inner_iterations, int max_restarts, double tolerance,
+                                int precision, void* Q, int ldq, double* eigenvalues, int* info,
+                                void* stream) {
+  if (precision != 32 && precision != 64) { set_error("precision must be 32 or 64"); return -2; }
+  if (n < 1 || inner_iterations < 1 || inner_iterations > MAXM || nnz < 0 || nnz > 0x7fffffffLL) {
+    set_error("eigsh_noalloc: bad sizes n=%d nnz=%lld inner_iterations=%d (<= %d)", n, nnz,
+              inner_iterations, MAXM);
+    return -2;
+  }
+  const size_t need = usbs_eigsh_workspace_bytes(n, nnz, inner_iterations, precision);
+  if (need > (size_t)USBS_EIGSH_STATIC_SCRATCH_BYTES) {
+    set_error("eigsh_noalloc: n=%d nnz=%lld inner_iterations=%d precision=%d needs %zu bytes of "
+              "scratch, the static scratch holds %zu; call usbs_eigsh_smallest with a workspace",
+              n, nnz, inner_iterations, precision, need, (size_t)USBS_EIGSH_STATIC_SCRATCH_BYTES);
+    return -2;
+  }
+  void* scratch = nullptr;
+  int rc = eigsh_static_scratch(&scratch);
+  if (rc) return rc;
+  return usbs_eigsh_smallest(n, nnz, rowptr, col, c_val, c_scale, slot_ptr, slot_tid, t_con, t_a,
+                             adjoint_left_vec, q0, num_desired, inner_iterations, max_restarts,
+                             tolerance, precision, Q, ldq, eigenvalues, info, scratch,
+                             (size_t)USBS_EIGSH_STATIC_SCRATCH_BYTES, stream);
 }
 
 }  // extern "C"

@@ -20,7 +20,6 @@
 // eigensolver; after a barrier every CTA rotates its rows of Q by the saved
 // Ritz vectors.
 #include <stdlib.h>
-#include <vector>
 #include "common.cuh"
 #include "dense.cuh"
 #include "internal.h"
@@ -622,7 +621,7 @@ static int run_typed(const DeviceInfo& di, const LanczosProblem* probs, int coun
     TeamBatch<VT> batch;
     batch.count = cnt;
     int total = 0;
-    std::vector<int> want(cnt);
+    int want[MAX_TEAMS];   // cnt <= MAX_TEAMS; no heap allocation on the launch path
     for (int i = 0; i < cnt; ++i) {
       want[i] = lanczos_team_size(di, probs[base + i].n, sizeof(VT) == 8 ? 64 : 32);
       total += want[i];
