@@ -178,6 +178,30 @@ def spmv_gbs(device, reps=20):
             "gbs": alg / (t * 1e-3) / 1e9}
 
 
+def profile_case(args):
+    """One untimed run of a single piece of the workload, for profiler captures."""
+    import torch
+    device = torch.device("cuda:0")
+    torch.cuda.set_device(device)
+    if args.profile_case == "spmv":
+        r = spmv_gbs(device, reps=1)
+        print(json.dumps({"profile_case": "spmv", "kernel_launches_timed": 1, **r}))
+        return 0
+    from usbs_gb300 import solver
+    from usbs_gb300.problems import maxcut
+    from usbs_gb300.rng import default_q0
+    W = workload(0)
+    st = maxcut.initialize_state(W, SETTINGS["sketch_dim"])
+    n = st.C.shape[0]
+    inst = solver.DeviceInstance(st, device)
+    out, info = run_usbs(st, n, args.iters_per_step, inst, device, q0=default_q0(n))
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_case": "usbs", "iterations": info["iterations"],
+                      "lanczos_launches": info["lanczos_launches"],
+                      "kernel_launches": info["kernel_launches"]}))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -187,7 +211,13 @@ def main():
     ap.add_argument("--iters-per-step", type=int, default=10)
     ap.add_argument("--cpu-iters", type=int, default=24)
     ap.add_argument("--no-spmv", action="store_true")
+    ap.add_argument("--profile-case", choices=["usbs", "spmv"], default=None,
+                    help="run one piece of the workload once, untimed (for ncu captures): "
+                         "'usbs' = --iters-per-step outer iterations on the torus instance, "
+                         "'spmv' = the RGG operator apply (3 launches)")
     args = ap.parse_args()
+    if args.profile_case:
+        return profile_case(args)
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local = int(os.environ.get("LOCAL_RANK", "0"))

@@ -144,3 +144,45 @@ def test_eigsh_breakdown_small_operator(cuda):
     np.testing.assert_allclose(_np(gv), ov, atol=1e-9)
     ex = np.linalg.eigvalsh((-st.C).toarray())[:3]
     np.testing.assert_allclose(_np(gv), ex, atol=1e-9)
+
+
+def _ragged_csr(n, base_len, long_rows, long_len, seed):
+    rs = np.random.default_rng(seed)
+    lens = rs.integers(0, 2 * base_len + 1, size=n)
+    lens[rs.choice(n, size=min(long_rows, n), replace=False)] = long_len
+    rowptr = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    col = rs.integers(0, n, size=int(rowptr[-1])).astype(np.int32)
+    val = rs.standard_normal(int(rowptr[-1]))
+    return sp.csr_matrix((val, col, rowptr), shape=(n, n))
+
+
+# (n, typical entries per row, rows with long_len entries, long_len): tails that are
+# not multiples of 16 bytes, tiles above the staging capacity, empty rows, dense rows
+@pytest.mark.parametrize("shape", [(1, 1, 0, 0), (257, 3, 0, 0), (1000, 7, 3, 40),
+                                   (5003, 2, 2, 4000), (4099, 12, 1, 300), (3001, 30, 0, 0)])
+@pytest.mark.parametrize("precision", [64, 32])
+def test_operator_apply_ragged_csr(cuda, shape, precision):
+    import ctypes
+    import torch
+    from usbs_gb300 import _lib
+    lib = _lib.load()
+    M = _ragged_csr(*shape, seed=shape[0])
+    n, nnz = M.shape[0], M.nnz
+    vt = torch.float64 if precision == 64 else torch.float32
+    rs = np.random.default_rng(3)
+    x = rs.standard_normal(n)
+    rp = torch.tensor(M.indptr, dtype=torch.int32, device=cuda)
+    cl = torch.tensor(M.indices, dtype=torch.int32, device=cuda)
+    vv = torch.tensor(M.data, dtype=vt, device=cuda)
+    xx = torch.tensor(x, dtype=vt, device=cuda)
+    y = torch.full((n,), float("nan"), dtype=vt, device=cuda)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.usbs_operator_apply(n, nnz, p(rp), p(cl), p(vv), p(xx), p(y), precision, s) == 0
+    got = y.double().cpu().numpy()
+    Mv = M.astype(np.float32).astype(np.float64) if precision == 32 else M
+    xr = x.astype(np.float32).astype(np.float64) if precision == 32 else x
+    ref = Mv @ xr
+    scale = np.abs(Mv).sum(axis=1).A1 * np.abs(xr).max() + 1e-300
+    tol = 1e-13 if precision == 64 else 2e-6
+    assert np.all(np.abs(got - ref) <= tol * scale)

@@ -134,3 +134,33 @@ def test_usbs_precisions_agree_on_solution(cuda):
         assert info["obj_gap"] <= eps, info
         vals.append(out.primal_obj)
     assert abs(vals[0] - vals[1]) / abs(vals[0]) < 2 * eps
+
+
+def test_usbs_qap_fp64_trace_matches_oracle(cuda):
+    """QAP relaxation (general triples, '<=' rows, the upsilon alternating
+    minimisation of solver/usbs.py:359-433) on the device vs the FP64 oracle."""
+    from oracle import qap as oqap
+    from usbs_gb300 import solver
+    l = 5
+    D, Wf = wl.qap_instance(l, 0, grid=5)
+    st = oqap.initialize_state(D, Wf, 6)
+    n, m = st.C.shape[0], st.b.shape[0]
+    assert np.any(st.b_ineq_mask > 0)
+    trace_factor, rho = 2.0, 0.005
+    trace_ub = trace_factor * float(l + 1) * st.SCALE_X
+    q0 = orng.default_q0(n)
+    mL = min(n, 32)
+    iters = 4
+    otr = []
+    oout, ofin = ousbs.usbs(st, n, m, trace_ub, trace_factor, rho, 0.25, 2, 0, iters, np.inf,
+                            -1.0, -1.0, -1.0, mL, 300, 1e-9, 100, q0=q0, trace=otr)
+    gout, gtr, info = solver.usbs(st, n, m, trace_ub, trace_factor, rho, 0.25, 2, 0, iters,
+                                  np.inf, -1.0, -1.0, -1.0, mL, 300, 1e-9, 100, 1.0, None, None,
+                                  None, q0=q0, precision=64, return_trace=True)
+    assert info["status"] == 0 and info["iterations"] == iters
+    for a, b in zip(otr, gtr):
+        tol = (1e-7, 1e-6, 1e-5)[a["t"]] if a["t"] < 3 else 1e-4
+        for key in ("primal_obj", "obj_ub", "pen_dual_obj", "obj_gap", "infeas_gap",
+                    "max_infeas", "tr_X"):
+            assert _rel(a[key], b[key]) < tol, (a["t"], key, a[key], b[key])
+    np.testing.assert_allclose(gout.y.cpu().numpy(), oout.y, rtol=1e-3, atol=1e-5)

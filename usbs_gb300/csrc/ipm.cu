@@ -36,6 +36,9 @@ struct IpmShared {
   double redv[IPM_BLOCK / 32];
   int redi[IPM_BLOCK / 32];
   double lcol[IPM_MAXS];
+  double dinv[IPM_MAXS];
+  double u2[IPM_MAXS], w2[IPM_MAXS];   // per-column terms of the rank-2 correction
+  int cord[IPM_MAXS];                  // svec indices, off-diagonal ones first
 };
 
 // sum_a x[a] y[a], computed redundantly by every warp (identical in all threads)
@@ -58,20 +61,22 @@ __device__ __forceinline__ void svec_inv_to(const double* v, int k, int s, const
   }
 }
 
-// 0.5 * [U (T (x) X + X (x) T) U^T]_{a, a2}
-__device__ __forceinline__ double symkron(const double* T, const double* X, int k, int b, int c,
-                                          int b2, int c2) {
-  const int na = (b == c) ? 1 : 2, nb = (b2 == c2) ? 1 : 2;
-  const double wa = (b == c) ? 1.0 : RSQ2, wb = (b2 == c2) ? 1.0 : RSQ2;
-  double acc = 0.0;
-  for (int u = 0; u < na; ++u) {
-    const int i = u ? c : b, j = u ? b : c;
-    for (int v = 0; v < nb; ++v) {
-      const int i2 = v ? c2 : b2, j2 = v ? b2 : c2;
-      acc += T[i * k + i2] * X[j * k + j2] + X[i * k + i2] * T[j * k + j2];
-    }
+// 0.5 * [U (T (x) X + X (x) T) U^T]_{a, a2}, U the svec isometry.
+// The same entry with each distinct product summed once: of the 2 na nb
+// products of the definition every one appears twice (T_ii2 X_jj2 for the
+// ordering (i, j) equals X_jj2 T_ii2 for (j, i)), and 0.5 * 2 is exact, so
+//   entry = w * sum over the orderings (i2, j2) of a2 of T_b,i2 X_c,j2 + X_b,i2 T_c,j2
+// (one ordering when a is diagonal), w = 1/2 when a and a2 are both diagonal or
+// both off-diagonal, 1/sqrt(2) otherwise.
+__device__ __forceinline__ double symkron_sum(const double* T, const double* X, int k, int b,
+                                              int c, int b2, int c2) {
+  double S = T[b * k + b2] * X[c * k + c2];
+  S = fma(X[b * k + b2], T[c * k + c2], S);
+  if (b2 != c2 && b != c) {
+    S = fma(T[b * k + c2], X[c * k + b2], S);
+    S = fma(X[b * k + c2], T[c * k + b2], S);
   }
-  return 0.5 * wa * wb * acc;
+  return (((b == c) == (b2 == c2)) ? 0.5 : RSQ2) * S;
 }
 
 // Positive-definiteness test of A + s dA (k x k, lower triangle) by LDL^T
@@ -116,86 +121,126 @@ __device__ __forceinline__ unsigned long long abs_key(double x) {
   return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
 }
 
-// LU with partial pivoting and solve, whole CTA (G&VL Alg. 3.4.1).  Warps own
-// rows, lanes own columns.  The trailing update of column j+1 also records,
-// per warp, the largest |a| below the diagonal, so the next pivot is a pick
-// among 8 candidates; multipliers are formed inside each warp.  Two CTA
-// barriers per column.  Ties go to the smaller row index, as in LAPACK.
-__device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* redv, double* lcol,
+// LU with partial pivoting and solve, whole CTA (G&VL Alg. 3.4.1, right-looking
+// with a one-column look-ahead).  On GB300 a dependent FP64 operation costs
+// ~64 cycles and a division ~440, so the pivot chain of each column (argmax,
+// reciprocal, multipliers) is kept off the critical path: while warps 1..7
+// apply the rank-1 update of column j to columns j+2.., warp 0 updates column
+// j+1, picks its pivot (largest |a|, ties to the smaller row index as in
+// LAPACK), forms the pivot reciprocal and the multipliers of column j+1 and
+// applies column j to b.  Rows are swapped physically at the start of each
+// column.  L is not stored: b is eliminated alongside.  Every element sees the
+// arithmetic of the textbook algorithm (a_ic - l_i a_jc, l_i = a_ij * (1/a_jj)).
+__device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* dinv, double* lcol,
                              int* piv_out, int* ok_out) {
-  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
-  __shared__ unsigned long long cand_key[IPM_BLOCK / 32];
-  __shared__ int cand_row[IPM_BLOCK / 32];
-  (void)lcol;
-  // pivot candidates for column 0
-  {
+  const int tid = threadIdx.x, lane = tid & 31;
+  __shared__ double lnext[IPM_MAXS];
+  __shared__ int pnext[2];   // pivot of column j in pnext[j & 1] (written one column ahead)
+  double* lc = lcol;      // multipliers of the current column (indexed by row)
+  double* ln = lnext;     // multipliers of the next column
+  // look-ahead for column 0 (warp 0): pivot, reciprocal, multipliers
+  auto pick = [&](int j, double* lout) {
+    // rows j..n-1 of column j are final; lane q holds rows j+q, j+q+32, ...
     unsigned long long best = 0ull;
     int bi = 0x7fffffff;
-    for (int i = wid; i < n; i += nw) {
-      if (lane == 0) {
-        const unsigned long long k = abs_key(A[i * lda]);
-        if (k > best || (k == best && i < bi) || bi == 0x7fffffff) { best = k; bi = i; }
+    for (int i = j + lane; i < n; i += 32) {
+      const unsigned long long kk = abs_key(A[i * lda + j]);
+      if (bi == 0x7fffffff || kk > best) { best = kk; bi = i; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const unsigned long long k2 = __shfl_xor_sync(0xffffffffu, best, o);
+      const int r2 = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (r2 != 0x7fffffff && (bi == 0x7fffffff || k2 > best || (k2 == best && r2 < bi))) {
+        best = k2; bi = r2;
       }
     }
-    if (lane == 0) { cand_key[wid] = best; cand_row[wid] = bi; }
-  }
+    if (bi == 0x7fffffff) bi = j;
+    const double pv = A[bi * lda + j];
+    const double inv = (pv == 0.0) ? 1.0 : 1.0 / pv;
+    // multipliers of rows j..n-1 as they sit now; the pivot row's entry is
+    // moved to row j by the swap at the start of column j
+    for (int i = j + lane; i < n; i += 32) lout[i] = A[i * lda + j] * inv;
+    if (lane == 0) {
+      pnext[j & 1] = bi;
+      dinv[j] = inv;
+      if (pv == 0.0) *ok_out = 0;
+    }
+  };
   if (tid == 0) *ok_out = 1;
   __syncthreads();
+  if (tid < 32) pick(0, lc);
+  __syncthreads();
   for (int j = 0; j < n; ++j) {
-    if (tid == 0) {
-      unsigned long long best = 0ull;
-      int bi = 0x7fffffff;
-      for (int w = 0; w < nw; ++w) {
-        const int r = cand_row[w];
-        if (r == 0x7fffffff) continue;
-        const unsigned long long k = cand_key[w];
-        if (bi == 0x7fffffff || k > best || (k == best && r < bi)) { best = k; bi = r; }
-      }
-      if (bi == 0x7fffffff) bi = j;
-      *piv_out = bi;
-      const double pv = A[bi * lda + j];
-      if (pv == 0.0) *ok_out = 0;
-      redv[0] = (pv == 0.0) ? 1.0 : 1.0 / pv;
-    }
-    __syncthreads();
-    const int piv = *piv_out;
-    const double inv = redv[0];
+    const int piv = pnext[j & 1];
+    if (j == 0) *piv_out = piv;
+    // swap rows j and piv (columns j.., b and the multipliers of column j)
     if (piv != j) {
-      for (int c = tid; c < n; c += blockDim.x) {
+      for (int c = j + tid; c < n; c += blockDim.x) {
         const double t = A[j * lda + c];
         A[j * lda + c] = A[piv * lda + c];
         A[piv * lda + c] = t;
       }
-      if (tid == 0) { const double t = b[j]; b[j] = b[piv]; b[piv] = t; }
+      if (tid == 0) {
+        const double t = b[j]; b[j] = b[piv]; b[piv] = t;
+        lc[piv] = lc[j];
+      }
       __syncthreads();
     }
-    const double bj = b[j];
-    unsigned long long best = 0ull;
-    int bi = 0x7fffffff;
-    for (int i = j + 1 + wid; i < n; i += nw) {
-      const double l = A[i * lda + j] * inv;
+    const int w = n - j - 1;
+    if (w == 0) break;
+    if (tid < 32) {
+      // column j+1 of rows j+1.., then b, then the look-ahead of column j+1
+      const double ujn = A[j * lda + j + 1];
+      for (int i = j + 1 + lane; i < n; i += 32)
+        A[i * lda + j + 1] = A[i * lda + j + 1] - lc[i] * ujn;
+      const double bj = b[j];
+      for (int i = j + 1 + lane; i < n; i += 32) b[i] -= lc[i] * bj;
       __syncwarp();
-      if (lane == 0) { A[i * lda + j] = l; b[i] -= l * bj; }
-      for (int c = j + 1 + lane; c < n; c += 32) {
-        const double v = A[i * lda + c] - l * A[j * lda + c];
-        A[i * lda + c] = v;
-        if (c == j + 1) {
-          const unsigned long long k = abs_key(v);
-          if (bi == 0x7fffffff || k > best) { best = k; bi = i; }
+      pick(j + 1, ln);
+    } else if (w > 1) {
+      // columns j+2.. of rows j+1..: flat over warps 1..7
+      const int nt = (int)blockDim.x - 32, t = tid - 32;
+      const int ncol = w - 1;
+      const int rpp = nt / ncol;
+      const int rr = t / ncol, c = j + 2 + (t - (t / ncol) * ncol);
+      if (rr < rpp && rr < w) {
+        const double u = A[j * lda + c];
+        for (int r = rr; r < w; r += rpp) {
+          const int i = j + 1 + r;
+          A[i * lda + c] = A[i * lda + c] - lc[i] * u;
         }
       }
     }
-    // lane holding column j+1 is lane 0 of each warp (c = j+1+lane)
-    if (lane == 0) { cand_key[wid] = best; cand_row[wid] = bi; }
     __syncthreads();
+    double* tsw = lc; lc = ln; ln = tsw;
   }
-  for (int j = n - 1; j >= 0; --j) {
-    if (tid == 0) b[j] = b[j] / A[j * lda + j];
-    __syncthreads();
-    const double bj = b[j];
-    for (int i = tid; i < j; i += blockDim.x) b[i] -= A[i * lda + j] * bj;
-    __syncthreads();
+  __syncthreads();
+  // U x = b by one warp: lane l keeps b[l], b[l + 32], b[l + 64] in registers;
+  // x_j = b_j * (1 / u_jj) with the pivot reciprocal of the factorisation (as
+  // the multipliers), then every lane updates its rows above j.
+  if (tid < 32) {
+    constexpr int NB = (IPM_MAXS + 31) / 32;
+    double br[NB];
+#pragma unroll
+    for (int q = 0; q < NB; ++q) br[q] = (lane + 32 * q < n) ? b[lane + 32 * q] : 0.0;
+    for (int j = n - 1; j >= 0; --j) {
+      const int oq = j >> 5, ol = j & 31;
+      double bj = 0.0;
+#pragma unroll
+      for (int q = 0; q < NB; ++q) if (q == oq) bj = br[q];
+      bj = __shfl_sync(0xffffffffu, bj, ol) * dinv[j];
+#pragma unroll
+      for (int q = 0; q < NB; ++q) {
+        const int i = lane + 32 * q;
+        if (i == j) br[q] = bj;
+        else if (i < j) br[q] -= A[i * lda + j] * bj;
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < NB; ++q) if (lane + 32 * q < n) b[lane + 32 * q] = br[q];
   }
+  __syncthreads();
 }
 
 __global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ IpmArgs A) {
@@ -211,9 +256,14 @@ __global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ 
   double* coeff = dyn + s * s;  // s*s
   double* sm = A.smalls;
   if (tid == 0) {
-    int a = 0;
+    int a = 0, o = 0;
     for (int b = 0; b < k; ++b)
-      for (int c = 0; c <= b; ++c) { sh.bi[a] = b; sh.ci[a] = c; ++a; }
+      for (int c = 0; c <= b; ++c) {
+        sh.bi[a] = b; sh.ci[a] = c;
+        if (b != c) sh.cord[o++] = a;
+        ++a;
+      }
+    for (int b = 0; b < k; ++b) sh.cord[o++] = b * (b + 1) / 2 + b;
   }
   const int ngrid = A.ipm_grid;
   for (int j = tid; j < ngrid && j < 256; j += IPM_BLOCK) grid[j] = pow(0.9, (double)j);
@@ -359,18 +409,25 @@ __global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ 
     // steps once the system is ill-conditioned near the end of the IPM)
     const double lbc = (A.mode == 1) ? (ze / (k1 * ze + 1)) : 0.0;
     const double rden = 1.0 / den;
-    for (int a = wid; a < s; a += nw) {
-      const int b = sh.bi[a], c = sh.ci[a];
-      for (int a2 = lane; a2 < s; a2 += 32) {
-        double v = symkron(sh.T, sh.Si, k, b, c, sh.bi[a2], sh.ci[a2]);
-        if (A.mode == 0) {
-          v = Q11[a * s + a2] + v;
-          v -= (sh.q12[a] * (k1 * sh.q12[a2] + sh.sI[a2]) + sh.sI[a] * (sh.q12[a2] - k2 * sh.sI[a2])) * rden;
-        } else {
-          v += lbc * (sh.sI[a] * sh.sI[a2]);
-        }
-        coeff[a * s + a2] = v;
+    if (A.mode == 0) {
+      for (int a2 = tid; a2 < s; a2 += IPM_BLOCK) {
+        sh.u2[a2] = k1 * sh.q12[a2] + sh.sI[a2];
+        sh.w2[a2] = sh.q12[a2] - k2 * sh.sI[a2];
       }
+      __syncthreads();
+    }
+    // every entry of the s x s matrix, flat over the CTA; columns in cord order
+    // so that the off-diagonal / diagonal branch is uniform across most warps
+    for (int e = tid; e < s * s; e += IPM_BLOCK) {
+      const int a = e / s, a2 = sh.cord[e - a * s];
+      double v = symkron_sum(sh.T, sh.Si, k, sh.bi[a], sh.ci[a], sh.bi[a2], sh.ci[a2]);
+      if (A.mode == 0) {
+        v = Q11[a * s + a2] + v;
+        v -= (sh.q12[a] * sh.u2[a2] + sh.sI[a] * sh.w2[a2]) * rden;
+      } else {
+        v += lbc * (sh.sI[a] * sh.sI[a2]);
+      }
+      coeff[a * s + a2] = v;
     }
     if (tid == 0) {
       if (A.mode == 0) {
@@ -397,7 +454,7 @@ __global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ 
     }
     __syncthreads();
     if (tid == 0) { const long long c = clock64(); ph0 += c - tclk; tclk = c; }
-    ipm_lu_solve(coeff, s, sh.ord, s, sh.redv, sh.lcol, &s_piv, &s_ok);
+    ipm_lu_solve(coeff, s, sh.ord, s, sh.dinv, sh.lcol, &s_piv, &s_ok);
     if (tid == 0) { const long long c = clock64(); ph1 += c - tclk; tclk = c; }
     if (tid == 0 && !s_ok) atomicOr(A.status, ST_SMALL_DENSE_FAIL);
     // sh.ord now holds dsS
@@ -452,25 +509,40 @@ __global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ 
     __syncthreads();
     // ---- line search over the grid 0.9^j (solver/usbs.py:134-154): the largest
     // grid step keeping S (lanes 0-15) and T (lanes 16-31) positive definite is the
-    // first positive-definite grid index; batches of 16 with early exit ----
+    // first positive-definite grid index ----
     if (wid == 0) {
       const int half = lane >> 4, sub = lane & 15;
       const double* M = half ? sh.T : sh.S;
       const double* dM = half ? sh.dT : sh.dS;
-      int firstS = -1, firstT = -1;
-      for (int base = 0; base < ngrid && (firstS < 0 || firstT < 0); base += 16) {
-        const int j = base + sub;
-        const bool need = half ? (firstT < 0) : (firstS < 0);
-        bool pd = false;
-        if (need && j < ngrid) {
-          const double a = (j < 256) ? grid[j] : pow(0.9, (double)j);
-          pd = pd_test(M, dM, a, k);
-        }
+      // PD-ness of A + a dA is monotone along the grid (the PD steps form an
+      // interval containing 0), so after the first 16 points the first PD
+      // index is bracketed by testing every 16th point, then resolved inside
+      // the bracket: at most three rounds of 16 tests per matrix.
+      auto gstep = [&](int j) { return (j < 256) ? grid[j] : pow(0.9, (double)j); };
+      int first = -1;
+      {
+        const bool pd = (sub < ngrid) && pd_test(M, dM, gstep(sub), k);
         const unsigned bal = __ballot_sync(0xffffffffu, pd);
-        const unsigned bs = bal & 0xffffu, bt = bal >> 16;
-        if (firstS < 0 && bs) firstS = base + __ffs(bs) - 1;
-        if (firstT < 0 && bt) firstT = base + __ffs(bt) - 1;
+        const unsigned mine = half ? (bal >> 16) : (bal & 0xffffu);
+        if (mine) first = __ffs(mine) - 1;
       }
+      const bool need2 = (first < 0) && (ngrid > 16);
+      if (__any_sync(0xffffffffu, need2)) {
+        const int jc = min(31 + 16 * sub, ngrid - 1);
+        const bool pd = need2 && (16 + 16 * sub < ngrid) && pd_test(M, dM, gstep(jc), k);
+        const unsigned bal = __ballot_sync(0xffffffffu, pd);
+        const unsigned mine = half ? (bal >> 16) : (bal & 0xffffu);
+        const int q = mine ? (__ffs(mine) - 1) : -1;
+        const bool need3 = need2 && q >= 0;
+        const int j3 = 16 + 16 * (q < 0 ? 0 : q) + sub;
+        const int jq = min(31 + 16 * (q < 0 ? 0 : q), ngrid - 1);
+        const bool pd3 = need3 && j3 <= jq && pd_test(M, dM, gstep(j3), k);
+        const unsigned bal3 = __ballot_sync(0xffffffffu, pd3);
+        const unsigned mine3 = half ? (bal3 >> 16) : (bal3 & 0xffffu);
+        if (need3 && mine3) first = 16 + 16 * q + __ffs(mine3) - 1;
+      }
+      const int firstS = __shfl_sync(0xffffffffu, first, 0);
+      const int firstT = __shfl_sync(0xffffffffu, first, 16);
       if (lane == 0) {
         const double cS = (firstS < 0) ? 0.0 : (firstS < 256 ? grid[firstS] : pow(0.9, (double)firstS));
         const double cT = (firstT < 0) ? 0.0 : (firstT < 256 ? grid[firstT] : pow(0.9, (double)firstT));
