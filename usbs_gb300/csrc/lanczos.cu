@@ -143,6 +143,45 @@ __device__ __forceinline__ void reduce_part(const double* part_pass, int R, int 
   __syncthreads();
 }
 
+// SpMV of one 256-row tile, L lanes per row: sh.u.st.ys[r] = (Op x)[base + r].
+// Groups of up to 4 passes issue their rowptr loads, then their first col/val
+// loads, before any result is used: two dependent L2 round trips per group
+// instead of two per pass.
+template <typename VT, int L>
+__device__ __forceinline__ void spmv_tile(const TeamDesc<VT>& P, LzShared<VT>& sh, int base,
+                                          const VT* xsrc, const VT* xs, bool use_xs) {
+  typedef typename Acc<VT>::type AT;
+  constexpr int GPP = LZ_BLOCK / L;
+  constexpr int CH = L < 4 ? L : 4;          // passes whose loads are issued together
+  const int tid = threadIdx.x, g = tid / L, lig = tid - (tid / L) * L;
+#pragma unroll 1
+  for (int q0 = 0; q0 < L; q0 += CH) {
+    int pb[CH], pe[CH];
+#pragma unroll
+    for (int q = 0; q < CH; ++q) {
+      const int row = base + (q0 + q) * GPP + g;
+      pb[q] = 0; pe[q] = 0;
+      if (row < P.n) { pb[q] = P.rowptr[row] + lig; pe[q] = P.rowptr[row + 1]; }
+    }
+    int c0[CH];
+    VT v0[CH];
+#pragma unroll
+    for (int q = 0; q < CH; ++q) {
+      c0[q] = 0; v0[q] = (VT)0;
+      if (pb[q] < pe[q]) { c0[q] = P.col[pb[q]]; v0[q] = P.val[pb[q]]; }
+    }
+#pragma unroll
+    for (int q = 0; q < CH; ++q) {
+      AT s = (AT)v0[q] * (AT)(use_xs ? xs[c0[q]] : __ldcg(xsrc + c0[q]));
+      for (int p = pb[q] + L; p < pe[q]; p += L)
+        s += (AT)P.val[p] * (AT)(use_xs ? xs[P.col[p]] : __ldcg(xsrc + P.col[p]));
+#pragma unroll
+      for (int o = L >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lig == 0) sh.u.st.ys[(q0 + q) * GPP + g] = (double)s;
+    }
+  }
+}
+
 // Phase A: y = Op (xsrc * xscale) for own rows -> vout, acc[c] = Q[:, c] . y (c <= i).
 // If wq, also stores Q[:, i] = xsrc * xscale for own rows.
 template <typename VT>
@@ -160,27 +199,32 @@ __device__ void phase_spmv(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0, int 
   VT* xs = (VT*)lz_dyn;
   const bool use_xs = P.xsmem != 0;
   if (use_xs) {
-    for (int j = tid; j < P.n; j += LZ_BLOCK) xs[j] = __ldcg(xsrc + j);
+    // 16-byte loads, several in flight per thread (xsrc is a 256-byte aligned
+    // vector buffer or a column of Q with ld a multiple of 32)
+    constexpr int VE = 16 / (int)sizeof(VT);
+    const int n16 = P.n / VE;
+    const uint4* src = (const uint4*)xsrc;
+    uint4* dst = (uint4*)xs;
+    int j = tid;
+    for (; j + 3 * LZ_BLOCK < n16; j += 4 * LZ_BLOCK) {
+      const uint4 a = __ldcg(src + j), b = __ldcg(src + j + LZ_BLOCK),
+                  c = __ldcg(src + j + 2 * LZ_BLOCK), d = __ldcg(src + j + 3 * LZ_BLOCK);
+      dst[j] = a; dst[j + LZ_BLOCK] = b; dst[j + 2 * LZ_BLOCK] = c; dst[j + 3 * LZ_BLOCK] = d;
+    }
+    for (; j < n16; j += LZ_BLOCK) dst[j] = __ldcg(src + j);
+    for (int r = n16 * VE + tid; r < P.n; r += LZ_BLOCK) xs[r] = __ldcg(xsrc + r);
     __syncthreads();
   }
+  (void)gpp; (void)g; (void)lig;
   for (int tile = t0; tile < t1; ++tile) {
     const int base = tile * LZ_BLOCK;
-    for (int pass = 0; pass < L; ++pass) {
-      const int rl = pass * gpp + g;
-      const int row = base + rl;
-      AT s = (AT)0;
-      if (row < P.n) {
-        const int pe = P.rowptr[row + 1];
-        if (use_xs) {
-          for (int p = P.rowptr[row] + lig; p < pe; p += L)
-            s += (AT)P.val[p] * (AT)xs[P.col[p]];
-        } else {
-          for (int p = P.rowptr[row] + lig; p < pe; p += L)
-            s += (AT)P.val[p] * (AT)__ldcg(xsrc + P.col[p]);
-        }
-      }
-      for (int o = L >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lig == 0) sh.u.st.ys[rl] = (double)s;
+    switch (L) {
+      case 1: spmv_tile<VT, 1>(P, sh, base, xsrc, xs, use_xs); break;
+      case 2: spmv_tile<VT, 2>(P, sh, base, xsrc, xs, use_xs); break;
+      case 4: spmv_tile<VT, 4>(P, sh, base, xsrc, xs, use_xs); break;
+      case 8: spmv_tile<VT, 8>(P, sh, base, xsrc, xs, use_xs); break;
+      case 16: spmv_tile<VT, 16>(P, sh, base, xsrc, xs, use_xs); break;
+      default: spmv_tile<VT, 32>(P, sh, base, xsrc, xs, use_xs); break;
     }
     __syncthreads();
     const int row = base + tid;
@@ -285,8 +329,12 @@ __device__ void phase_update_norm(const TeamDesc<VT>& P, LzShared<VT>& sh, int t
 // CTA 0 of a team: projected eigenproblem and thick-restart selection
 // (solver/lanczos.py:128-168, 202-221).  k = number of saved vectors of the
 // finished cycle, beta_last = beta[m-1].
-template <typename VT>
-__device__ void restart_select(const TeamDesc<VT>& P, LzShared<VT>& sh, int k) {
+// LOCAL_YS: every CTA of a cluster runs this redundantly (identical inputs give
+// identical results) and keeps the saved Ritz vectors in sh.u.Ys; only the CTA
+// with write_out set stores alpha/beta/ctl.  Otherwise (team kernel) the Ritz
+// vectors go through P.Ybuf.
+template <bool LOCAL_YS, typename VT, typename D>
+__device__ void restart_select(const D& P, LzShared<VT>& sh, int k, bool write_out = true) {
   const int m = P.m, tid = threadIdx.x;
   double* T = sh.u.rs.T;
   double* X = sh.u.rs.X;
@@ -375,9 +423,17 @@ __device__ void restart_select(const TeamDesc<VT>& P, LzShared<VT>& sh, int k) {
   __syncthreads();
   const int kn = sh.k_next;
   const double bl = sh.beta[m - 1];
-  for (int e = tid; e < m * m; e += LZ_BLOCK) {
-    const int j = e / m, c = e - j * m;
-    P.Ybuf[j * m + c] = Z[j * MP1 + sh.order[c]];
+  if constexpr (LOCAL_YS) {
+    // sh.u.Ys overlays sh.u.rs.T only (T is no longer needed; Z lives in X)
+    for (int e = tid; e < m * MAXM; e += LZ_BLOCK) {
+      const int j = e / MAXM, c = e - j * MAXM;
+      sh.u.Ys[e] = (c < kn) ? (VT)Z[j * MP1 + sh.order[c]] : (VT)0;
+    }
+  } else {
+    for (int e = tid; e < m * m; e += LZ_BLOCK) {
+      const int j = e / m, c = e - j * m;
+      P.Ybuf[j * m + c] = Z[j * MP1 + sh.order[c]];
+    }
   }
   __syncthreads();
   if (tid < m) {
@@ -386,10 +442,12 @@ __device__ void restart_select(const TeamDesc<VT>& P, LzShared<VT>& sh, int k) {
     const double b = (c < kn) ? bl * Z[(m - 1) * MP1 + sh.order[c]] : 0.0;
     sh.alpha[c] = a;
     sh.beta[c] = b;
-    P.alpha[c] = a;
-    P.beta[c] = b;
+    if (write_out) {
+      P.alpha[c] = a;
+      P.beta[c] = b;
+    }
   }
-  if (tid == 0) {
+  if (tid == 0 && write_out) {
     P.ctl[0] = kn;
     P.ctl[1] = sh.nconv;
   }
@@ -519,7 +577,7 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
     __syncthreads();
     if (rank == 0) {
       const long long c0 = clock64();
-      restart_select(P, sh, k);
+      restart_select<false>(P, sh, k);
       clk_restart += clock64() - c0;
     }
     if (!bar.sync()) return;
@@ -568,6 +626,445 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
     P.ctl[14] = sum_kn;
     if (restart == 0) P.ctl[0] = 0;
   }
+}
+
+// ---------------------------------------------------------------- cluster path
+// A problem of at most CL_MAX_CTAS x rc rows runs as one thread-block cluster.
+// CTA r of the cluster owns rows [r rc, (r+1) rc) and keeps, for the whole
+// eigsh call, its rows of the basis Q (column-major, stride rc), the two work
+// vectors and, when it fits, its slice of the operator (CSR with the column
+// pre-split into owner CTA and local row) in shared memory.  The SpMV gathers
+// x straight from the owner CTAs' shared memory (distributed shared memory,
+// mapa + ld.shared::cluster); each phase's per-CTA partial sums are written to
+// the CTA's own shared memory and, after a hardware cluster barrier, summed by
+// every CTA over the cluster in the same fixed order, so all CTAs hold
+// bit-identical coefficients and take identical branches.  The restart's
+// projected eigenproblem is solved redundantly by every CTA (identical inputs,
+// identical results), which needs no broadcast.  A cluster is co-scheduled by
+// the hardware, so there is no software barrier and no spin-wait.
+constexpr int CL_MAX_CTAS = 16;
+
+template <typename VT>
+struct ClusterDesc {
+  int n, ld, m, num_desired, max_restarts, lanes, rc, csr_cap;
+  long long nnz;
+  double tol;
+  const int* rowptr;
+  const int* col;
+  const VT* val;
+  VT* Q;
+  double* alpha;
+  double* beta;
+  int* ctl;
+  int* status;
+};
+
+template <typename VT>
+struct ClusterBatch {
+  int count, csize;
+  ClusterDesc<VT> t[MAX_TEAMS];
+};
+
+__device__ __forceinline__ unsigned cl_rank() {
+  unsigned r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ void cl_sync() {
+  asm volatile("barrier.cluster.arrive.release.aligned;\n\t"
+               "barrier.cluster.wait.acquire.aligned;" ::: "memory");
+}
+__device__ __forceinline__ uint32_t cl_map(const void* p, unsigned rank) {
+  uint32_t a = (uint32_t)__cvta_generic_to_shared(p), r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ float cl_ld(uint32_t a, float) {
+  float v;
+  asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ double cl_ld(uint32_t a, double) {
+  double v;
+  asm volatile("ld.shared::cluster.f64 %0, [%1];" : "=d"(v) : "r"(a) : "memory");
+  return v;
+}
+
+// per-CTA shared-memory layout of the cluster kernel (byte offsets)
+struct ClLayout {
+  size_t q, vb, part, rp, cg, val, total;
+};
+__host__ __device__ inline size_t cl_al(size_t b) { return (b + 15) & ~(size_t)15; }
+template <typename VT>
+__host__ __device__ inline ClLayout cl_layout(int m, int rc, int csr_cap) {
+  ClLayout L;
+  L.q = 0;
+  L.vb = L.q + cl_al((size_t)(m + 1) * rc * sizeof(VT));
+  L.part = L.vb + cl_al((size_t)2 * rc * sizeof(VT));
+  L.rp = L.part + cl_al((size_t)3 * MP1 * sizeof(double));
+  L.cg = L.rp + cl_al((size_t)(rc + 1) * sizeof(int));
+  L.val = L.cg + cl_al((size_t)csr_cap * sizeof(int));
+  L.total = L.val + cl_al((size_t)csr_cap * sizeof(VT));
+  return L;
+}
+
+// h[c] = sum over the cluster's CTAs r = 0..C-1 of part_r[c], c < nv, summed
+// as a fixed pairwise tree (FP64 adds are ~64 cycles dependent on this part).
+template <typename VT>
+__device__ __forceinline__ void cl_reduce(const double* part, int C, int nv, LzShared<VT>& sh) {
+  const int lane = threadIdx.x & 31;
+  if (threadIdx.x < 32) {
+    for (int c = lane; c < nv; c += 32) {
+      double v[CL_MAX_CTAS];
+#pragma unroll
+      for (int r = 0; r < CL_MAX_CTAS; ++r) v[r] = (r < C) ? cl_ld(cl_map(part + c, r), 0.0) : 0.0;
+#pragma unroll
+      for (int h = CL_MAX_CTAS / 2; h >= 1; h >>= 1)
+#pragma unroll
+        for (int r = 0; r < h; ++r) v[r] = v[r] + v[r + h];
+      sh.h[c] = v[0];
+    }
+  }
+  __syncthreads();
+}
+
+template <typename VT>
+struct ClCtx {
+  const ClusterDesc<VT>* P;
+  int rank, C, r0, rows;
+  bool staged;          // CSR slice in shared memory
+  int p0;               // first entry of the slice
+  VT* Qs;               // (m+1) x rc
+  VT* vb;               // 2 x rc
+  double* part;         // 3 x MP1
+  int* rp;              // rows+1, relative to p0
+  int* cg;              // (owner << 24) | local row
+  VT* vs;
+};
+
+// Phase A: y = Op (x * xscale) for own rows -> vout, partial Q[:, c] . y (c <= i).
+// x is column `xcol` of the cluster's vectors: xq selects Qs (else vb); the
+// gathers read the owner CTA's copy.  If wq, Qs[:, i] = x * xscale (own rows).
+template <typename VT, int L>
+__device__ void cl_phase_spmv(const ClCtx<VT>& X, LzShared<VT>& sh, int i, const VT* xbase,
+                              VT xscale, bool wq, VT* vout, double* part_out) {
+  typedef typename Acc<VT>::type AT;
+  const ClusterDesc<VT>& P = *X.P;
+  const int tid = threadIdx.x, rc = P.rc;
+  constexpr int GPP = LZ_BLOCK / L;
+  const int g = tid / L, lig = tid - (tid / L) * L;
+  AT acc[MP1];
+#pragma unroll
+  for (int c = 0; c < MP1; ++c) acc[c] = (AT)0;
+  for (int base = 0; base < X.rows; base += LZ_BLOCK) {
+    // SpMV of rows base..base+255 (L lanes per row) into sh.u.st.ys
+#pragma unroll 1
+    for (int q = 0; q < L; ++q) {
+      const int lr = base + q * GPP + g;
+      AT sacc = (AT)0;
+      if (lr < X.rows) {
+        if (X.staged) {
+          const int pe = X.rp[lr + 1];
+          for (int p = X.rp[lr] + lig; p < pe; p += L) {
+            const int w = X.cg[p];
+            sacc += (AT)X.vs[p] * (AT)cl_ld(cl_map(xbase + (w & 0xffffff), (unsigned)w >> 24), (VT)0);
+          }
+        } else {
+          const int row = X.r0 + lr;
+          const int pe = P.rowptr[row + 1];
+          for (int p = P.rowptr[row] + lig; p < pe; p += L) {
+            const int gc = P.col[p];
+            const int o = gc / rc;
+            sacc += (AT)P.val[p] * (AT)cl_ld(cl_map(xbase + (gc - o * rc), (unsigned)o), (VT)0);
+          }
+        }
+      }
+#pragma unroll
+      for (int o = L >> 1; o > 0; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
+      if (lig == 0) sh.u.st.ys[q * GPP + g] = (double)sacc;
+    }
+    __syncthreads();
+    const int lr = base + tid;
+    if (lr < X.rows) {
+      const VT y = (VT)sh.u.st.ys[tid] * xscale;
+      vout[lr] = y;
+      VT xn = (VT)0;
+      if (wq) {
+        xn = xbase[lr] * xscale;
+        X.Qs[(size_t)i * rc + lr] = xn;
+      }
+#pragma unroll
+      for (int c = 0; c < MP1; ++c) {
+        if (c <= i) {
+          const VT qc = (wq && c == i) ? xn : X.Qs[(size_t)c * rc + lr];
+          acc[c] += (AT)qc * (AT)y;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  block_reduce_cols(acc, i + 1, sh, part_out, 1);
+}
+
+template <typename VT>
+__device__ void cl_phase_random(const ClCtx<VT>& X, LzShared<VT>& sh, int nv, uint64_t key,
+                                VT* buf, double* part_out) {
+  typedef typename Acc<VT>::type AT;
+  const int rc = X.P->rc;
+  AT acc[MP1];
+#pragma unroll
+  for (int c = 0; c < MP1; ++c) acc[c] = (AT)0;
+  for (int lr = threadIdx.x; lr < X.rows; lr += LZ_BLOCK) {
+    const VT r = (VT)hash_normal(key, (uint64_t)(X.r0 + lr));
+    buf[lr] = r;
+#pragma unroll
+    for (int c = 0; c < MP1; ++c)
+      if (c < nv) acc[c] += (AT)X.Qs[(size_t)c * rc + lr] * (AT)r;
+  }
+  block_reduce_cols(acc, nv, sh, part_out, 1);
+}
+
+template <typename VT>
+__device__ void cl_phase_update_dot(const ClCtx<VT>& X, LzShared<VT>& sh, int nv, VT* buf,
+                                    double* part_out) {
+  typedef typename Acc<VT>::type AT;
+  const int rc = X.P->rc;
+  AT acc[MP1];
+#pragma unroll
+  for (int c = 0; c < MP1; ++c) acc[c] = (AT)0;
+  for (int lr = threadIdx.x; lr < X.rows; lr += LZ_BLOCK) {
+    VT qr[MP1];
+    VT s = (VT)0;
+#pragma unroll
+    for (int c = 0; c < MP1; ++c) {
+      if (c < nv) {
+        qr[c] = X.Qs[(size_t)c * rc + lr];
+        s += qr[c] * (VT)sh.h[c];
+      }
+    }
+    const VT q1 = buf[lr] - s;
+    buf[lr] = q1;
+#pragma unroll
+    for (int c = 0; c < MP1; ++c)
+      if (c < nv) acc[c] += (AT)qr[c] * (AT)q1;
+  }
+  block_reduce_cols(acc, nv, sh, part_out, 1);
+}
+
+template <typename VT>
+__device__ void cl_phase_update_norm(const ClCtx<VT>& X, LzShared<VT>& sh, int nv, VT* buf,
+                                     double* part_out) {
+  typedef typename Acc<VT>::type AT;
+  const int rc = X.P->rc;
+  AT nrm = (AT)0;
+  for (int lr = threadIdx.x; lr < X.rows; lr += LZ_BLOCK) {
+    VT s = (VT)0;
+#pragma unroll
+    for (int c = 0; c < MP1; ++c)
+      if (c < nv) s += X.Qs[(size_t)c * rc + lr] * (VT)sh.h[c];
+    const VT q2 = buf[lr] - s;
+    buf[lr] = q2;
+    nrm += (AT)q2 * (AT)q2;
+  }
+  AT one[MP1];
+  one[0] = nrm;
+  block_reduce_cols(one, 1, sh, part_out, 1);
+}
+
+template <typename VT>
+__device__ void cl_spmv_dispatch(const ClCtx<VT>& X, LzShared<VT>& sh, int i, const VT* xbase,
+                                 VT xscale, bool wq, VT* vout, double* part_out) {
+  switch (X.P->lanes) {
+    case 1: cl_phase_spmv<VT, 1>(X, sh, i, xbase, xscale, wq, vout, part_out); break;
+    case 2: cl_phase_spmv<VT, 2>(X, sh, i, xbase, xscale, wq, vout, part_out); break;
+    case 4: cl_phase_spmv<VT, 4>(X, sh, i, xbase, xscale, wq, vout, part_out); break;
+    case 8: cl_phase_spmv<VT, 8>(X, sh, i, xbase, xscale, wq, vout, part_out); break;
+    case 16: cl_phase_spmv<VT, 16>(X, sh, i, xbase, xscale, wq, vout, part_out); break;
+    default: cl_phase_spmv<VT, 32>(X, sh, i, xbase, xscale, wq, vout, part_out); break;
+  }
+}
+
+template <typename VT>
+__global__ void __launch_bounds__(LZ_BLOCK)
+lanczos_cluster_kernel(const __grid_constant__ ClusterBatch<VT> batch) {
+  __shared__ LzShared<VT> sh;
+  extern __shared__ __align__(16) unsigned char cl_dyn[];
+  const int C = batch.csize;
+  const ClusterDesc<VT>& P = batch.t[blockIdx.x / C];
+  const int rank = (int)cl_rank();
+  const int tid = threadIdx.x;
+  const int n = P.n, m = P.m, rc = P.rc;
+  const size_t ld = (size_t)P.ld;
+  const ClLayout Lo = cl_layout<VT>(m, rc, P.csr_cap);
+  ClCtx<VT> X;
+  X.P = &P;
+  X.rank = rank;
+  X.C = C;
+  X.r0 = rank * rc;
+  X.rows = max(0, min(rc, n - X.r0));
+  X.Qs = (VT*)(cl_dyn + Lo.q);
+  X.vb = (VT*)(cl_dyn + Lo.vb);
+  X.part = (double*)(cl_dyn + Lo.part);
+  X.rp = (int*)(cl_dyn + Lo.rp);
+  X.cg = (int*)(cl_dyn + Lo.cg);
+  X.vs = (VT*)(cl_dyn + Lo.val);
+  double* part0 = X.part;
+  double* part1 = X.part + MP1;
+  double* part2 = X.part + 2 * MP1;
+  // stage Q[:, 0] (the start vector) and, if it fits, the operator slice
+  for (int lr = tid; lr < X.rows; lr += LZ_BLOCK) X.Qs[lr] = P.Q[X.r0 + lr];
+  X.p0 = (X.rows > 0) ? P.rowptr[X.r0] : 0;
+  const int p1 = (X.rows > 0) ? P.rowptr[X.r0 + X.rows] : 0;
+  X.staged = (p1 - X.p0) <= P.csr_cap;
+  if (X.staged) {
+    for (int lr = tid; lr <= X.rows; lr += LZ_BLOCK) X.rp[lr] = P.rowptr[X.r0 + lr] - X.p0;
+    for (int p = X.p0 + tid; p < p1; p += LZ_BLOCK) {
+      const int gc = P.col[p];
+      const int o = gc / rc;
+      X.cg[p - X.p0] = (o << 24) | (gc - o * rc);
+      X.vs[p - X.p0] = P.val[p];
+    }
+  }
+  int k = 0, nconv = 0, restart = 0, breakdowns = 0, steps = 0, sum_nv = 0, sum_kn = 0;
+  long long clk_start = clock64(), clk_restart = 0;
+  long long tp[5] = {0, 0, 0, 0, 0}, tmark = clock64();
+  const bool timing = (rank == 0 && tid == 0);
+  if (tid < MAXM) { sh.alpha[tid] = 0.0; sh.beta[tid] = 0.0; }
+  __syncthreads();
+  cl_sync();
+  int prev = 0;
+  VT invb = (VT)1;
+  while (nconv < P.num_desired && restart < P.max_restarts) {
+    int cur = 0;
+    for (int i = k; i < m; ++i) {
+      const VT* xbase;
+      bool wq;
+      if (i == k) {
+        xbase = X.Qs + (size_t)k * rc;
+        invb = (VT)1;
+        wq = false;
+      } else {
+        cl_reduce(part2, C, 1, sh);
+        const double b = sqrt(sh.h[0]);
+        if (tid == 0) sh.beta[i - 1] = b;
+        if (b < 1e-15) {
+          // Krylov space exhausted: random vector orthogonalised twice
+          // against Q[:, :i] (solver/lanczos.py:107-117)
+          ++breakdowns;
+          VT* buf = X.vb + (size_t)prev * rc;
+          cl_phase_random(X, sh, i, (uint64_t)i, buf, part0);
+          cl_sync();
+          cl_reduce(part0, C, i, sh);
+          cl_phase_update_dot(X, sh, i, buf, part1);
+          cl_sync();
+          cl_reduce(part1, C, i, sh);
+          cl_phase_update_norm(X, sh, i, buf, part2);
+          cl_sync();
+          cl_reduce(part2, C, 1, sh);
+          invb = (VT)(1.0 / sqrt(sh.h[0]));
+        } else {
+          invb = (VT)(1.0 / b);
+        }
+        xbase = X.vb + (size_t)prev * rc;
+        wq = true;
+      }
+      VT* vout = X.vb + (size_t)cur * rc;
+      if (timing) { const long long c = clock64(); tp[1] += c - tmark; tmark = c; }
+      cl_spmv_dispatch(X, sh, i, xbase, invb, wq, vout, part0);
+      if (timing) { const long long c = clock64(); tp[2] += c - tmark; tmark = c; }
+      cl_sync();
+      if (timing) { const long long c = clock64(); tp[0] += c - tmark; tmark = c; }
+      cl_reduce(part0, C, i + 1, sh);
+      if (timing) { const long long c = clock64(); tp[1] += c - tmark; tmark = c; }
+      const double h1i = sh.h[i];
+      cl_phase_update_dot(X, sh, i + 1, vout, part1);
+      if (timing) { const long long c = clock64(); tp[3] += c - tmark; tmark = c; }
+      cl_sync();
+      if (timing) { const long long c = clock64(); tp[0] += c - tmark; tmark = c; }
+      cl_reduce(part1, C, i + 1, sh);
+      if (timing) { const long long c = clock64(); tp[1] += c - tmark; tmark = c; }
+      if (tid == 0) sh.alpha[i] = h1i + sh.h[i];
+      cl_phase_update_norm(X, sh, i + 1, vout, part2);
+      if (timing) { const long long c = clock64(); tp[4] += c - tmark; tmark = c; }
+      cl_sync();
+      if (timing) { const long long c = clock64(); tp[0] += c - tmark; tmark = c; }
+      prev = cur;
+      cur ^= 1;
+      ++steps;
+      sum_nv += i + 1;
+    }
+    // ---- restart ----
+    const bool stepped = (k < m);
+    if (stepped) {
+      cl_reduce(part2, C, 1, sh);
+      const double b = sqrt(sh.h[0]);
+      if (tid == 0) sh.beta[m - 1] = b;
+      if (b < 1e-15) {
+        ++breakdowns;
+        VT* buf = X.vb + (size_t)prev * rc;
+        cl_phase_random(X, sh, m, (uint64_t)m, buf, part0);
+        cl_sync();
+        cl_reduce(part0, C, m, sh);
+        cl_phase_update_dot(X, sh, m, buf, part1);
+        cl_sync();
+        cl_reduce(part1, C, m, sh);
+        cl_phase_update_norm(X, sh, m, buf, part2);
+        cl_sync();
+        cl_reduce(part2, C, 1, sh);
+        invb = (VT)(1.0 / sqrt(sh.h[0]));
+      } else {
+        invb = (VT)(1.0 / b);
+      }
+    }
+    __syncthreads();
+    const long long c0 = clock64();
+    restart_select<true>(P, sh, k, /*write_out=*/rank == 0);
+    if (timing) clk_restart += clock64() - c0;
+    const int kn = sh.k_next;
+    nconv = sh.nconv;
+    const VT* last = stepped ? (X.vb + (size_t)prev * rc) : (X.Qs + (size_t)m * rc);
+    const VT lscale = stepped ? invb : (VT)1;
+    for (int lr = tid; lr < X.rows; lr += LZ_BLOCK) {
+      VT qr[MAXM];
+#pragma unroll
+      for (int j = 0; j < MAXM; ++j) qr[j] = (j < m) ? X.Qs[(size_t)j * rc + lr] : (VT)0;
+      const VT xl = last[lr] * lscale;
+      for (int c = 0; c < kn; ++c) {
+        if (c >= m) break;
+        VT s = (VT)0;
+#pragma unroll
+        for (int j = 0; j < MAXM; ++j)
+          if (j < m) s += qr[j] * sh.u.Ys[j * MAXM + c];
+        X.Qs[(size_t)c * rc + lr] = s;
+      }
+      X.Qs[(size_t)kn * rc + lr] = xl;
+      if (kn != m) X.Qs[(size_t)m * rc + lr] = xl;
+    }
+    k = kn;
+    sum_kn += kn;
+    ++restart;
+    __syncthreads();
+    cl_sync();   // rotated rows visible to the next cycle's gathers
+    if (timing) tmark = clock64();
+  }
+  // the basis back to global memory (own rows; untouched if no cycle ran)
+  if (restart > 0) {
+    for (int c = 0; c <= m; ++c)
+      for (int lr = tid; lr < X.rows; lr += LZ_BLOCK)
+        P.Q[(size_t)c * ld + X.r0 + lr] = X.Qs[(size_t)c * rc + lr];
+  }
+  if (rank == 0 && tid == 0) {
+    P.ctl[2] = restart;
+    P.ctl[3] = breakdowns;
+    P.ctl[4] = steps;
+    P.ctl[6] = (int)(clk_restart >> 10);
+    P.ctl[7] = (int)((clock64() - clk_start) >> 10);
+    for (int j = 0; j < 5; ++j) P.ctl[8 + j] = (int)(tp[j] >> 10);
+    P.ctl[13] = sum_nv;
+    P.ctl[14] = sum_kn;
+    if (restart == 0) P.ctl[0] = 0;
+  }
+  cl_sync();   // no CTA leaves while a peer may still read its shared memory
 }
 
 // ---------------------------------------------------------------- host side
@@ -691,10 +1188,103 @@ static int run_typed(const DeviceInfo& di, const LanczosProblem* probs, int coun
   return 0;
 }
 
+// Cluster path: every problem of the launch as one cluster of `csize` CTAs.
+// Returns 1 if the problems do not fit (the caller then runs the team kernel),
+// 0 on success, negative on a launch error.
+template <typename VT>
+static int run_cluster(const LanczosProblem* probs, int count, cudaStream_t stream) {
+  static const int enabled = [] {
+    const char* e = getenv("USBS_LANCZOS_CLUSTER");   // 0 forces the team kernel
+    return e ? atoi(e) : 1;
+  }();
+  if (!enabled || count < 1 || count > MAX_TEAMS) return 1;
+  constexpr size_t STATIC_SMEM = sizeof(LzShared<VT>);
+  constexpr size_t BUDGET = 227 * 1024 - STATIC_SMEM - 1024;
+  // rows per CTA: FP64 arithmetic is slow on this part, so FP64 problems are
+  // spread thinner
+  const int target = (sizeof(VT) == 8) ? 128 : 640;
+  int csize = 1;
+  for (int i = 0; i < count; ++i) {
+    const int c = (probs[i].n + target - 1) / target;
+    csize = c > csize ? c : csize;
+  }
+  if (csize > CL_MAX_CTAS) return 1;
+  ClusterBatch<VT> batch;
+  batch.count = count;
+  size_t dyn = 0;
+  for (int i = 0; i < count; ++i) {
+    const LanczosProblem& p = probs[i];
+    if (p.m > MAXM || p.m < 1 || p.n < 1 || p.ld < p.n) return 1;
+    const int rc = (p.n + csize - 1) / csize;
+    const ClLayout base = cl_layout<VT>(p.m, rc, 0);
+    if (base.total > BUDGET) return 1;
+    // whatever is left holds the operator slice (else it is read from L2)
+    const int cap = (int)((BUDGET - base.total) / (sizeof(int) + sizeof(VT))) - 8;
+    ClusterDesc<VT>& t = batch.t[i];
+    t.n = p.n; t.ld = p.ld; t.m = p.m; t.num_desired = p.num_desired;
+    t.max_restarts = p.max_restarts; t.tol = p.tol; t.nnz = p.nnz;
+    t.lanes = lanczos_lanes(p.n, p.nnz);
+    t.rc = rc;
+    t.csr_cap = cap > 0 ? cap : 0;
+    t.rowptr = p.rowptr; t.col = p.col; t.val = (const VT*)p.val;
+    t.Q = (VT*)p.Q; t.alpha = p.alpha; t.beta = p.beta; t.ctl = p.ctl; t.status = p.status;
+    const size_t tot = cl_layout<VT>(p.m, rc, t.csr_cap).total;
+    dyn = tot > dyn ? tot : dyn;
+  }
+  batch.csize = csize;
+  static bool attr_set = false;
+  if (!attr_set) {
+    cudaFuncSetAttribute((const void*)lanczos_cluster_kernel<VT>,
+                         cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaFuncSetAttribute((const void*)lanczos_cluster_kernel<VT>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)BUDGET);
+    attr_set = true;
+  }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)(csize * count));
+  cfg.blockDim = dim3(LZ_BLOCK);
+  cfg.dynamicSmemBytes = dyn;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeClusterDimension;
+  attr[0].val.clusterDim.x = (unsigned)csize;
+  attr[0].val.clusterDim.y = 1;
+  attr[0].val.clusterDim.z = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  int nclusters = 0;
+  if (cudaOccupancyMaxActiveClusters(&nclusters, (const void*)lanczos_cluster_kernel<VT>, &cfg) !=
+          cudaSuccess || nclusters < 1) {
+    cudaGetLastError();
+    return 1;
+  }
+  for (int i = 0; i < count; ++i) {
+    if (cudaMemsetAsync(probs[i].ctl, 0, 16 * sizeof(int), stream) != cudaSuccess) {
+      set_error("lanczos: memset failed");
+      return -4;
+    }
+  }
+  cudaError_t e = cudaLaunchKernelEx(&cfg, lanczos_cluster_kernel<VT>, batch);
+  if (e != cudaSuccess) {
+    set_error("lanczos: cluster launch (%d x %d CTAs) failed: %s", count, csize,
+              cudaGetErrorString(e));
+    return -5;
+  }
+  return 0;
+}
+
 int lanczos_run(const DeviceInfo& di, const LanczosProblem* probs, int count, int prec,
                 cudaStream_t stream) {
-  if (prec == 64) return run_typed<double>(di, probs, count, stream);
-  if (prec == 32) return run_typed<float>(di, probs, count, stream);
+  if (prec == 64) {
+    const int rc = run_cluster<double>(probs, count, stream);
+    if (rc <= 0) return rc;
+    return run_typed<double>(di, probs, count, stream);
+  }
+  if (prec == 32) {
+    const int rc = run_cluster<float>(probs, count, stream);
+    if (rc <= 0) return rc;
+    return run_typed<float>(di, probs, count, stream);
+  }
   set_error("lanczos: precision must be 32 or 64");
   return -2;
 }
