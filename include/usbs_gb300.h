@@ -11,8 +11,9 @@
  *    Numerical/device conditions are reported through the `info`/`status`
  *    words the caller passes (device memory, read after synchronising).
  *  - `precision` selects the storage/arithmetic type of the n-sized vectors:
- *    64 = FP64 throughout (the parity path), 32 = FP32 vectors and dot products
- *    with FP64 team reductions and FP64 projected eigensolve.
+ *    64 = FP64 throughout (the parity path; the projected eigensolve is FP32
+ *    Jacobi refined to FP64 by two Ogita-Aishima steps), 32 = FP32 vectors,
+ *    dot products and projected eigensolve, with FP64 reductions over CTAs.
  *  - Triples: the reference's constraint tensor A is a list of (c, i, j, a)
  *    (A_indices rows and A_data, utils/maxcut_helpers.py:26-33,
  *    utils/qap_helpers.py:175-318).  The device keeps them sorted by
@@ -95,8 +96,11 @@ size_t usbs_eigsh_workspace_bytes(int n, long long nnz, int inner_iterations, in
  *         [6] kilo-cycles in the restarts, [7] kilo-cycles in total,
  *         [8..12] kilo-cycles of CTA 0 in barrier waits, team reductions and
  *         the three step phases, [13] sum over steps of the active basis
- *         columns, [14] sum over restarts of the saved vectors (for byte counts).
- * Runs as one cooperative kernel; the call is asynchronous. */
+ *         columns, [14] sum over restarts of the saved vectors (for byte counts),
+ *         [15] kilo-cycles of CTA 0 in the projected eigensolver.
+ * Runs as one kernel launch: one thread-block cluster when the problem's rows
+ * fit in the cluster's shared memory, else a cooperative team of CTAs.  The
+ * call is asynchronous. */
 int usbs_eigsh_smallest(int n, long long nnz, const int* rowptr, const int* col,
                         const double* c_val, double c_scale, const int* slot_ptr, const int* slot_tid,
                         const int* t_con, const double* t_a, const double* adjoint_left_vec,

@@ -136,12 +136,13 @@ class EigshInfo:
             self.status = (int(v) for v in raw[:6])
         self.restart_kcycles, self.total_kcycles = int(raw[6]), int(raw[7])
         self.phase_kcycles = [int(v) for v in raw[8:13]]
+        self.eig_kcycles = int(raw[15])
 
     def __repr__(self):
         return (f"EigshInfo(restarts={self.restarts}, converged={self.num_converged}, "
                 f"matvecs={self.matvecs}, breakdowns={self.breakdowns}, status={self.status}, "
                 f"restart_kcycles={self.restart_kcycles}, total_kcycles={self.total_kcycles}, "
-                f"bar/red/A/B/C={self.phase_kcycles})")
+                f"eig_kcycles={self.eig_kcycles}, bar/red/A/B/C={self.phase_kcycles})")
 
 
 def eigsh_smallest(n, C, A_data, A_indices, adjoint_left_vec, q0, num_desired, inner_iterations,

@@ -74,6 +74,7 @@ struct LzShared {
     VT Ys[MAXM * MAXM];          // saved Ritz vectors, every CTA, after the restart barrier
   } u;
   double h[MP1];
+  VT hv[MP1];                    // h in the vector type, converted once per reduction
   double alpha[MAXM];
   double beta[MAXM];
   double ritz[MAXM];
@@ -82,6 +83,7 @@ struct LzShared {
   int pidx[MAXM];
   int order[MAXM];
   int k_next, nconv;
+  long long eig_cycles;          // cycles in the projected eigensolver (thread 0)
 };
 
 // acc[c] (c < nv) summed over the CTA, written to out[c * R] (column-major
@@ -122,7 +124,7 @@ __device__ __forceinline__ void reduce_part(const double* part_pass, int R, int 
       double a = 0.0;
       for (int r = lane; r < R; r += 32) a += __ldcg(part_pass + r);
       a = warp_sum(a);
-      if (lane == 0) sh.h[0] = a;
+      if (lane == 0) { sh.h[0] = a; sh.hv[0] = (VT)a; }
     } else {
       double acc[32];
 #pragma unroll
@@ -136,8 +138,8 @@ __device__ __forceinline__ void reduce_part(const double* part_pass, int R, int 
       }
       extra = warp_sum(extra);
       const double v = warp_reduce_scatter32(acc);
-      if (lane < nv) sh.h[lane] = v;
-      if (lane == 0 && nv > 32) sh.h[32] = extra;
+      if (lane < nv) { sh.h[lane] = v; sh.hv[lane] = (VT)v; }
+      if (lane == 0 && nv > 32) { sh.h[32] = extra; sh.hv[32] = (VT)extra; }
     }
   }
   __syncthreads();
@@ -289,7 +291,7 @@ __device__ void phase_update_dot(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0
       for (int c = 0; c < MP1; ++c) {
         if (c < nv) {
           qr[c] = P.Q[(size_t)c * ld + row];
-          s += qr[c] * (VT)sh.h[c];
+          s += qr[c] * sh.hv[c];
         }
       }
       const VT q1 = buf[row] - s;
@@ -315,7 +317,7 @@ __device__ void phase_update_norm(const TeamDesc<VT>& P, LzShared<VT>& sh, int t
       VT s = (VT)0;
 #pragma unroll
       for (int c = 0; c < MP1; ++c)
-        if (c < nv) s += P.Q[(size_t)c * ld + row] * (VT)sh.h[c];
+        if (c < nv) s += P.Q[(size_t)c * ld + row] * sh.hv[c];
       const VT q2 = buf[row] - s;
       buf[row] = q2;
       nrm += (AT)q2 * (AT)q2;
@@ -354,7 +356,9 @@ __device__ void restart_select(const D& P, LzShared<VT>& sh, int k, bool write_o
   __syncthreads();
   // eigh(T) (solver/lanczos.py:203): FP32 parallel Jacobi by the CTA ...
   {
+    const long long c0 = clock64();
     const bool ok = cta_jacobi_f32(Tf, MP1, m, sh.wf, Zf, MP1, sh.pidx, sh.rc, sh.rsn, sh.redf);
+    if (tid == 0) sh.eig_cycles += clock64() - c0;
     if (!ok && tid == 0) atomicOr(P.status, ST_SMALL_DENSE_FAIL);
   }
   for (int e = tid; e < m * m; e += LZ_BLOCK) {
@@ -489,6 +493,7 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
     }                                                   \
   } while (0)
   if (rank == 0 && tid < MAXM) { sh.alpha[tid] = 0.0; sh.beta[tid] = 0.0; }
+  if (tid == 0) sh.eig_cycles = 0;
   __syncthreads();
   int prev = 0;          // vbuf slot holding the latest unnormalised vector
   VT invb = (VT)1;       // its normalisation
@@ -624,6 +629,7 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
     for (int j = 0; j < 5; ++j) P.ctl[8 + j] = (int)(tp[j] >> 10);
     P.ctl[13] = sum_nv;
     P.ctl[14] = sum_kn;
+    P.ctl[15] = (int)(sh.eig_cycles >> 10);
     if (restart == 0) P.ctl[0] = 0;
   }
 }
@@ -723,6 +729,7 @@ __device__ __forceinline__ void cl_reduce(const double* part, int C, int nv, LzS
 #pragma unroll
         for (int r = 0; r < h; ++r) v[r] = v[r] + v[r + h];
       sh.h[c] = v[0];
+      sh.hv[c] = (VT)v[0];
     }
   }
   __syncthreads();
@@ -757,31 +764,44 @@ __device__ void cl_phase_spmv(const ClCtx<VT>& X, LzShared<VT>& sh, int i, const
 #pragma unroll
   for (int c = 0; c < MP1; ++c) acc[c] = (AT)0;
   for (int base = 0; base < X.rows; base += LZ_BLOCK) {
-    // SpMV of rows base..base+255 (L lanes per row) into sh.u.st.ys
+    // SpMV of rows base..base+255 (L lanes per row) into sh.u.st.ys; groups of
+    // up to 4 passes load their row bounds and first entries before any gather
+    constexpr int CH = L < 4 ? L : 4;
 #pragma unroll 1
-    for (int q = 0; q < L; ++q) {
-      const int lr = base + q * GPP + g;
-      AT sacc = (AT)0;
-      if (lr < X.rows) {
+    for (int q0 = 0; q0 < L; q0 += CH) {
+      int pb[CH], pe[CH];
+#pragma unroll
+      for (int q = 0; q < CH; ++q) {
+        const int lr = base + (q0 + q) * GPP + g;
+        pb[q] = 0; pe[q] = 0;
+        if (lr < X.rows) {
+          if (X.staged) { pb[q] = X.rp[lr] + lig; pe[q] = X.rp[lr + 1]; }
+          else { pb[q] = P.rowptr[X.r0 + lr] + lig; pe[q] = P.rowptr[X.r0 + lr + 1]; }
+        }
+      }
+      AT sacc[CH];
+#pragma unroll
+      for (int q = 0; q < CH; ++q) {
+        sacc[q] = (AT)0;
         if (X.staged) {
-          const int pe = X.rp[lr + 1];
-          for (int p = X.rp[lr] + lig; p < pe; p += L) {
+          for (int p = pb[q]; p < pe[q]; p += L) {
             const int w = X.cg[p];
-            sacc += (AT)X.vs[p] * (AT)cl_ld(cl_map(xbase + (w & 0xffffff), (unsigned)w >> 24), (VT)0);
+            sacc[q] += (AT)X.vs[p] * (AT)cl_ld(cl_map(xbase + (w & 0xffffff), (unsigned)w >> 24), (VT)0);
           }
         } else {
-          const int row = X.r0 + lr;
-          const int pe = P.rowptr[row + 1];
-          for (int p = P.rowptr[row] + lig; p < pe; p += L) {
+          for (int p = pb[q]; p < pe[q]; p += L) {
             const int gc = P.col[p];
             const int o = gc / rc;
-            sacc += (AT)P.val[p] * (AT)cl_ld(cl_map(xbase + (gc - o * rc), (unsigned)o), (VT)0);
+            sacc[q] += (AT)P.val[p] * (AT)cl_ld(cl_map(xbase + (gc - o * rc), (unsigned)o), (VT)0);
           }
         }
       }
 #pragma unroll
-      for (int o = L >> 1; o > 0; o >>= 1) sacc += __shfl_xor_sync(0xffffffffu, sacc, o);
-      if (lig == 0) sh.u.st.ys[q * GPP + g] = (double)sacc;
+      for (int q = 0; q < CH; ++q) {
+#pragma unroll
+        for (int o = L >> 1; o > 0; o >>= 1) sacc[q] += __shfl_xor_sync(0xffffffffu, sacc[q], o);
+        if (lig == 0) sh.u.st.ys[(q0 + q) * GPP + g] = (double)sacc[q];
+      }
     }
     __syncthreads();
     const int lr = base + tid;
@@ -839,7 +859,7 @@ __device__ void cl_phase_update_dot(const ClCtx<VT>& X, LzShared<VT>& sh, int nv
     for (int c = 0; c < MP1; ++c) {
       if (c < nv) {
         qr[c] = X.Qs[(size_t)c * rc + lr];
-        s += qr[c] * (VT)sh.h[c];
+        s += qr[c] * sh.hv[c];
       }
     }
     const VT q1 = buf[lr] - s;
@@ -861,7 +881,7 @@ __device__ void cl_phase_update_norm(const ClCtx<VT>& X, LzShared<VT>& sh, int n
     VT s = (VT)0;
 #pragma unroll
     for (int c = 0; c < MP1; ++c)
-      if (c < nv) s += X.Qs[(size_t)c * rc + lr] * (VT)sh.h[c];
+      if (c < nv) s += X.Qs[(size_t)c * rc + lr] * sh.hv[c];
     const VT q2 = buf[lr] - s;
     buf[lr] = q2;
     nrm += (AT)q2 * (AT)q2;
@@ -885,7 +905,7 @@ __device__ void cl_spmv_dispatch(const ClCtx<VT>& X, LzShared<VT>& sh, int i, co
 }
 
 template <typename VT>
-__global__ void __launch_bounds__(LZ_BLOCK)
+__global__ void __launch_bounds__(LZ_BLOCK, 1)
 lanczos_cluster_kernel(const __grid_constant__ ClusterBatch<VT> batch) {
   __shared__ LzShared<VT> sh;
   extern __shared__ __align__(16) unsigned char cl_dyn[];
@@ -930,6 +950,7 @@ lanczos_cluster_kernel(const __grid_constant__ ClusterBatch<VT> batch) {
   long long tp[5] = {0, 0, 0, 0, 0}, tmark = clock64();
   const bool timing = (rank == 0 && tid == 0);
   if (tid < MAXM) { sh.alpha[tid] = 0.0; sh.beta[tid] = 0.0; }
+  if (tid == 0) sh.eig_cycles = 0;
   __syncthreads();
   cl_sync();
   int prev = 0;
@@ -1062,6 +1083,7 @@ lanczos_cluster_kernel(const __grid_constant__ ClusterBatch<VT> batch) {
     for (int j = 0; j < 5; ++j) P.ctl[8 + j] = (int)(tp[j] >> 10);
     P.ctl[13] = sum_nv;
     P.ctl[14] = sum_kn;
+    P.ctl[15] = (int)(sh.eig_cycles >> 10);
     if (restart == 0) P.ctl[0] = 0;
   }
   cl_sync();   // no CTA leaves while a peer may still read its shared memory
