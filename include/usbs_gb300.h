@@ -78,6 +78,12 @@ int usbs_apply_A_adjoint(int n, int k, const int* row_ptr, const int* r_con, con
                          const double* r_a, const double* z, const double* U, int ldu,
                          double* out, int ldo, void* stream);
 
+/* Which Lanczos kernel usbs_eigsh_smallest launches for n rows (host call):
+ * 1 = one thread-block cluster with the basis in shared memory, 0 = a
+ * cooperative team streaming the basis through L2/HBM; negative on error.
+ * No counterpart in the reference. */
+int usbs_lanczos_kernel(int n, int inner_iterations, int precision);
+
 /* Workspace bytes needed by usbs_eigsh_smallest (host call, no GPU work). */
 size_t usbs_eigsh_workspace_bytes(int n, long long nnz, int inner_iterations, int precision);
 
@@ -229,6 +235,36 @@ size_t usbs_solve_workspace_bytes(const usbs_problem* problem, const usbs_params
 int usbs_solve(const usbs_problem* problem, const usbs_params* params, usbs_state* state,
                void* workspace, size_t workspace_bytes, usbs_cond_callback callback,
                void* callback_user, void* stream);
+
+/* ------------------------------------------------------------------ cgal()
+ * Settings of cgal() (solver/cgal.py:21-39). */
+typedef struct usbs_cgal_params {
+  double trace_ub, beta0;
+  int max_iters;
+  double max_time;          /* seconds of wall clock */
+  double obj_gap_eps, infeas_gap_eps, max_infeas_eps;
+  int lanczos_inner_iterations;  /* <= 32 */
+  int lanczos_max_restarts;
+  double subprob_eps;       /* Lanczos tolerance */
+  double cond_exp_base;     /* in [1, 2] */
+  int precision;            /* 64: FP64 everywhere; 32: FP32 Lanczos + FP64 rest */
+  int sketch_mode;          /* 0: Nystrom sketch P = X Omega, 1: dense X */
+  int sketch_dim;           /* columns of Omega (mode 0) */
+} usbs_cgal_params;
+
+/* Workspace bytes for usbs_cgal_solve (host call). */
+size_t usbs_cgal_workspace_bytes(const usbs_problem* problem, const usbs_cgal_params* params);
+
+/* cgal() (solver/cgal.py:21-243): CGAL iterations (one smallest eigenpair of
+ * -C + A*(adj) per iteration, rank-one sketch update, dual step) until the
+ * reference's stop condition holds, checked on the cond_exp_base schedule.
+ * Uses y, z, P/Omega (mode 0) or X (mode 1), q0, tr_X and primal_obj of
+ * `state` (V and debug are ignored); trace, if given, receives per iteration
+ * [t, smallest eigenvalue, obj_gap, infeas_gap, max_infeas, primal_obj, tr_X,
+ * dual step] in the first 8 of 20 doubles.  Synchronous. */
+int usbs_cgal_solve(const usbs_problem* problem, const usbs_cgal_params* params,
+                    usbs_state* state, void* workspace, size_t workspace_bytes,
+                    usbs_cond_callback callback, void* callback_user, void* stream);
 
 #ifdef __cplusplus
 }

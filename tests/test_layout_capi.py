@@ -4,6 +4,7 @@ import os
 import re
 
 import numpy as np
+import pytest
 import scipy.sparse as sp
 
 from usbs_gb300 import problem as P
@@ -89,3 +90,30 @@ def test_library_builds_and_exports_every_declared_symbol():
     assert set(names) <= set(_lib.SIGNATURES), "ctypes signatures missing for some entry points"
     lib.usbs_abi_version.restype = ctypes.c_int
     assert lib.usbs_abi_version() == 1
+
+
+def _as_set(A_data, A_idx, b, mask):
+    trip = {}
+    for (c, i, j), a in zip(np.asarray(A_idx), np.asarray(A_data)):
+        trip[(int(c), int(i), int(j))] = trip.get((int(c), int(i), int(j)), 0.0) + float(a)
+    return trip
+
+
+@pytest.mark.parametrize("l", [3, 5])
+def test_product_qap_builder_matches_oracle(l):
+    """usbs_gb300.problems.qap builds the same SDP as the oracle restatement of
+    utils/qap_helpers.py:157-381 (same constraints, right-hand sides, masks and scales)."""
+    from usbs_gb300.problems import qap as pqap
+    D, W = wl.qap_instance(l, 1, grid=6)
+    a = oqap.initialize_state(D, W, 4)
+    b = pqap.initialize_state(D, W, 4)
+    assert (a.C != b.C).nnz == 0
+    np.testing.assert_array_equal(a.b_ineq_mask, b.b_ineq_mask)
+    np.testing.assert_allclose(b.b, a.b, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(b.SCALE_A, a.SCALE_A, rtol=1e-10)
+    assert b.SCALE_C == pytest.approx(a.SCALE_C, rel=1e-14)
+    assert b.SCALE_X == a.SCALE_X
+    ta, tb = _as_set(a.A_data, a.A_indices, a.b, a.b_ineq_mask), \
+        _as_set(b.A_data, b.A_indices, b.b, b.b_ineq_mask)
+    assert ta.keys() == tb.keys()
+    assert max(abs(ta[k] - tb[k]) for k in ta) < 1e-12

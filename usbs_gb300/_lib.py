@@ -25,6 +25,7 @@ SIGNATURES = {
     "usbs_operator_apply": (c_int, [c_int, c_ll, P, P, P, P, P, c_int, P]),
     "usbs_apply_A_operator": (c_int, [c_int, c_int, P, P, P, P, P, c_int, P, P]),
     "usbs_apply_A_adjoint": (c_int, [c_int, c_int, P, P, P, P, P, P, c_int, P, c_int, P]),
+    "usbs_lanczos_kernel": (c_int, [c_int, c_int, c_int]),
     "usbs_eigsh_workspace_bytes": (c_size_t, [c_int, c_ll, c_int, c_int]),
     "usbs_eigsh_smallest": (c_int, [c_int, c_ll, P, P, P, c_double, P, P, P, P, P, P, c_int, c_int, c_int,
                                     c_double, c_int, P, c_int, P, P, P, c_size_t, P]),
@@ -33,6 +34,8 @@ SIGNATURES = {
     # struct-typed entry points; usbs_gb300.solver installs the exact ctypes types
     "usbs_solve_workspace_bytes": (c_size_t, [P, P]),
     "usbs_solve": (c_int, [P, P, P, P, c_size_t, P, P, P]),
+    "usbs_cgal_workspace_bytes": (c_size_t, [P, P]),
+    "usbs_cgal_solve": (c_int, [P, P, P, P, c_size_t, P, P, P]),
 }
 
 

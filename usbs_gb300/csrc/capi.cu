@@ -141,6 +141,11 @@ int usbs_apply_A_adjoint(int n, int k, const int* row_ptr, const int* r_con, con
                          (cudaStream_t)stream);
 }
 
+int usbs_lanczos_kernel(int n, int inner_iterations, int precision) {
+  if (precision != 32 && precision != 64) { set_error("precision must be 32 or 64"); return -2; }
+  return lanczos_kernel_kind(n, inner_iterations, precision);
+}
+
 size_t usbs_eigsh_workspace_bytes(int n, long long nnz, int inner_iterations, int precision) {
   DeviceInfo di;
   if (get_device_info(&di)) {

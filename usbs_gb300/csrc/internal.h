@@ -39,7 +39,11 @@ size_t lanczos_workspace_bytes(int n, int ld, int m, int prec, int nctas);
 int lanczos_team_size(const DeviceInfo& di, int n, int prec);
 int lanczos_lanes(int n, long long nnz);
 int lanczos_occupancy(int prec);
-// Runs `count` independent problems in one cooperative launch (one team each).
+// 1 if a problem of n rows and m inner vectors runs as a thread-block cluster
+// (shared-memory resident), 0 if it runs as a cooperative team.
+int lanczos_kernel_kind(int n, int m, int prec);
+// Runs `count` independent problems in one launch: one cluster each when they
+// fit, else one cooperative team each.
 int lanczos_run(const DeviceInfo& di, const LanczosProblem* probs, int count, int prec,
                 cudaStream_t stream);
 

@@ -1210,6 +1210,35 @@ static int run_typed(const DeviceInfo& di, const LanczosProblem* probs, int coun
   return 0;
 }
 
+// shared memory left for the cluster kernel's dynamic layout
+template <typename VT>
+constexpr size_t cl_budget() { return 227 * 1024 - sizeof(LzShared<VT>) - 1024; }
+// cluster size for n rows: FP64 arithmetic is slow on this part, so FP64
+// problems are spread thinner (128 rows per CTA against 640 for FP32); past
+// 16 CTAs the rows per CTA grow until the shared memory is full
+template <typename VT>
+inline int cl_csize(int n) {
+  const int target = (sizeof(VT) == 8) ? 128 : 640;
+  const int c = (n + target - 1) / target;
+  return c < 1 ? 1 : (c > CL_MAX_CTAS ? CL_MAX_CTAS : c);
+}
+template <typename VT>
+static bool cl_fits(int n, int m) {
+  const int csize = cl_csize<VT>(n);
+  if (csize > CL_MAX_CTAS || m > MAXM || m < 1 || n < 1) return false;
+  const int rc = (n + csize - 1) / csize;
+  return cl_layout<VT>(m, rc, 0).total <= cl_budget<VT>();
+}
+
+int lanczos_kernel_kind(int n, int m, int prec) {
+  static const int enabled = [] {
+    const char* e = getenv("USBS_LANCZOS_CLUSTER");
+    return e ? atoi(e) : 1;
+  }();
+  if (!enabled) return 0;
+  return (prec == 64 ? cl_fits<double>(n, m) : cl_fits<float>(n, m)) ? 1 : 0;
+}
+
 // Cluster path: every problem of the launch as one cluster of `csize` CTAs.
 // Returns 1 if the problems do not fit (the caller then runs the team kernel),
 // 0 on success, negative on a launch error.
@@ -1220,14 +1249,10 @@ static int run_cluster(const LanczosProblem* probs, int count, cudaStream_t stre
     return e ? atoi(e) : 1;
   }();
   if (!enabled || count < 1 || count > MAX_TEAMS) return 1;
-  constexpr size_t STATIC_SMEM = sizeof(LzShared<VT>);
-  constexpr size_t BUDGET = 227 * 1024 - STATIC_SMEM - 1024;
-  // rows per CTA: FP64 arithmetic is slow on this part, so FP64 problems are
-  // spread thinner
-  const int target = (sizeof(VT) == 8) ? 128 : 640;
+  constexpr size_t BUDGET = cl_budget<VT>();
   int csize = 1;
   for (int i = 0; i < count; ++i) {
-    const int c = (probs[i].n + target - 1) / target;
+    const int c = cl_csize<VT>(probs[i].n);
     csize = c > csize ? c : csize;
   }
   if (csize > CL_MAX_CTAS) return 1;

@@ -1012,6 +1012,193 @@ static std::vector<long long> cond_schedule(long long maxiter, double base) {
   return out;
 }
 
+// ================================================================ CGAL
+// cgal() (solver/cgal.py:21-243) on the device: per iteration one m-vector
+// pass (projection onto the constraint set, the adjoint weights and the gap
+// and infeasibility sums), eigsh(1) on -C + A*(adj), C v and A(v v^T), a
+// second m-vector pass (the new z and the dual-step denominator, its last block
+// forms every scalar of the iteration), the y step and the rank-one sketch (or
+// dense X) update.  All reductions are fixed-order (per-block partials summed
+// by the last block), so results are deterministic.
+
+enum CgalSlot {
+  CG_ADJZ = 0, CG_YDZ, CG_DZDZ, CG_INF2, CG_PB2, CG_INFMAX, CG_VCV, CG_VV, CG_ADJAV, CG_ZNPB,
+  CG_PRIMAL, CG_TRX, CG_OBJGAP, CG_INFGAP, CG_MAXINF, CG_DSS, CG_EIG0, CG_NUM
+};
+
+struct CgalArgs {
+  int m, t;
+  double* sc;                       // CG_NUM scalars, then v^T Omega
+  double *y, *z, *adj, *zn, *Av;
+  const double *b, *mask, *scale_a;
+  double scale_c, scale_x, beta, beta_next, eta, trace_ub, beta0;
+  double* partial;
+  unsigned int* counter;
+  double* trace;
+  int trace_capacity;
+};
+
+__device__ __forceinline__ MvecArgs cg_fin(const CgalArgs& a) {
+  MvecArgs f;
+  f.partial = a.partial;
+  f.counter = a.counter;
+  return f;
+}
+
+// proj_b, adj and the sums of solver/cgal.py:104-107 and 118-138 that use the
+// current z
+__global__ void __launch_bounds__(RED_BLOCK) cgal_pre_kernel(CgalArgs a) {
+  __shared__ double red[RED_BLOCK / 32];
+  double v[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < a.m; c += gridDim.x * blockDim.x) {
+    const double y = a.y[c], z = a.z[c], b = a.b[c], mk = a.mask[c], sa = a.scale_a[c];
+    const double pb = (1.0 - mk) * b + mk * fmin(z + (1.0 / a.beta) * y, b);
+    const double dz = z - pb;
+    const double adj = y + a.beta * dz;
+    a.adj[c] = adj;
+    v[0] += adj * z;
+    v[1] += y * dz;
+    v[2] += dz * dz;
+    const double pb0 = (1.0 - mk) * b + mk * fmin(z, b);
+    const double e = ((z - pb0) / sa) / a.scale_x;
+    const double f = (pb0 / sa) / a.scale_x;
+    v[3] += e * e;
+    v[4] += f * f;
+    v[5] = fmax(v[5], fabs((z - pb0) / sa));
+  }
+  const bool is_max[6] = {false, false, false, false, false, true};
+  if (!mvec_finish<6>(cg_fin(a), v, is_max, red)) return;
+  if (threadIdx.x == 0)
+    for (int r = 0; r < 6; ++r) a.sc[CG_ADJZ + r] = red[r];
+}
+
+// v = Q[:, 0], or 0 when the smallest eigenvalue is >= 0 (solver/cgal.py:113-116)
+template <typename VT>
+__global__ void cgal_v_kernel(int n, const VT* __restrict__ Q, const double* alpha,
+                              double* __restrict__ v, double* sc) {
+  const bool zero = !(alpha[0] < 0.0);
+  if (blockIdx.x == 0 && threadIdx.x == 0) sc[CG_EIG0] = alpha[0];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    v[i] = zero ? 0.0 : (double)Q[i];
+}
+
+// z_next and the dual-step denominator; the last block forms the iteration's
+// scalars (solver/cgal.py:108-112, 139-170)
+__global__ void __launch_bounds__(RED_BLOCK) cgal_post_kernel(CgalArgs a) {
+  __shared__ double red[RED_BLOCK / 32];
+  double v[2] = {0.0, 0.0};
+  const double eta = a.eta, tr = a.trace_ub;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < a.m; c += gridDim.x * blockDim.x) {
+    const double zn = (1.0 - eta) * a.z[c] + eta * tr * a.Av[c];
+    a.zn[c] = zn;
+    const double b = a.b[c], mk = a.mask[c];
+    const double pbn = (1.0 - mk) * b + mk * fmin(zn + (1.0 / a.beta_next) * a.y[c], b);
+    v[0] += a.adj[c] * a.Av[c];
+    const double d = zn - pbn;
+    v[1] += d * d;
+  }
+  const bool is_max[2] = {false, false};
+  if (!mvec_finish<2>(cg_fin(a), v, is_max, red)) return;
+  if (threadIdx.x != 0) return;
+  double* sc = a.sc;
+  sc[CG_ADJAV] = red[0];
+  sc[CG_ZNPB] = red[1];
+  const double primal = sc[CG_PRIMAL];
+  const double scx = a.scale_c * a.scale_x;
+  // v^T A*(adj) v = adj . A(v v^T)
+  double sdg = tr * sc[CG_VCV] - primal;
+  sdg += sc[CG_ADJZ];
+  sdg -= tr * red[0];
+  double og = sdg - sc[CG_YDZ];
+  og -= 0.5 * a.beta * sc[CG_DZDZ];
+  og = og / scx;
+  og /= 1.0 + fabs(primal) / scx;
+  const double ig = sqrt(sc[CG_INF2]) / (1.0 + sqrt(sc[CG_PB2]));
+  const double mi = sc[CG_INFMAX] / a.scale_x;
+  const double q = 4.0 * a.beta_next * eta * eta * tr * tr / red[1];
+  const double dss = fmin(fmax(q, 0.0), a.beta0);
+  const double primal_n = (1.0 - eta) * primal + eta * tr * sc[CG_VCV];
+  const double trx_n = (1.0 - eta) * sc[CG_TRX] + eta * tr * sc[CG_VV];
+  sc[CG_OBJGAP] = og;
+  sc[CG_INFGAP] = ig;
+  sc[CG_MAXINF] = mi;
+  sc[CG_DSS] = dss;
+  sc[CG_PRIMAL] = primal_n;
+  sc[CG_TRX] = trx_n;
+  if (a.trace && a.t < a.trace_capacity) {
+    double* r = a.trace + (size_t)a.t * TR_NUM;
+    r[0] = a.t; r[1] = sc[CG_EIG0]; r[2] = og; r[3] = ig; r[4] = mi; r[5] = primal_n;
+    r[6] = trx_n; r[7] = dss;
+  }
+}
+
+// y <- y + dss (z_next - proj_b), z <- z_next (solver/cgal.py:168-172)
+__global__ void cgal_y_kernel(CgalArgs a) {
+  const double dss = a.sc[CG_DSS];
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < a.m; c += gridDim.x * blockDim.x) {
+    const double zn = a.zn[c], b = a.b[c], mk = a.mask[c], y = a.y[c];
+    const double pbn = (1.0 - mk) * b + mk * fmin(zn + (1.0 / a.beta_next) * y, b);
+    a.y[c] = y + dss * (zn - pbn);
+    a.z[c] = zn;
+  }
+}
+
+// P <- (1 - eta) P + eta tr v (v^T Omega)   (solver/cgal.py:155-158)
+__global__ void cgal_sketch_kernel(int n, int ssk, const double* __restrict__ v,
+                                   const double* __restrict__ vO, double* __restrict__ P, int ldp,
+                                   double eta, double tr) {
+  const long long total = (long long)n * ssk;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int c = (int)(e / n), i = (int)(e - (long long)c * n);
+    const size_t o = (size_t)c * ldp + i;
+    P[o] = (1.0 - eta) * P[o] + eta * tr * (v[i] * vO[c]);
+  }
+}
+
+// X <- (1 - eta) X + eta tr v v^T   (row-major n x n, solver/cgal.py:153-154)
+__global__ void cgal_dense_kernel(int n, const double* __restrict__ v, double* __restrict__ X,
+                                  double eta, double tr) {
+  const long long total = (long long)n * n;
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int r = (int)(e / n), c = (int)(e - (long long)r * n);
+    X[e] = (1.0 - eta) * X[e] + eta * tr * (v[r] * v[c]);
+  }
+}
+
+struct CgalLayout {
+  int n, m, ld, mL, vt, ssk, grid_red, grid_gram;
+  double *sc, *adj, *zn, *Av, *v, *Cv, *mpart, *gpart, *alpha, *beta;
+  void *opL, *Q, *q0L, *lz_work;
+  unsigned int* counters;
+  int *status, *ctl;
+};
+
+static void cgal_plan(const usbs_problem* P, const usbs_cgal_params* Pa, const DeviceInfo& di,
+                      Arena& ar, CgalLayout& L) {
+  L.n = P->n; L.m = P->m; L.ld = (L.n + 31) & ~31; L.mL = Pa->lanczos_inner_iterations;
+  L.vt = (Pa->precision == 64) ? 8 : 4;
+  L.ssk = (Pa->sketch_mode == 0) ? Pa->sketch_dim : 0;
+  L.grid_red = di.sm_count * 2;
+  L.grid_gram = di.sm_count * 2;
+  L.sc = ar.take<double>(CG_NUM + 64);
+  L.adj = ar.take<double>(L.m); L.zn = ar.take<double>(L.m); L.Av = ar.take<double>(L.m);
+  L.v = ar.take<double>(L.ld); L.Cv = ar.take<double>(L.ld);
+  L.mpart = ar.take<double>((size_t)L.grid_red * 8);
+  L.gpart = ar.take<double>((size_t)L.grid_gram * 64);
+  L.alpha = ar.take<double>(2 * MAXM);
+  L.beta = L.alpha ? L.alpha + MAXM : nullptr;
+  L.opL = ar.take<char>((size_t)(P->nnz > 0 ? P->nnz : 1) * L.vt);
+  L.Q = ar.take<char>((size_t)L.ld * (L.mL + 1) * L.vt);
+  L.q0L = ar.take<char>((size_t)L.ld * L.vt);
+  L.counters = ar.take<unsigned int>(16);
+  L.status = ar.take<int>(32);
+  L.ctl = L.status + 16;
+  const int nct = lanczos_team_size(di, L.n, Pa->precision);
+  L.lz_work = ar.take<char>(lanczos_workspace_bytes(L.n, L.ld, L.mL, Pa->precision, nct));
+}
+
 }  // namespace usbs
 
 using namespace usbs;
@@ -1188,6 +1375,190 @@ int usbs_solve(const usbs_problem* P, const usbs_params* Pa, usbs_state* S, void
   S->status = status[0];
   S->elapsed = elapsed();
   S->kernel_launches = X.launches;
+  return 0;
+}
+
+size_t usbs_cgal_workspace_bytes(const usbs_problem* P, const usbs_cgal_params* Pa) {
+  DeviceInfo di;
+  if (get_device_info(&di)) { di.sm_count = 152; di.lanczos_occ64 = di.lanczos_occ32 = 4; }
+  Arena ar{nullptr, 0, 0};
+  CgalLayout L;
+  cgal_plan(P, Pa, di, ar, L);
+  return ar.off + 4096;
+}
+
+int usbs_cgal_solve(const usbs_problem* P, const usbs_cgal_params* Pa, usbs_state* S,
+                    void* workspace, size_t workspace_bytes, usbs_cond_callback cb, void* cb_user,
+                    void* stream) {
+  if (!P || !Pa || !S) { set_error("usbs_cgal_solve: null argument"); return -2; }
+  if (Pa->lanczos_inner_iterations < 1 || Pa->lanczos_inner_iterations > MAXM) {
+    set_error("usbs_cgal_solve: lanczos_inner_iterations must be in [1, %d]", MAXM);
+    return -2;
+  }
+  if (Pa->precision != 64 && Pa->precision != 32) { set_error("precision must be 32 or 64"); return -2; }
+  if (Pa->sketch_mode == 0 && (Pa->sketch_dim < 1 || Pa->sketch_dim > 64 || !S->Omega || !S->P)) {
+    set_error("usbs_cgal_solve: sketch mode needs 1 <= sketch_dim <= 64, P and Omega");
+    return -2;
+  }
+  if (Pa->sketch_mode == 1 && (!S->X || P->n > 46340)) {
+    set_error("usbs_cgal_solve: dense-X mode needs X and n <= 46340");
+    return -2;
+  }
+  if (Pa->sketch_mode != 0 && Pa->sketch_mode != 1) { set_error("usbs_cgal_solve: sketch_mode must be 0 or 1"); return -2; }
+  if (S->ld != ((P->n + 31) & ~31)) { set_error("usbs_cgal_solve: state ld must be n rounded up to 32"); return -2; }
+  if (Pa->cond_exp_base < 1.0 || Pa->cond_exp_base > 2.0) { set_error("cond_exp_base must be in [1, 2]"); return -2; }
+  DeviceInfo di;
+  CK(get_device_info(&di));
+  Arena ar{(char*)workspace, 0, workspace_bytes};
+  CgalLayout L;
+  cgal_plan(P, Pa, di, ar, L);
+  if (!workspace || ar.off + 1024 > workspace_bytes) {
+    set_error("usbs_cgal_solve: workspace of %zu bytes given, %zu needed", workspace_bytes, ar.off + 4096);
+    return -2;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  long long launches = 0;
+  const int lanes = lanczos_lanes(L.n, P->nnz);
+  auto rgrid = [&](long long work) {
+    long long b = (work + 255) / 256;
+    if (b > (long long)di.sm_count * 8) b = (long long)di.sm_count * 8;
+    return (int)(b < 1 ? 1 : b);
+  };
+  int mgrid = (L.m + RED_BLOCK - 1) / RED_BLOCK;
+  if (mgrid > L.grid_red) mgrid = L.grid_red;
+  if (mgrid < 1) mgrid = 1;
+  auto gram1 = [&](const double* Y, int ky, double* out) -> int {
+    GramArgs g;
+    g.n = L.n; g.kx = 1; g.ky = ky; g.ldx = L.ld; g.ldy = L.ld; g.X = L.v; g.Y = Y;
+    g.partial = L.gpart; g.counter = L.counters + 8; g.out = out; g.skip = nullptr;
+    int blocks = (L.n + GR_ROWS - 1) / GR_ROWS;
+    if (blocks > L.grid_gram) blocks = L.grid_gram;
+    if (blocks < 1) blocks = 1;
+    ++launches;
+    gram_kernel<1><<<blocks, RED_BLOCK, 0, st>>>(g);
+    return kerr("cgal gram");
+  };
+  cudaMemsetAsync(L.counters, 0, 16 * sizeof(unsigned int), st);
+  cudaMemsetAsync(L.status, 0, 32 * sizeof(int), st);
+  cudaMemsetAsync(L.sc, 0, (CG_NUM + 64) * sizeof(double), st);
+  if (Pa->precision == 64)
+    cudaMemcpyAsync(L.q0L, S->q0, (size_t)L.n * sizeof(double), cudaMemcpyDeviceToDevice, st);
+  else
+    to_vt_kernel<float><<<rgrid(L.n), 256, 0, st>>>(L.n, S->q0, (float*)L.q0L);
+  {
+    double init[2] = {S->primal_obj, S->tr_X};
+    double g3[3] = {1.1 * Pa->obj_gap_eps, 1.1 * Pa->infeas_gap_eps, 1.1 * Pa->max_infeas_eps};
+    if (cudaMemcpyAsync(L.sc + CG_PRIMAL, init, sizeof(init), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaMemcpyAsync(L.sc + CG_OBJGAP, g3, sizeof(g3), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return kerr("cgal init");
+  }
+  CK(kerr("cgal init"));
+  CgalArgs a;
+  a.m = L.m; a.sc = L.sc; a.y = S->y; a.z = S->z; a.adj = L.adj; a.zn = L.zn; a.Av = L.Av;
+  a.b = P->b; a.mask = P->b_ineq_mask; a.scale_a = P->scale_a; a.scale_c = P->scale_c;
+  a.scale_x = P->scale_x; a.trace_ub = Pa->trace_ub; a.beta0 = Pa->beta0;
+  a.partial = L.mpart; a.counter = L.counters; a.trace = S->trace;
+  a.trace_capacity = S->trace ? S->trace_capacity : 0;
+  auto body = [&](int t) -> int {
+    a.t = t;
+    a.beta = Pa->beta0 * std::sqrt((double)t + 1.0);
+    a.beta_next = Pa->beta0 * std::sqrt((double)t + 2.0);
+    a.eta = 2.0 / ((double)t + 2.0);
+    ++launches;
+    cgal_pre_kernel<<<mgrid, RED_BLOCK, 0, st>>>(a);
+    CK(kerr("cgal pre"));
+    // eigsh(1) of -C + A*(adj) (solver/cgal.py:108-112)
+    ++launches;
+    CK(assemble_operator((int)P->nnz, P->c_val, -1.0, P->slot_ptr, P->slot_tid, P->t_con, P->t_a0,
+                         L.adj, L.opL, Pa->precision, st));
+    if (cudaMemcpyAsync(L.Q, L.q0L, (size_t)L.n * L.vt, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
+      return kerr("cgal q0");
+    LanczosProblem lp;
+    lp.n = L.n; lp.ld = L.ld; lp.m = L.mL; lp.num_desired = 1;
+    lp.max_restarts = Pa->lanczos_max_restarts; lp.nnz = P->nnz; lp.tol = Pa->subprob_eps;
+    lp.rowptr = P->rowptr; lp.col = P->col; lp.val = L.opL; lp.Q = L.Q;
+    lp.alpha = L.alpha; lp.beta = L.beta; lp.ctl = L.ctl; lp.status = L.status; lp.work = L.lz_work;
+    ++launches;
+    CK(lanczos_run(di, &lp, 1, Pa->precision, st));
+    ++launches;
+    if (Pa->precision == 64)
+      cgal_v_kernel<double><<<rgrid(L.n), 256, 0, st>>>(L.n, (const double*)L.Q, L.alpha, L.v, L.sc);
+    else
+      cgal_v_kernel<float><<<rgrid(L.n), 256, 0, st>>>(L.n, (const float*)L.Q, L.alpha, L.v, L.sc);
+    CK(kerr("cgal v"));
+    // C v and A(v v^T)
+    ++launches;
+    spmm_kernel<<<rgrid((long long)L.n * lanes), 256, 0, st>>>(L.n, P->rowptr, P->col, P->c_val, L.v,
+                                                             L.ld, 1, L.Cv, L.ld, lanes, nullptr);
+    CK(kerr("cgal Cv"));
+    ++launches;
+    CK(apply_A_operator(L.m, P->con_ptr, P->t_row, P->t_col, P->t_a, L.v, L.ld, 1, L.Av, st));
+    CK(gram1(L.Cv, 1, L.sc + CG_VCV));
+    CK(gram1(L.v, 1, L.sc + CG_VV));
+    if (Pa->sketch_mode == 0) CK(gram1(S->Omega, L.ssk, L.sc + CG_NUM));
+    ++launches;
+    cgal_post_kernel<<<mgrid, RED_BLOCK, 0, st>>>(a);
+    CK(kerr("cgal post"));
+    ++launches;
+    cgal_y_kernel<<<mgrid, RED_BLOCK, 0, st>>>(a);
+    CK(kerr("cgal y"));
+    ++launches;
+    if (Pa->sketch_mode == 0)
+      cgal_sketch_kernel<<<rgrid((long long)L.n * L.ssk), 256, 0, st>>>(L.n, L.ssk, L.v, L.sc + CG_NUM,
+                                                                       S->P, S->ld, a.eta, Pa->trace_ub);
+    else
+      cgal_dense_kernel<<<rgrid((long long)L.n * L.n), 256, 0, st>>>(L.n, L.v, S->X, a.eta, Pa->trace_ub);
+    return kerr("cgal update");
+  };
+  // loop with the reference's condition schedule (utils/loop.py:80-115,
+  // cond = solver/cgal.py:76-97)
+  const auto t0 = std::chrono::steady_clock::now();
+  auto elapsed = [&]() {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  };
+  double curr_time = 0.0;
+  auto read = [&](double* out, int first, int count) -> int {
+    if (cudaMemcpyAsync(out, L.sc + first, count * sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaStreamSynchronize(st) != cudaSuccess)
+      return kerr("cgal read");
+    return 0;
+  };
+  auto cond = [&](int t, bool* go) -> int {
+    double g[3];
+    CK(read(g, CG_OBJGAP, 3));
+    if (cb) cb(cb_user, t);
+    *go = (t == 0) || ((curr_time < Pa->max_time) &&
+                       (g[0] > Pa->obj_gap_eps || g[1] > Pa->infeas_gap_eps || g[2] > Pa->max_infeas_eps));
+    return 0;
+  };
+  const std::vector<long long> sched = cond_schedule(Pa->max_iters, Pa->cond_exp_base);
+  int t = 0;
+  bool go = true;
+  CK(cond(0, &go));
+  for (size_t bk = 0; bk < sched.size() && go; ++bk) {
+    for (long long j = 0; j < sched[bk]; ++j) {
+      CK(body(t));
+      ++t;
+    }
+    if (cudaStreamSynchronize(st) != cudaSuccess) return kerr("cgal iteration");
+    curr_time = elapsed();
+    CK(cond(t, &go));
+  }
+  double sc[CG_NUM];
+  CK(read(sc, 0, CG_NUM));
+  int status[8];
+  if (cudaMemcpy(status, L.status, sizeof(status), cudaMemcpyDeviceToHost) != cudaSuccess)
+    return kerr("cgal status");
+  S->iterations = t;
+  S->tr_X = sc[CG_TRX];
+  S->primal_obj = sc[CG_PRIMAL];
+  S->obj_gap = sc[CG_OBJGAP];
+  S->infeas_gap = sc[CG_INFGAP];
+  S->max_infeas = sc[CG_MAXINF];
+  S->status = status[0];
+  S->elapsed = elapsed();
+  S->kernel_launches = launches;
   return 0;
 }
 

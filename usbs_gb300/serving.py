@@ -1,0 +1,223 @@
+"""Continuous-batching solve service: many SDP instances resident on one GPU.
+
+Requests (an SDPState plus the usbs() arguments) are admitted as a slot and enough
+HBM free up, so requests that arrive while others run start without waiting for the
+batch to drain. Each admitted request runs ``usbs()`` to completion on its own CUDA
+stream, driven by its own host thread. ctypes releases the GIL during the call, so
+the solves' kernels overlap on the device.
+
+A problem whose Lanczos basis fits in one thread-block cluster's shared memory
+(``usbs_lanczos_kernel`` = 1) uses cluster-scheduled kernels only, and any number
+of those run side by side. A larger problem uses the cooperative team kernel, whose
+grid is sized for the whole GPU. It therefore runs alone: it waits for the
+running solves to finish, and nothing else is admitted until it is done.
+
+Admission by memory: the service owns the HBM that was free when it started,
+less ``reserve_bytes``. A request's device footprint (its state and its
+``usbs_solve`` workspace) is computed exactly at submission. The request is
+admitted only if that footprint plus the footprints of the running solves fits in
+the budget.
+
+The reference has no serving layer. Each result is the same as a solve of that
+request alone: the kernels are deterministic and share no state between solves.
+"""
+import collections
+import ctypes
+import threading
+import time
+
+import numpy as np
+
+from . import _lib, solver
+
+__all__ = ["SolveRequest", "SolverService", "Admission", "footprint_bytes"]
+
+
+class Admission:
+    """Slot and memory accounting of the service (host logic only)."""
+
+    def __init__(self, budget_bytes, max_slots):
+        self.budget = int(budget_bytes)
+        self.free_slots = int(max_slots)
+        self.running = 0
+        self.running_bytes = 0
+        self.exclusive = False
+
+    def admissible(self, footprint, exclusive):
+        if self.exclusive or self.free_slots == 0:
+            return False
+        if exclusive and self.running > 0:
+            return False
+        return self.running_bytes + footprint <= self.budget
+
+    def start(self, footprint, exclusive):
+        self.free_slots -= 1
+        self.running += 1
+        self.running_bytes += footprint
+        self.exclusive = self.exclusive or exclusive
+
+    def finish(self, footprint, exclusive):
+        self.free_slots += 1
+        self.running -= 1
+        self.running_bytes -= footprint
+        if exclusive:
+            self.exclusive = False
+
+    def pick(self, queue):
+        """Index of the first admissible request in arrival order, or None.  A
+        request that does not fit does not block smaller ones behind it, except
+        an exclusive one, which holds the line until the GPU drains."""
+        for i, (footprint, exclusive) in enumerate(queue):
+            if self.admissible(footprint, exclusive):
+                return i
+            if exclusive:
+                return None
+        return None
+
+
+class SolveRequest:
+    """One usbs() call.  ``kwargs`` are usbs()'s arguments after ``sdp_state``
+    (n, m, trace_ub, ... as keywords); ``precision`` 32 or 64."""
+
+    def __init__(self, sdp_state, precision=32, tag=None, **kwargs):
+        self.sdp_state = sdp_state
+        self.precision = int(precision)
+        self.kwargs = kwargs
+        self.tag = tag
+        self.arrival = None
+        self.start = None
+        self.finish = None
+        self.result = None
+        self.info = None
+        self.error = None
+        self.done = threading.Event()
+        self.footprint = None
+        self.exclusive = False
+
+    @property
+    def latency(self):
+        return None if self.finish is None else self.finish - self.arrival
+
+    def wait(self, timeout=None):
+        self.done.wait(timeout)
+        if self.error is not None:
+            raise self.error
+        return self.result
+
+
+def footprint_bytes(host_layout, k, sketch_dim, params_struct, lib):
+    """Device bytes one solve holds: its problem layout, constraint vectors,
+    iterate state and usbs_solve workspace."""
+    n, m = host_layout.n, host_layout.m
+    ld = (n + 31) // 32 * 32
+    prob = solver.UsbsProblem()
+    prob.n, prob.m, prob.nnz, prob.num_triples = n, m, host_layout.nnz, host_layout.num_triples
+    ws = int(lib.usbs_solve_workspace_bytes(ctypes.byref(prob), ctypes.byref(params_struct)))
+    lay = sum(getattr(host_layout, f).nbytes for f in solver.DeviceProblem.FIELDS)
+    state = 8 * (3 * m + 2 * m + ld * k + 2 * ld * max(sketch_dim, 1) + ld)
+    return ws + lay + state
+
+
+class SolverService:
+    """``submit()`` requests; ``max_slots`` solves run at once."""
+
+    def __init__(self, device="cuda", max_slots=8, reserve_bytes=2 << 30, mem_info=None):
+        import torch
+        self.device = torch.device(device)
+        self.max_slots = int(max_slots)
+        self.reserve = int(reserve_bytes)
+        mem_info = mem_info or (lambda: torch.cuda.mem_get_info(self.device))
+        free, _total = mem_info()
+        self._adm = Admission(free - self.reserve, self.max_slots)
+        self._cv = threading.Condition()
+        self._queue = collections.deque()
+        self._stop = False
+        self._streams = [torch.cuda.Stream(self.device) for _ in range(self.max_slots)]
+        self._free_streams = list(range(self.max_slots))
+        self._threads = [threading.Thread(target=self._worker, daemon=True)
+                         for _ in range(self.max_slots)]
+        for t in self._threads:
+            t.start()
+
+    # ------------------------------------------------------------ public
+    def submit(self, req):
+        lib = _lib.load()
+        solver._sigs(lib)
+        kw = req.kwargs
+        host = solver.host_problem_layout(req.sdp_state)
+        req._host_layout = host
+        n = kw["n"]
+        k = kw["k_curr"] + kw["k_past"]
+        sdim = 0 if req.sdp_state.Omega is None else int(np.shape(req.sdp_state.Omega)[1])
+        prm = solver.UsbsParams()
+        prm.k_curr, prm.k_past = kw["k_curr"], kw["k_past"]
+        prm.lanczos_inner_iterations = kw["lanczos_inner_iterations"]
+        prm.precision = req.precision
+        prm.sketch_mode = 0 if sdim else (1 if req.sdp_state.X is not None else 2)
+        prm.sketch_dim = sdim
+        req.footprint = footprint_bytes(host, k, sdim, prm, lib)
+        req.exclusive = lib.usbs_lanczos_kernel(n, kw["lanczos_inner_iterations"],
+                                                req.precision) != 1
+        req.arrival = time.perf_counter()
+        with self._cv:
+            self._queue.append(req)
+            self._cv.notify_all()
+        return req
+
+    def shutdown(self):
+        with self._cv:
+            self._stop = True
+            self._cv.notify_all()
+        for t in self._threads:
+            t.join()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.shutdown()
+
+    # ------------------------------------------------------------ scheduling
+    def _next(self):
+        """Called with the lock held: pop the next admissible request."""
+        i = self._adm.pick([(r.footprint, r.exclusive) for r in self._queue])
+        if i is None:
+            return None
+        req = self._queue[i]
+        del self._queue[i]
+        return req
+
+    def _worker(self):
+        import torch
+        while True:
+            with self._cv:
+                while True:
+                    if self._stop and not self._queue:
+                        return
+                    req = self._next()
+                    if req is not None:
+                        break
+                    self._cv.wait(0.05)
+                sidx = self._free_streams.pop()
+                self._adm.start(req.footprint, req.exclusive)
+            stream = self._streams[sidx]
+            req.start = time.perf_counter()
+            try:
+                with torch.cuda.stream(stream):
+                    inst = solver.DeviceInstance(req.sdp_state, self.device,
+                                                 host_layout=req._host_layout)
+                    out, info = solver.usbs(req.sdp_state, precision=req.precision,
+                                            device=self.device, return_info=True,
+                                            instance=inst, stream=stream, **req.kwargs)
+                    stream.synchronize()
+                    del inst
+                req.result, req.info = out, info
+            except Exception as exc:   # reported to the caller through wait()
+                req.error = exc
+            req.finish = time.perf_counter()
+            with self._cv:
+                self._adm.finish(req.footprint, req.exclusive)
+                self._free_streams.append(sidx)
+                self._cv.notify_all()
+            req._host_layout = None
+            req.done.set()

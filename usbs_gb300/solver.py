@@ -62,6 +62,16 @@ class UsbsState(ctypes.Structure):
          ("kernel_launches", ctypes.c_longlong)]
 
 
+class CgalParams(ctypes.Structure):
+    _fields_ = [("trace_ub", ctypes.c_double), ("beta0", ctypes.c_double),
+                ("max_iters", ctypes.c_int), ("max_time", ctypes.c_double),
+                ("obj_gap_eps", ctypes.c_double), ("infeas_gap_eps", ctypes.c_double),
+                ("max_infeas_eps", ctypes.c_double), ("lanczos_inner_iterations", ctypes.c_int),
+                ("lanczos_max_restarts", ctypes.c_int), ("subprob_eps", ctypes.c_double),
+                ("cond_exp_base", ctypes.c_double), ("precision", ctypes.c_int),
+                ("sketch_mode", ctypes.c_int), ("sketch_dim", ctypes.c_int)]
+
+
 CALLBACK = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int)
 
 TRACE_FIELDS = ["t", "primal_obj", "obj_ub", "obj_gap", "infeas_gap", "max_infeas",
@@ -77,22 +87,36 @@ def _sigs(lib):
     lib.usbs_solve.restype = ctypes.c_int
     lib.usbs_solve.argtypes = [ctypes.POINTER(UsbsProblem), ctypes.POINTER(UsbsParams),
                                ctypes.POINTER(UsbsState), P, ctypes.c_size_t, CALLBACK, P, P]
+    lib.usbs_cgal_workspace_bytes.restype = ctypes.c_size_t
+    lib.usbs_cgal_workspace_bytes.argtypes = [ctypes.POINTER(UsbsProblem),
+                                              ctypes.POINTER(CgalParams)]
+    lib.usbs_cgal_solve.restype = ctypes.c_int
+    lib.usbs_cgal_solve.argtypes = [ctypes.POINTER(UsbsProblem), ctypes.POINTER(CgalParams),
+                                    ctypes.POINTER(UsbsState), P, ctypes.c_size_t, CALLBACK, P,
+                                    P]
 
 
 def _ptr(t):
     return int(t.data_ptr()) if t is not None else None
 
 
+def host_problem_layout(sdp_state):
+    """The problem's device layout built on the host (no device memory)."""
+    A_idx = np.asarray(_host(sdp_state.A_indices))
+    b = np.asarray(_host(sdp_state.b))
+    return layout(sp.csr_matrix(sdp_state.C), _host(sdp_state.A_data), A_idx, m=b.shape[0])
+
+
 class DeviceInstance:
     """Problem layout + constraint vectors of one SDP, resident on one device."""
 
-    def __init__(self, sdp_state, device):
+    def __init__(self, sdp_state, device, host_layout=None):
         import torch
         self.device = torch.device(device)
-        A_idx = np.asarray(_host(sdp_state.A_indices))
         b = np.asarray(_host(sdp_state.b), dtype=np.float64)
-        self.problem = DeviceProblem(layout(sp.csr_matrix(sdp_state.C), _host(sdp_state.A_data),
-                                            A_idx, m=b.shape[0]), device)
+        if host_layout is None:
+            host_layout = host_problem_layout(sdp_state)
+        self.problem = DeviceProblem(host_layout, device)
         mask = np.asarray(_host(sdp_state.b_ineq_mask), dtype=np.float64)
         SA = np.broadcast_to(np.asarray(_host(sdp_state.SCALE_A), dtype=np.float64),
                              b.shape).copy()
@@ -232,6 +256,97 @@ def usbs(sdp_state, n, m, trace_ub, trace_factor, rho, beta, k_curr, k_past, max
     if return_trace:
         tr = trace[:pst.iterations].cpu().numpy()
         recs = [{f: float(r[i]) for i, f in enumerate(TRACE_FIELDS)} for r in tr]
+        return out, recs, info
+    if return_info:
+        return out, info
+    return out
+
+
+CGAL_TRACE_FIELDS = ["t", "eig0", "obj_gap", "infeas_gap", "max_infeas", "primal_obj", "tr_X",
+                     "dual_step"]
+
+
+def cgal(sdp_state, n, m, trace_ub, beta0, max_iters, max_time, obj_gap_eps, infeas_gap_eps,
+         max_infeas_eps, lanczos_inner_iterations, lanczos_max_restarts, subprob_eps,
+         cond_exp_base=1.0, callback_fn=None, callback_static_args=None,
+         callback_nonstatic_args=None, *, q0=None, precision=64, device="cuda",
+         return_trace=False, return_info=False, instance=None, stream=None):
+    """cgal() of solver/cgal.py:21-243 (same positional arguments), run by the
+    device driver ``usbs_cgal_solve``.  Returns the updated SDPState; with
+    ``return_trace`` also a list of per-iteration records, with
+    ``return_info`` a dict of counters.  ``q0`` stands in for the reference's
+    ``PRNGKey(0)`` Lanczos start vector (the same one every iteration)."""
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("usbs_gb300.cgal needs a CUDA device (GB300); none is visible")
+    lib = _lib.load()
+    _sigs(lib)
+    dev = torch.device(device)
+    inst = instance if instance is not None else DeviceInstance(sdp_state, dev)
+    ld = (n + 31) // 32 * 32
+    f64 = torch.float64
+    y = _to_dev(sdp_state.y, dev).clone()
+    z = _to_dev(sdp_state.z, dev).clone()
+    if sdp_state.Omega is not None:
+        mode = 0
+        sdim = int(sdp_state.Omega.shape[1])
+        Om = _dev_cols(sdp_state.Omega, n, ld, sdim, dev, f64)
+        Pm = _dev_cols(sdp_state.P, n, ld, sdim, dev, f64)
+        X = None
+    elif sdp_state.X is not None:
+        mode, sdim = 1, 0
+        X = _to_dev(sdp_state.X, dev).clone()
+        Pm = Om = None
+    else:
+        raise ValueError("cgal needs either Omega (sketch) or X (dense) in sdp_state")
+    q0t = _to_dev(default_q0(n) if q0 is None else q0, dev)
+    trace = torch.zeros((max(max_iters, 1), TRACE_WIDTH), dtype=f64, device=dev) \
+        if return_trace else None
+    prm = CgalParams()
+    prm.trace_ub, prm.beta0, prm.max_iters = float(trace_ub), float(beta0), int(max_iters)
+    prm.max_time = float(max_time)
+    prm.obj_gap_eps, prm.infeas_gap_eps, prm.max_infeas_eps = (obj_gap_eps, infeas_gap_eps,
+                                                               max_infeas_eps)
+    prm.lanczos_inner_iterations = int(lanczos_inner_iterations)
+    prm.lanczos_max_restarts = int(lanczos_max_restarts)
+    prm.subprob_eps = float(subprob_eps)
+    prm.cond_exp_base = float(cond_exp_base)
+    prm.precision, prm.sketch_mode, prm.sketch_dim = int(precision), mode, sdim
+    pst = UsbsState()
+    pst.ld = ld
+    pst.y, pst.z, pst.V = _ptr(y), _ptr(z), None
+    pst.P, pst.Omega, pst.X, pst.q0, pst.trace = _ptr(Pm), _ptr(Om), _ptr(X), _ptr(q0t), _ptr(trace)
+    pst.trace_capacity = int(max_iters) if return_trace else 0
+    pst.debug = None
+    pst.tr_X, pst.primal_obj = float(sdp_state.tr_X), float(sdp_state.primal_obj)
+    prob = inst.c_struct()
+    need = int(lib.usbs_cgal_workspace_bytes(ctypes.byref(prob), ctypes.byref(prm)))
+    ws = torch.empty(need, dtype=torch.uint8, device=dev)
+    cb_val = {}
+
+    def _cb(_user, t):
+        if callback_fn is not None and Om is not None:
+            cb_val[t] = callback_fn(Pm[:, :n].t(), Om[:, :n].t(), callback_static_args,
+                                    callback_nonstatic_args)
+
+    ccb = CALLBACK(_cb)
+    st = stream if stream is not None else torch.cuda.current_stream(dev)
+    rc = lib.usbs_cgal_solve(ctypes.byref(prob), ctypes.byref(prm), ctypes.byref(pst), _ptr(ws),
+                             need, ccb, None, int(st.cuda_stream))
+    _lib.check(rc, "usbs_cgal_solve")
+    if pst.status & 1:
+        raise RuntimeError("usbs_cgal_solve: a device barrier timed out")
+    out = SDPState(C=sdp_state.C, A_indices=sdp_state.A_indices, A_data=sdp_state.A_data,
+                   b=sdp_state.b, b_ineq_mask=sdp_state.b_ineq_mask, X=X,
+                   P=(Pm[:, :n].t() if mode == 0 else None), Omega=sdp_state.Omega, y=y, z=z,
+                   tr_X=pst.tr_X, primal_obj=pst.primal_obj, SCALE_C=sdp_state.SCALE_C,
+                   SCALE_X=sdp_state.SCALE_X, SCALE_A=sdp_state.SCALE_A)
+    info = dict(iterations=pst.iterations, obj_gap=pst.obj_gap, infeas_gap=pst.infeas_gap,
+                max_infeas=pst.max_infeas, elapsed=pst.elapsed, status=pst.status,
+                callback_vals=cb_val, kernel_launches=pst.kernel_launches)
+    if return_trace:
+        tr = trace[:pst.iterations].cpu().numpy()
+        recs = [{f: float(r[i]) for i, f in enumerate(CGAL_TRACE_FIELDS)} for r in tr]
         return out, recs, info
     if return_info:
         return out, info
