@@ -39,6 +39,7 @@ struct IpmShared {
   double dinv[IPM_MAXS];
   double u2[IPM_MAXS], w2[IPM_MAXS];   // per-column terms of the rank-2 correction
   int cord[IPM_MAXS];                  // svec indices, off-diagonal ones first
+  double part3[3 * IPM_MAXS];          // partial sums of cta_matvec3
 };
 
 // sum_a x[a] y[a], computed redundantly by every warp (identical in all threads)
@@ -119,6 +120,88 @@ __device__ __forceinline__ double wdot(const double* x, const double* y, int s) 
 // is the ordering of |x|, so pivot comparisons stay off the FP64 pipe.
 __device__ __forceinline__ unsigned long long abs_key(double x) {
   return (unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffull;
+}
+
+// Inverse of an n x n matrix (n <= IPM_MAXK, row-major, lda = n) by Gauss-Jordan
+// elimination with partial pivoting on [A | I], whole CTA: per pivot, warp 0
+// picks the row (largest |a|, ties to the smaller index), every thread then
+// updates one or two entries of the 2n-wide augmented rows.  Per element the
+// arithmetic is that of the row-by-row algorithm (pivot row scaled by 1/a_jj,
+// a_ic - a_ij * row_c).  A is destroyed.  Returns false if a pivot is zero.
+__device__ bool cta_inverse(double* A, int n, double* Ainv, double* fcol, int* piv_s,
+                            double* inv_s) {
+  const int tid = threadIdx.x, lane = tid & 31, nt = blockDim.x;
+  for (int e = tid; e < n * n; e += nt) Ainv[e] = ((e / n) == (e % n)) ? 1.0 : 0.0;
+  bool ok = true;
+  __syncthreads();
+  for (int j = 0; j < n; ++j) {
+    if (tid < 32) {
+      unsigned long long best = 0ull;
+      int bi = 0x7fffffff;
+      if (lane >= j && lane < n) { best = abs_key(A[lane * n + j]); bi = lane; }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const unsigned long long k2 = __shfl_xor_sync(0xffffffffu, best, o);
+        const int r2 = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (r2 != 0x7fffffff && (bi == 0x7fffffff || k2 > best || (k2 == best && r2 < bi))) {
+          best = k2; bi = r2;
+        }
+      }
+      if (lane == 0) {
+        if (bi == 0x7fffffff) bi = j;
+        *piv_s = bi;
+        const double pv = A[bi * n + j];
+        *inv_s = (pv == 0.0) ? 0.0 : 1.0 / pv;
+      }
+    }
+    __syncthreads();
+    const int piv = *piv_s;
+    const double inv = *inv_s;
+    if (inv == 0.0) ok = false;
+    if (piv != j) {
+      for (int c = tid; c < 2 * n; c += nt) {
+        double* M = (c < n) ? A : Ainv;
+        const int cc = (c < n) ? c : c - n;
+        const double t = M[j * n + cc];
+        M[j * n + cc] = M[piv * n + cc];
+        M[piv * n + cc] = t;
+      }
+      __syncthreads();
+    }
+    for (int i = tid; i < n; i += nt) fcol[i] = A[i * n + j];
+    __syncthreads();
+    for (int c = tid; c < 2 * n; c += nt) {
+      double* M = (c < n) ? A : Ainv;
+      const int cc = (c < n) ? c : c - n;
+      M[j * n + cc] *= inv;
+    }
+    __syncthreads();
+    for (int e = tid; e < n * 2 * n; e += nt) {
+      const int i = e / (2 * n), c = e - i * 2 * n;
+      if (i == j) continue;
+      double* M = (c < n) ? A : Ainv;
+      const int cc = (c < n) ? c : c - n;
+      M[i * n + cc] -= fcol[i] * M[j * n + cc];
+    }
+    __syncthreads();
+  }
+  return ok;
+}
+
+// y[a] = sum_b M[a, b] x[b] (s x s, row-major) as three partial chains per row,
+// combined in a fixed order (a 66-long dependent FP64 chain costs ~4k cycles)
+__device__ void cta_matvec3(const double* M, const double* x, int s, double* part, double* y) {
+  const int tid = threadIdx.x;
+  if (tid < 3 * s) {
+    const int a = tid / 3, q = tid - 3 * (tid / 3);
+    const int b0 = (q * s) / 3, b1 = ((q + 1) * s) / 3;
+    double v = 0.0;
+    for (int b = b0; b < b1; ++b) v += M[a * s + b] * x[b];
+    part[tid] = v;
+  }
+  __syncthreads();
+  for (int a = tid; a < s; a += blockDim.x) y[a] = (part[3 * a] + part[3 * a + 1]) + part[3 * a + 2];
+  __syncthreads();
 }
 
 // LU with partial pivoting and solve, whole CTA (G&VL Alg. 3.4.1, right-looking
@@ -381,10 +464,9 @@ __global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ 
     const double k1 = sc.k1, k2 = sc.k2, den = sc.den, ze = sc.ze;
     // ---- Newton system ----
     if (A.mode == 0) {
+      cta_matvec3(Q11, sh.sS, s, sh.part3, sh.F1);
       for (int a = tid; a < s; a += IPM_BLOCK) {
-        double v = 0.0;
-        for (int b = 0; b < s; ++b) v += Q11[a * s + b] * sh.sS[b];
-        const double f = v + eta_ * sh.q12[a] + sh.h1[a];
+        const double f = sh.F1[a] + eta_ * sh.q12[a] + sh.h1[a];
         sh.F1[a] = f + (-sh.sT[a] + omega * sh.sI[a]);
       }
       if (wid == 1) {
@@ -395,11 +477,12 @@ __global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ 
         }
       }
     }
-    if (wid == 0) {   // S^-1
-      for (int e = lane; e < k * k; e += 32) sh.wk[e] = sh.S[e];
-      __syncwarp();
-      const bool okinv = warp_inverse(sh.wk, k, k, sh.Si, k);
-      if (!okinv && lane == 0) atomicOr(A.status, ST_SMALL_DENSE_FAIL);
+    // S^-1 (the reference's jnp.linalg.inv, solver/usbs.py:91)
+    for (int e = tid; e < k * k; e += IPM_BLOCK) sh.wk[e] = sh.S[e];
+    __syncthreads();
+    {
+      const bool okinv = cta_inverse(sh.wk, k, sh.Si, sh.lcol, &s_piv, sh.redv);
+      if (!okinv && tid == 0) atomicOr(A.status, ST_SMALL_DENSE_FAIL);
     }
     __syncthreads();
     const double F2 = (A.mode == 0) ? sc.F2 : 0.0;
@@ -494,14 +577,13 @@ __global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ 
     }
     __syncthreads();
     const double d_eta = sc.d_eta, d_omega = sc.d_omega;
-    for (int a = tid; a < s; a += IPM_BLOCK) {
-      if (A.mode == 0) {
-        double v = 0.0;
-        for (int b = 0; b < s; ++b) v += Q11[a * s + b] * sh.ord[b];
-        sh.dsT[a] = v + d_eta * sh.q12[a] + d_omega * sh.sI[a] + sh.F1[a];
-      } else {
+    if (A.mode == 0) {
+      cta_matvec3(Q11, sh.ord, s, sh.part3, sh.dsT);
+      for (int a = tid; a < s; a += IPM_BLOCK)
+        sh.dsT[a] = sh.dsT[a] + d_eta * sh.q12[a] + d_omega * sh.sI[a] + sh.F1[a];
+    } else {
+      for (int a = tid; a < s; a += IPM_BLOCK)
         sh.dsT[a] = d_omega * sh.sI[a] - sh.sT[a] + sh.h1[a] + omega * sh.sI[a];
-      }
     }
     __syncthreads();
     svec_inv_to(sh.ord, k, s, sh.bi, sh.ci, sh.dS);
