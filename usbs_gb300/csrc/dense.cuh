@@ -217,51 +217,64 @@ __device__ inline bool cta_jacobi_f32(float* A, int lda, int n, float* w, float*
         rs[tid] = sn;
       }
       __syncthreads();
-      // rows (J^T A): element (pair, column)
+      // J^T A J in one pass: the 16 pairs are disjoint, so the 2 x 2 block of
+      // pairs (I, J) depends only on itself; thread (I, J) applies the row
+      // rotation of I, then the column rotation of J (the operations of a
+      // row pass followed by a column pass), and Z J by (row, pair)
+      for (int e = tid; e < H * H; e += nt) {
+        const int I = e >> 4, J = e & 15;
+        const int p = pidx[2 * I], q = pidx[2 * I + 1], p2 = pidx[2 * J], q2 = pidx[2 * J + 1];
+        const float c = rc[I], sn = rs[I], c2 = rc[J], s2 = rs[J];
+        const float app = A[p * lda + p2], apq = A[p * lda + q2];
+        const float aqp = A[q * lda + p2], aqq = A[q * lda + q2];
+        // rows
+        const float bpp = c * app - sn * aqp, bpq = c * apq - sn * aqq;
+        const float bqp = sn * app + c * aqp, bqq = sn * apq + c * aqq;
+        // columns
+        A[p * lda + p2] = c2 * bpp - s2 * bpq;
+        A[p * lda + q2] = s2 * bpp + c2 * bpq;
+        A[q * lda + p2] = c2 * bqp - s2 * bqq;
+        A[q * lda + q2] = s2 * bqp + c2 * bqq;
+      }
       for (int e = tid; e < H * M; e += nt) {
         const int pr = e >> 5, j = e & 31;
         const int p = pidx[2 * pr], q = pidx[2 * pr + 1];
         const float c = rc[pr], sn = rs[pr];
-        const float ap = A[p * lda + j], aq = A[q * lda + j];
-        A[p * lda + j] = c * ap - sn * aq;
-        A[q * lda + j] = sn * ap + c * aq;
-      }
-      __syncthreads();
-      // columns (A J) and Z J: element (pair, row)
-      for (int e = tid; e < 2 * H * M; e += nt) {
-        const int which = e >> 9, pr = (e >> 5) & 15, j = e & 31;
-        const int p = pidx[2 * pr], q = pidx[2 * pr + 1];
-        const float c = rc[pr], sn = rs[pr];
-        float* B = which ? Z : A;
-        const int ldb = which ? ldz : lda;
-        const float bp = B[j * ldb + p], bq = B[j * ldb + q];
-        B[j * ldb + p] = c * bp - sn * bq;
-        B[j * ldb + q] = sn * bp + c * bq;
+        const float bp = Z[j * ldz + p], bq = Z[j * ldz + q];
+        Z[j * ldz + p] = c * bp - sn * bq;
+        Z[j * ldz + q] = sn * bp + c * bq;
       }
       __syncthreads();
     }
   }
-  // eigenvalues from the diagonal, sorted ascending with their vectors (warp 0)
-  if (wid == 0) {
-    if (lane < n) w[lane] = A[lane * lda + lane];
-    __syncwarp();
-    for (int i = 0; i < n - 1; ++i) {
-      int kmin = i;
-      float vmin = w[i];
-      for (int j = i + 1; j < n; ++j)
-        if (w[j] < vmin) { vmin = w[j]; kmin = j; }
-      if (kmin != i) {
-        const float wi = w[i];
-        __syncwarp();
-        if (lane < n) {
-          const float t = Z[lane * ldz + i];
-          Z[lane * ldz + i] = Z[lane * ldz + kmin];
-          Z[lane * ldz + kmin] = t;
-        }
-        if (lane == 0) { w[kmin] = wi; w[i] = vmin; }
-        __syncwarp();
-      }
+  // eigenvalues from the diagonal, sorted ascending with their vectors: each
+  // value's rank (ties by index) is its position; A's diagonal is no longer
+  // needed, so A's first row holds the values and A's second the ranks
+  float* wv = A;
+  int* rk = (int*)(A + lda);
+  if (tid < M) wv[tid] = (tid < n) ? A[tid * lda + tid] : 0.0f;
+  __syncthreads();
+  if (tid < n) {
+    const float v = wv[tid];
+    int r = 0;
+    for (int j = 0; j < n; ++j) {
+      const float u = wv[j];
+      r += (u < v || (u == v && j < tid)) ? 1 : 0;
     }
+    rk[tid] = r;
+    w[r] = v;
+  }
+  __syncthreads();
+  // permute Z's columns: Z[:, rank[c]] = Z_old[:, c], through A's rows 2.. as scratch
+  float* zs = A + 2 * lda;   // n x n, stride M
+  for (int e = tid; e < n * n; e += nt) {
+    const int i = e / n, c = e - (e / n) * n;
+    zs[i * M + c] = Z[i * ldz + c];
+  }
+  __syncthreads();
+  for (int e = tid; e < n * n; e += nt) {
+    const int i = e / n, c = e - (e / n) * n;
+    Z[i * ldz + rk[c]] = zs[i * M + c];
   }
   __syncthreads();
   return ok;

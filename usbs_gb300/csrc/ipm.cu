@@ -205,54 +205,72 @@ __device__ void cta_matvec3(const double* M, const double* x, int s, double* par
 }
 
 // LU with partial pivoting and solve, whole CTA (G&VL Alg. 3.4.1, right-looking
-// with a one-column look-ahead).  On GB300 a dependent FP64 operation costs
-// ~64 cycles and a division ~440, so the pivot chain of each column (argmax,
-// reciprocal, multipliers) is kept off the critical path: while warps 1..7
-// apply the rank-1 update of column j to columns j+2.., warp 0 updates column
-// j+1, picks its pivot (largest |a|, ties to the smaller row index as in
-// LAPACK), forms the pivot reciprocal and the multipliers of column j+1 and
-// applies column j to b.  Rows are swapped physically at the start of each
-// column.  L is not stored: b is eliminated alongside.  Every element sees the
-// arithmetic of the textbook algorithm (a_ic - l_i a_jc, l_i = a_ij * (1/a_jj)).
+// with a one-column look-ahead).  A is stored column-major (A[c * lda + i] is
+// row i, column c), so every column access of the pivot chain is contiguous.
+// On GB300 a dependent FP64 operation costs ~64 cycles and a division ~440,
+// so the pivot chain of each column is kept off the critical path: while warps
+// 1..7 apply the rank-1 update of column j to columns j+2.., warp 0 updates
+// column j+1 and b (lane q of warp 0 holds rows j+1+q, j+33+q, j+65+q in
+// registers), picks the next pivot (largest |a|, ties to the smaller row index
+// as in LAPACK) from those registers, forms its reciprocal and the next
+// multipliers.  Rows are swapped physically at the start of each column.  L is
+// not stored: b is eliminated alongside.  Every element sees the arithmetic of
+// the textbook algorithm (a_ic - l_i a_jc, l_i = a_ij * (1/a_jj)).
+constexpr int LU_RPL = (IPM_MAXS + 31) / 32;   // rows per lane of warp 0
 __device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* dinv, double* lcol,
                              int* piv_out, int* ok_out) {
   const int tid = threadIdx.x, lane = tid & 31;
   __shared__ double lnext[IPM_MAXS];
   __shared__ int pnext[2];   // pivot of column j in pnext[j & 1] (written one column ahead)
-  double* lc = lcol;      // multipliers of the current column (indexed by row)
-  double* ln = lnext;     // multipliers of the next column
-  // look-ahead for column 0 (warp 0): pivot, reciprocal, multipliers
-  auto pick = [&](int j, double* lout) {
-    // rows j..n-1 of column j are final; lane q holds rows j+q, j+q+32, ...
+  double* lc = lcol;         // multipliers of the current column (indexed by row)
+  double* ln = lnext;        // multipliers of the next column
+  // warp 0: rows r = j + lane + 32 q of column j are in v[q]; pivot, reciprocal
+  // and multipliers of column j
+  auto pick = [&](int j, const double (&v)[LU_RPL], double* lout) {
     unsigned long long best = 0ull;
     int bi = 0x7fffffff;
-    for (int i = j + lane; i < n; i += 32) {
-      const unsigned long long kk = abs_key(A[i * lda + j]);
-      if (bi == 0x7fffffff || kk > best) { best = kk; bi = i; }
+    double bv = 0.0;
+#pragma unroll
+    for (int q = 0; q < LU_RPL; ++q) {
+      const int i = j + lane + 32 * q;
+      if (i < n) {
+        const unsigned long long kk = abs_key(v[q]);
+        if (bi == 0x7fffffff || kk > best) { best = kk; bi = i; bv = v[q]; }
+      }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       const unsigned long long k2 = __shfl_xor_sync(0xffffffffu, best, o);
       const int r2 = __shfl_xor_sync(0xffffffffu, bi, o);
+      const double v2 = __shfl_xor_sync(0xffffffffu, bv, o);
       if (r2 != 0x7fffffff && (bi == 0x7fffffff || k2 > best || (k2 == best && r2 < bi))) {
-        best = k2; bi = r2;
+        best = k2; bi = r2; bv = v2;
       }
     }
-    if (bi == 0x7fffffff) bi = j;
-    const double pv = A[bi * lda + j];
-    const double inv = (pv == 0.0) ? 1.0 : 1.0 / pv;
-    // multipliers of rows j..n-1 as they sit now; the pivot row's entry is
-    // moved to row j by the swap at the start of column j
-    for (int i = j + lane; i < n; i += 32) lout[i] = A[i * lda + j] * inv;
+    if (bi == 0x7fffffff) { bi = j; bv = A[j * lda + j]; }
+    const double inv = (bv == 0.0) ? 1.0 : 1.0 / bv;
+#pragma unroll
+    for (int q = 0; q < LU_RPL; ++q) {
+      const int i = j + lane + 32 * q;
+      if (i < n) lout[i] = v[q] * inv;
+    }
     if (lane == 0) {
       pnext[j & 1] = bi;
       dinv[j] = inv;
-      if (pv == 0.0) *ok_out = 0;
+      if (bv == 0.0) *ok_out = 0;
     }
   };
   if (tid == 0) *ok_out = 1;
   __syncthreads();
-  if (tid < 32) pick(0, lc);
+  if (tid < 32) {
+    double v[LU_RPL];
+#pragma unroll
+    for (int q = 0; q < LU_RPL; ++q) {
+      const int i = lane + 32 * q;
+      v[q] = (i < n) ? A[i] : 0.0;
+    }
+    pick(0, v, lc);
+  }
   __syncthreads();
   for (int j = 0; j < n; ++j) {
     const int piv = pnext[j & 1];
@@ -260,9 +278,9 @@ __device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* dinv,
     // swap rows j and piv (columns j.., b and the multipliers of column j)
     if (piv != j) {
       for (int c = j + tid; c < n; c += blockDim.x) {
-        const double t = A[j * lda + c];
-        A[j * lda + c] = A[piv * lda + c];
-        A[piv * lda + c] = t;
+        const double t = A[c * lda + j];
+        A[c * lda + j] = A[c * lda + piv];
+        A[c * lda + piv] = t;
       }
       if (tid == 0) {
         const double t = b[j]; b[j] = b[piv]; b[piv] = t;
@@ -273,25 +291,39 @@ __device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* dinv,
     const int w = n - j - 1;
     if (w == 0) break;
     if (tid < 32) {
-      // column j+1 of rows j+1.., then b, then the look-ahead of column j+1
-      const double ujn = A[j * lda + j + 1];
-      for (int i = j + 1 + lane; i < n; i += 32)
-        A[i * lda + j + 1] = A[i * lda + j + 1] - lc[i] * ujn;
-      const double bj = b[j];
-      for (int i = j + 1 + lane; i < n; i += 32) b[i] -= lc[i] * bj;
-      __syncwarp();
-      pick(j + 1, ln);
+      // column j+1 and b for rows j+1.. (all loads first), then the look-ahead
+      const double* colj1 = A + (size_t)(j + 1) * lda;
+      const double ujn = colj1[j], bj = b[j];
+      double a[LU_RPL], l[LU_RPL], bb[LU_RPL];
+#pragma unroll
+      for (int q = 0; q < LU_RPL; ++q) {
+        const int i = j + 1 + lane + 32 * q;
+        a[q] = (i < n) ? colj1[i] : 0.0;
+        l[q] = (i < n) ? lc[i] : 0.0;
+        bb[q] = (i < n) ? b[i] : 0.0;
+      }
+      double v[LU_RPL];
+#pragma unroll
+      for (int q = 0; q < LU_RPL; ++q) {
+        const int i = j + 1 + lane + 32 * q;
+        v[q] = a[q] - l[q] * ujn;
+        if (i < n) {
+          A[(size_t)(j + 1) * lda + i] = v[q];
+          b[i] = bb[q] - l[q] * bj;
+        }
+      }
+      pick(j + 1, v, ln);
     } else if (w > 1) {
-      // columns j+2.. of rows j+1..: flat over warps 1..7
+      // columns j+2.. of rows j+1..: flat over warps 1..7, lanes along rows
       const int nt = (int)blockDim.x - 32, t = tid - 32;
-      const int ncol = w - 1;
-      const int rpp = nt / ncol;
-      const int rr = t / ncol, c = j + 2 + (t - (t / ncol) * ncol);
-      if (rr < rpp && rr < w) {
-        const double u = A[j * lda + c];
-        for (int r = rr; r < w; r += rpp) {
-          const int i = j + 1 + r;
-          A[i * lda + c] = A[i * lda + c] - lc[i] * u;
+      const int cpp = nt / w;                 // columns per pass
+      const int cc = t / w, r = t - (t / w) * w;
+      if (cc < cpp) {
+        const int i = j + 1 + r;
+        const double li = lc[i];
+        for (int c = j + 2 + cc; c < n; c += cpp) {
+          double* col = A + (size_t)c * lda;
+          col[i] = col[i] - li * col[j];
         }
       }
     }
@@ -303,30 +335,30 @@ __device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* dinv,
   // x_j = b_j * (1 / u_jj) with the pivot reciprocal of the factorisation (as
   // the multipliers), then every lane updates its rows above j.
   if (tid < 32) {
-    constexpr int NB = (IPM_MAXS + 31) / 32;
-    double br[NB];
+    double br[LU_RPL];
 #pragma unroll
-    for (int q = 0; q < NB; ++q) br[q] = (lane + 32 * q < n) ? b[lane + 32 * q] : 0.0;
+    for (int q = 0; q < LU_RPL; ++q) br[q] = (lane + 32 * q < n) ? b[lane + 32 * q] : 0.0;
     for (int j = n - 1; j >= 0; --j) {
       const int oq = j >> 5, ol = j & 31;
       double bj = 0.0;
 #pragma unroll
-      for (int q = 0; q < NB; ++q) if (q == oq) bj = br[q];
+      for (int q = 0; q < LU_RPL; ++q) if (q == oq) bj = br[q];
       bj = __shfl_sync(0xffffffffu, bj, ol) * dinv[j];
+      const double* colj = A + (size_t)j * lda;
 #pragma unroll
-      for (int q = 0; q < NB; ++q) {
+      for (int q = 0; q < LU_RPL; ++q) {
         const int i = lane + 32 * q;
         if (i == j) br[q] = bj;
-        else if (i < j) br[q] -= A[i * lda + j] * bj;
+        else if (i < j) br[q] -= colj[i] * bj;
       }
     }
 #pragma unroll
-    for (int q = 0; q < NB; ++q) if (lane + 32 * q < n) b[lane + 32 * q] = br[q];
+    for (int q = 0; q < LU_RPL; ++q) if (lane + 32 * q < n) b[lane + 32 * q] = br[q];
   }
   __syncthreads();
 }
 
-__global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ IpmArgs A) {
+__global__ void __launch_bounds__(IPM_BLOCK, 1) ipm_kernel(const __grid_constant__ IpmArgs A) {
   extern __shared__ double dyn[];
   __shared__ IpmShared sh;
   __shared__ IpmScal sc;
@@ -501,8 +533,10 @@ __global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ 
     }
     // every entry of the s x s matrix, flat over the CTA; columns in cord order
     // so that the off-diagonal / diagonal branch is uniform across most warps
+    // (stored column-major for the LU: coeff[a2 * s + a] is row a, column a2;
+    // consecutive threads take consecutive rows of one column)
     for (int e = tid; e < s * s; e += IPM_BLOCK) {
-      const int a = e / s, a2 = sh.cord[e - a * s];
+      const int ca = e / s, a = e - ca * s, a2 = sh.cord[ca];
       double v = symkron_sum(sh.T, sh.Si, k, sh.bi[a], sh.ci[a], sh.bi[a2], sh.ci[a2]);
       if (A.mode == 0) {
         v = Q11[a * s + a2] + v;
@@ -510,7 +544,7 @@ __global__ void __launch_bounds__(IPM_BLOCK) ipm_kernel(const __grid_constant__ 
       } else {
         v += lbc * (sh.sI[a] * sh.sI[a2]);
       }
-      coeff[a * s + a2] = v;
+      coeff[a2 * s + a] = v;
     }
     if (tid == 0) {
       if (A.mode == 0) {
