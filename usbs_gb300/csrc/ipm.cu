@@ -209,13 +209,14 @@ __device__ void cta_matvec3(const double* M, const double* x, int s, double* par
 // row i, column c), so every column access of the pivot chain is contiguous.
 // On GB300 a dependent FP64 operation costs ~64 cycles and a division ~440,
 // so the pivot chain of each column is kept off the critical path: while warps
-// 1..7 apply the rank-1 update of column j to columns j+2.., warp 0 updates
-// column j+1 and b (lane q of warp 0 holds rows j+1+q, j+33+q, j+65+q in
-// registers), picks the next pivot (largest |a|, ties to the smaller row index
-// as in LAPACK) from those registers, forms its reciprocal and the next
-// multipliers.  Rows are swapped physically at the start of each column.  L is
-// not stored: b is eliminated alongside.  Every element sees the arithmetic of
-// the textbook algorithm (a_ic - l_i a_jc, l_i = a_ij * (1/a_jj)).
+// 1..7 eliminate b and apply the rank-1 update of column j to columns j+2..,
+// warp 0 updates column j+1 (lane q holds rows j+1+q, j+33+q, j+65+q in
+// registers), picks the next pivot from those registers (largest |a|, ties to
+// the smaller row index as in LAPACK; warp reduction instructions on the
+// integer keys of |a|), forms its reciprocal and the next multipliers.  Rows
+// are swapped physically at the start of each column.  L is not stored: b is
+// eliminated alongside.  Every element sees the arithmetic of the textbook
+// algorithm (a_ic - l_i a_jc, l_i = a_ij * (1/a_jj)).
 constexpr int LU_RPL = (IPM_MAXS + 31) / 32;   // rows per lane of warp 0
 __device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* dinv, double* lcol,
                              int* piv_out, int* ok_out) {
@@ -227,27 +228,37 @@ __device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* dinv,
   // warp 0: rows r = j + lane + 32 q of column j are in v[q]; pivot, reciprocal
   // and multipliers of column j
   auto pick = [&](int j, const double (&v)[LU_RPL], double* lout) {
+    // lane-local candidate: largest |a| key, smallest row among equal keys
     unsigned long long best = 0ull;
     int bi = 0x7fffffff;
-    double bv = 0.0;
 #pragma unroll
     for (int q = 0; q < LU_RPL; ++q) {
       const int i = j + lane + 32 * q;
       if (i < n) {
         const unsigned long long kk = abs_key(v[q]);
-        if (bi == 0x7fffffff || kk > best) { best = kk; bi = i; bv = v[q]; }
+        if (bi == 0x7fffffff || kk > best) { best = kk; bi = i; }
       }
     }
+    // warp argmax by reduction instructions: high word, then low word among
+    // the lanes holding the top high word, then the smallest row among ties
+    const unsigned hi = (unsigned)(best >> 32), lo = (unsigned)best;
+    const unsigned mhi = __reduce_max_sync(0xffffffffu, hi);
+    const bool th = (bi != 0x7fffffff) && hi == mhi;
+    const unsigned mlo = __reduce_max_sync(0xffffffffu, th ? lo : 0u);
+    const bool tl = th && lo == mlo;
+    const unsigned mrow = __reduce_min_sync(0xffffffffu, tl ? (unsigned)bi : 0xffffffffu);
+    double bv;
+    if (mrow == 0xffffffffu) {
+      bi = j;
+      bv = A[(size_t)j * lda + j];
+    } else {
+      bi = (int)mrow;
+      const int off = bi - j;           // the row's owner lane and register
+      double sel = 0.0;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const unsigned long long k2 = __shfl_xor_sync(0xffffffffu, best, o);
-      const int r2 = __shfl_xor_sync(0xffffffffu, bi, o);
-      const double v2 = __shfl_xor_sync(0xffffffffu, bv, o);
-      if (r2 != 0x7fffffff && (bi == 0x7fffffff || k2 > best || (k2 == best && r2 < bi))) {
-        best = k2; bi = r2; bv = v2;
-      }
+      for (int q = 0; q < LU_RPL; ++q) if (q == (off >> 5)) sel = v[q];
+      bv = __shfl_sync(0xffffffffu, sel, off & 31);
     }
-    if (bi == 0x7fffffff) { bi = j; bv = A[j * lda + j]; }
     const double inv = (bv == 0.0) ? 1.0 : 1.0 / bv;
 #pragma unroll
     for (int q = 0; q < LU_RPL; ++q) {
@@ -291,31 +302,33 @@ __device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* dinv,
     const int w = n - j - 1;
     if (w == 0) break;
     if (tid < 32) {
-      // column j+1 and b for rows j+1.. (all loads first), then the look-ahead
+      // column j+1 for rows j+1.. (all loads first), then the look-ahead
       const double* colj1 = A + (size_t)(j + 1) * lda;
-      const double ujn = colj1[j], bj = b[j];
-      double a[LU_RPL], l[LU_RPL], bb[LU_RPL];
+      const double ujn = colj1[j];
+      double a[LU_RPL], l[LU_RPL];
 #pragma unroll
       for (int q = 0; q < LU_RPL; ++q) {
         const int i = j + 1 + lane + 32 * q;
         a[q] = (i < n) ? colj1[i] : 0.0;
         l[q] = (i < n) ? lc[i] : 0.0;
-        bb[q] = (i < n) ? b[i] : 0.0;
       }
       double v[LU_RPL];
 #pragma unroll
       for (int q = 0; q < LU_RPL; ++q) {
         const int i = j + 1 + lane + 32 * q;
         v[q] = a[q] - l[q] * ujn;
-        if (i < n) {
-          A[(size_t)(j + 1) * lda + i] = v[q];
-          b[i] = bb[q] - l[q] * bj;
-        }
+        if (i < n) A[(size_t)(j + 1) * lda + i] = v[q];
       }
       pick(j + 1, v, ln);
-    } else if (w > 1) {
-      // columns j+2.. of rows j+1..: flat over warps 1..7, lanes along rows
+    } else {
       const int nt = (int)blockDim.x - 32, t = tid - 32;
+      // b for rows j+1.. (forward elimination of the right-hand side)
+      if (t < w) {
+        const int i = j + 1 + t;
+        b[i] = b[i] - lc[i] * b[j];
+      }
+      if (w > 1) {
+      // columns j+2.. of rows j+1..: flat over warps 1..7, lanes along rows
       const int cpp = nt / w;                 // columns per pass
       const int cc = t / w, r = t - (t / w) * w;
       if (cc < cpp) {
@@ -325,6 +338,7 @@ __device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* dinv,
           double* col = A + (size_t)c * lda;
           col[i] = col[i] - li * col[j];
         }
+      }
       }
     }
     __syncthreads();
