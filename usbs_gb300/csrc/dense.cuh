@@ -154,28 +154,30 @@ __device__ inline bool warp_syev(double* A, int lda, int n, double* w, double* Z
 }
 
 // Cyclic parallel Jacobi eigensolver (float) for a symmetric n x n matrix, run
-// by a whole CTA (blockDim a multiple of 32, >= 64) at order 32 (indices >= n
-// are padding that couples to nothing): 16 disjoint rotations per round in
+// by a whole CTA (blockDim a multiple of 32, >= 64) at order M (32 or 16;
+// indices >= n are padding that couples to nothing): M/2 disjoint rotations per round in
 // round-robin ("chess tournament") order, Rutishauser's rotation formulas,
 // sweeps until the off-diagonal Frobenius norm is below 4 eps ||A||_F.  Each
 // round: threads 0-15 form the rotations, then the 512 row updates and the
-// 1024 column updates (A and Z) are spread over the CTA.  A (row-major,
-// lda >= 32) is destroyed; w receives the eigenvalues ascending, Z (row-major,
-// ldz >= 32) the eigenvectors as columns.  Returns false (uniformly) if 20
-// sweeps do not converge.  pidx needs 32 ints, rc/rs 16 floats, red 32 floats.
+// column updates (A and Z) are spread over the CTA.  A (row-major, lda >= M,
+// room for 2 lda + n M floats) is destroyed; w receives the eigenvalues
+// ascending, Z (row-major, ldz >= M) the eigenvectors as columns.  Returns
+// false (uniformly) if 20 sweeps do not converge.  pidx needs M ints, rc/rs
+// M/2 floats, red 32 floats.
+template <int M>
 __device__ inline bool cta_jacobi_f32(float* A, int lda, int n, float* w, float* Z, int ldz,
                                       int* pidx, float* rc, float* rs, float* red) {
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5;
-  constexpr int M = 32, H = 16;
+  constexpr int H = M / 2;
   for (int e = tid; e < M * M; e += nt) {
-    const int i = e >> 5, j = e & 31;
+    const int i = e / M, j = e % M;
     Z[i * ldz + j] = (i == j) ? 1.0f : 0.0f;
     if (i >= n || j >= n) A[i * lda + j] = 0.0f;
   }
   __syncthreads();
   if (wid == 0) {
     float fro = 0.0f;
-    for (int i = 0; i < M; ++i) { const float a = A[i * lda + lane]; fro += a * a; }
+    for (int i = 0; i < M; ++i) { const float a = (lane < M) ? A[i * lda + lane] : 0.0f; fro += a * a; }
     fro = warp_sum(fro);
     if (lane == 0) red[0] = fro * (4.0f * 1.2e-7f) * (4.0f * 1.2e-7f);
   }
@@ -186,7 +188,7 @@ __device__ inline bool cta_jacobi_f32(float* A, int lda, int n, float* w, float*
     if (wid == 0) {
       float off = 0.0f;
       for (int i = 0; i < M; ++i) {
-        const float a = (lane != i) ? A[i * lda + lane] : 0.0f;
+        const float a = (lane < M && lane != i) ? A[i * lda + lane] : 0.0f;
         off += a * a;
       }
       off = warp_sum(off);
@@ -222,7 +224,7 @@ __device__ inline bool cta_jacobi_f32(float* A, int lda, int n, float* w, float*
       // rotation of I, then the column rotation of J (the operations of a
       // row pass followed by a column pass), and Z J by (row, pair)
       for (int e = tid; e < H * H; e += nt) {
-        const int I = e >> 4, J = e & 15;
+        const int I = e / H, J = e % H;
         const int p = pidx[2 * I], q = pidx[2 * I + 1], p2 = pidx[2 * J], q2 = pidx[2 * J + 1];
         const float c = rc[I], sn = rs[I], c2 = rc[J], s2 = rs[J];
         const float app = A[p * lda + p2], apq = A[p * lda + q2];
@@ -237,7 +239,7 @@ __device__ inline bool cta_jacobi_f32(float* A, int lda, int n, float* w, float*
         A[q * lda + q2] = s2 * bqp + c2 * bqq;
       }
       for (int e = tid; e < H * M; e += nt) {
-        const int pr = e >> 5, j = e & 31;
+        const int pr = e / M, j = e % M;
         const int p = pidx[2 * pr], q = pidx[2 * pr + 1];
         const float c = rc[pr], sn = rs[pr];
         const float bp = Z[j * ldz + p], bq = Z[j * ldz + q];

@@ -743,29 +743,64 @@ __global__ void __launch_bounds__(IPM_BLOCK, 1) ipm_kernel(const __grid_constant
 }
 
 // eigh(S) and the quantities the outer iteration derives from it.  One warp.
-__global__ void eigS_kernel(EigSArgs A) {
+__global__ void __launch_bounds__(IPM_BLOCK) eigS_kernel(EigSArgs A) {
   if (A.skip && *A.skip) return;
-  __shared__ double Sw[IPM_MAXK * (IPM_MAXK + 1)], Z[IPM_MAXK * (IPM_MAXK + 1)], lam[IPM_MAXK];
-  __shared__ double GW[IPM_MAXK * IPM_MAXK];
-  const int k = A.k, kc = A.k_curr, lane = threadIdx.x;
+  constexpr int L = 16;                               // ld of the FP64 k x k blocks
+  __shared__ double Sd[L * L], Z[L * L], R[L * L], S2[L * L], Wb[L * L], lam[L];
+  __shared__ double GW[IPM_MAXK * IPM_MAXK], red[IPM_BLOCK / 32];
+  __shared__ float Af[2 * (L + 1) + L * L + L], Zf[L * (L + 1)], wf[L], rcf[L], rsf[L], redf[32];
+  __shared__ int pidx[L], order[L];
+  const int k = A.k, kc = A.k_curr, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   double* sm = A.smalls;
   const double* S = sm + A.o_Sout;
-  for (int e = lane; e < k * k; e += 32) Sw[(e / k) * (IPM_MAXK + 1) + e % k] = S[e];
-  __syncwarp();
-  bool ok = warp_syev(Sw, IPM_MAXK + 1, k, lam, Z, IPM_MAXK + 1);
-  if (!ok && lane == 0) atomicOr(A.status, ST_SMALL_DENSE_FAIL);
-  __syncwarp();
-  if (lane < k) lam[lane] = fmax(lam[lane], 0.0);   // clip(eigvals, 0)
-  __syncwarp();
+  // eigh(S) (solver/usbs.py:568): FP32 parallel Jacobi at order 16, refined to
+  // FP64 accuracy by two Ogita-Aishima steps, then sorted ascending
+  for (int e = tid; e < k * k; e += IPM_BLOCK) {
+    const int r = e / k, c = e - r * k;
+    Sd[r * L + c] = S[e];
+    Af[r * (L + 1) + c] = (float)S[e];
+  }
+  __syncthreads();
+  bool ok = cta_jacobi_f32<L>(Af, L + 1, k, wf, Zf, L + 1, pidx, rcf, rsf, redf);
+  for (int e = tid; e < k * k; e += IPM_BLOCK) {
+    const int r = e / k, c = e - r * k;
+    Z[r * L + c] = (double)Zf[r * (L + 1) + c];
+  }
+  __syncthreads();
+  cta_refine_eig(Sd, Z, R, S2, Wb, lam, red, k, L);
+  cta_refine_eig(Sd, Z, R, S2, Wb, lam, red, k, L);
+  if (tid < k) {
+    const double v = lam[tid];
+    int r = 0;
+    for (int j = 0; j < k; ++j) {
+      const double u = lam[j];
+      r += (u < v || (u == v && j < tid)) ? 1 : 0;
+    }
+    order[r] = tid;
+  }
+  __syncthreads();
+  for (int e = tid; e < k * k; e += IPM_BLOCK) {
+    const int r = e / k, c = e - r * k;
+    S2[r * L + c] = Z[r * L + order[c]];
+  }
+  double lv = (tid < k) ? lam[order[tid]] : 0.0;
+  __syncthreads();
+  for (int e = tid; e < k * k; e += IPM_BLOCK) {
+    const int r = e / k, c = e - r * k;
+    Z[r * L + c] = S2[r * L + c];
+  }
+  if (tid < k) lam[tid] = fmax(lv, 0.0);   // clip(eigvals, 0)
+  if (!ok && tid == 0) atomicOr(A.status, ST_SMALL_DENSE_FAIL);
+  __syncthreads();
   double* W = sm + A.o_W;
   double* Sp = sm + A.o_Splus;
   double* Scp = sm + A.o_Scplus;
-  for (int e = lane; e < k * k; e += 32) {
+  for (int e = tid; e < k * k; e += IPM_BLOCK) {
     const int r = e / k, c = e - r * k;
-    W[e] = Z[r * (IPM_MAXK + 1) + c];
+    W[e] = Z[r * L + c];
     double a = 0.0, b = 0.0;
     for (int j = 0; j < k; ++j) {
-      const double t = Z[r * (IPM_MAXK + 1) + j] * lam[j] * Z[c * (IPM_MAXK + 1) + j];
+      const double t = Z[r * L + j] * lam[j] * Z[c * L + j];
       a += t;
       if (j < kc) b += t;
     }
@@ -774,40 +809,42 @@ __global__ void eigS_kernel(EigSArgs A) {
   }
   // trace(F^T C F) = sum_j lam_j (W^T G_C W)_jj
   const double* GC = sm + A.o_GC;
-  for (int e = lane; e < k * k; e += 32) {
+  for (int e = tid; e < k * k; e += IPM_BLOCK) {
     const int r = e / k, j = e - r * k;
     double v = 0.0;
-    for (int c = 0; c < k; ++c) v += GC[r * k + c] * Z[c * (IPM_MAXK + 1) + j];
+    for (int c = 0; c < k; ++c) v += GC[r * k + c] * Z[c * L + j];
     GW[e] = v;   // (G_C W)[r][j]
   }
-  __syncwarp();
-  double pj = 0.0;
-  if (lane < k) {
-    for (int r = 0; r < k; ++r) pj += Z[r * (IPM_MAXK + 1) + lane] * GW[r * k + lane];
-    pj *= lam[lane];
-  }
-  double pall = warp_sum(pj);
-  double pcur = warp_sum(lane < kc ? pj : 0.0);
-  double lc = warp_sum(lane < kc ? lam[lane] : 0.0);
-  if (lane == 0) {
-    double trS = 0.0;
-    for (int b = 0; b < k; ++b) trS += S[b * k + b];
-    sm[A.o_sc + SC_TRS] = trS;
-    sm[A.o_sc + SC_SUMLAMC] = lc;
-    sm[A.o_sc + SC_PFULL] = pall;
-    sm[A.o_sc + SC_PCUR] = pcur;
+  __syncthreads();
+  if (wid == 0) {
+    double pj = 0.0;
+    if (lane < k) {
+      for (int r = 0; r < k; ++r) pj += Z[r * L + lane] * GW[r * k + lane];
+      pj *= lam[lane];
+    }
+    const double pall = warp_sum(pj);
+    const double pcur = warp_sum(lane < kc ? pj : 0.0);
+    const double lc = warp_sum(lane < kc ? lam[lane] : 0.0);
+    if (lane == 0) {
+      double trS = 0.0;
+      for (int b = 0; b < k; ++b) trS += S[b * k + b];
+      sm[A.o_sc + SC_TRS] = trS;
+      sm[A.o_sc + SC_SUMLAMC] = lc;
+      sm[A.o_sc + SC_PFULL] = pall;
+      sm[A.o_sc + SC_PCUR] = pcur;
+    }
   }
   // W_past = W[:, kc:]
   const int kp = k - kc;
-  for (int e = lane; e < k * kp; e += 32) {
+  for (int e = tid; e < k * kp; e += IPM_BLOCK) {
     const int r = e / kp, c = e - r * kp;
-    sm[A.o_Wpast + e] = Z[r * (IPM_MAXK + 1) + kc + c];
+    sm[A.o_Wpast + e] = Z[r * L + kc + c];
   }
   // M = S+ (V^T Omega), Mc = Sc+ (V^T Omega)    (k x ssk)
   if (A.ssk > 0) {
+    __syncthreads();
     const double* VtO = sm + A.o_VtO;
-    __syncwarp();
-    for (int e = lane; e < k * A.ssk; e += 32) {
+    for (int e = tid; e < k * A.ssk; e += IPM_BLOCK) {
       const int r = e / A.ssk, c = e - r * A.ssk;
       double a = 0.0, b = 0.0;
       for (int j = 0; j < k; ++j) {
@@ -820,10 +857,14 @@ __global__ void eigS_kernel(EigSArgs A) {
   }
 }
 
-// One pass of (shifted) Cholesky QR: R^T R = G (+ shift I), output R^-1 (upper).
+// One pass of (shifted) Cholesky QR: R^T R = G (+ shift I), output R^-1
+// (upper), one warp.  Column j of R: lanes i >= j form G_ji - sum_p R_pj R_pi,
+// lane j's value gives r_jj = sqrt(.), the others are scaled by 1 / r_jj.
+// R^-1 by back substitution with one lane per column (reciprocals of the
+// diagonal computed once).
 __global__ void cholqr_kernel(CholQRArgs A) {
   if (A.skip && *A.skip) return;
-  __shared__ double R[IPM_MAXK * IPM_MAXK], Ri[IPM_MAXK * IPM_MAXK];
+  __shared__ double R[IPM_MAXK * IPM_MAXK], Ri[IPM_MAXK * IPM_MAXK], rd[IPM_MAXK];
   const int k = A.k, lane = threadIdx.x;
   double* sm = A.smalls;
   const double* G = sm + A.o_G;
@@ -834,31 +875,32 @@ __global__ void cholqr_kernel(CholQRArgs A) {
     // Fukaya et al. (SIAM J. Sci. Comput. 42(1), 2020): s = 11 (m n + n (n + 1)) u ||A||_2^2
     shift = 11.0 * ((double)A.n * k + (double)k * (k + 1)) * 1.1102230246251565e-16 * tr;
   }
-  if (lane == 0) {
-    bool ok = true;
-    for (int j = 0; j < k; ++j) {
-      double d = G[j * k + j] + shift;
-      for (int p = 0; p < j; ++p) d -= R[p * k + j] * R[p * k + j];
-      if (!(d > 0.0)) { ok = false; d = 1.0; }
-      const double rjj = sqrt(d);
-      R[j * k + j] = rjj;
-      for (int i = j + 1; i < k; ++i) {
-        double v = G[j * k + i];
-        for (int p = 0; p < j; ++p) v -= R[p * k + j] * R[p * k + i];
-        R[j * k + i] = v / rjj;
-      }
-      for (int i = 0; i < j; ++i) R[j * k + i] = 0.0;
+  for (int e = lane; e < k * k; e += 32) R[e] = 0.0;
+  __syncwarp();
+  bool ok = true;
+  for (int j = 0; j < k; ++j) {
+    double v = 0.0;
+    if (lane >= j && lane < k) {
+      v = G[j * k + lane] + ((lane == j) ? shift : 0.0);
+      for (int p = 0; p < j; ++p) v -= R[p * k + j] * R[p * k + lane];
     }
-    // R^-1 (upper triangular) by back substitution, column by column
-    for (int c = 0; c < k; ++c) {
-      for (int r = k - 1; r >= 0; --r) {
-        double v = (r == c) ? 1.0 : 0.0;
-        for (int p = r + 1; p < k; ++p) v -= R[r * k + p] * Ri[p * k + c];
-        Ri[r * k + c] = (r > c) ? 0.0 : v / R[r * k + r];
-      }
-    }
-    if (!ok) atomicOr(A.status, ST_SMALL_DENSE_FAIL);
+    double d = __shfl_sync(0xffffffffu, v, j);
+    if (!(d > 0.0)) { ok = false; d = 1.0; }
+    const double rjj = sqrt(d);
+    const double inv = 1.0 / rjj;
+    if (lane == j) { R[j * k + j] = rjj; rd[j] = inv; }
+    else if (lane > j && lane < k) R[j * k + lane] = v * inv;
+    __syncwarp();
   }
+  if (lane < k) {
+    const int c = lane;
+    for (int r = k - 1; r >= 0; --r) {
+      double v = (r == c) ? 1.0 : 0.0;
+      for (int p = r + 1; p <= c; ++p) v -= R[r * k + p] * Ri[p * k + c];
+      Ri[r * k + c] = (r > c) ? 0.0 : v * rd[r];
+    }
+  }
+  if (!ok && lane == 0) atomicOr(A.status, ST_SMALL_DENSE_FAIL);
   __syncwarp();
   for (int e = lane; e < k * k; e += 32) sm[A.o_Rinv + e] = Ri[e];
 }
@@ -879,7 +921,7 @@ int launch_ipm(const IpmArgs& a, cudaStream_t st) {
 }
 
 int launch_eigS(const EigSArgs& a, cudaStream_t st) {
-  eigS_kernel<<<1, 32, 0, st>>>(a);
+  eigS_kernel<<<1, IPM_BLOCK, 0, st>>>(a);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) { set_error("eigS launch: %s", cudaGetErrorString(e)); return -5; }
   return 0;

@@ -357,7 +357,7 @@ __device__ void restart_select(const D& P, LzShared<VT>& sh, int k, bool write_o
   // eigh(T) (solver/lanczos.py:203): FP32 parallel Jacobi by the CTA ...
   {
     const long long c0 = clock64();
-    const bool ok = cta_jacobi_f32(Tf, MP1, m, sh.wf, Zf, MP1, sh.pidx, sh.rc, sh.rsn, sh.redf);
+    const bool ok = cta_jacobi_f32<32>(Tf, MP1, m, sh.wf, Zf, MP1, sh.pidx, sh.rc, sh.rsn, sh.redf);
     if (tid == 0) sh.eig_cycles += clock64() - c0;
     if (!ok && tid == 0) atomicOr(P.status, ST_SMALL_DENSE_FAIL);
   }

@@ -82,10 +82,20 @@ __global__ void __launch_bounds__(RED_BLOCK) gram_kernel(GramArgs a) {
   __syncthreads();
   if (!last) return;
   __threadfence();
+  // four interleaved chains over the blocks, combined in a fixed order (a
+  // single chain of dependent FP64 adds costs ~64 cycles per block)
+  const int nb = (int)gridDim.x;
   for (int e = tid; e < E; e += RED_BLOCK) {
-    double s = 0.0;
-    for (int b = 0; b < (int)gridDim.x; ++b) s += __ldcg(a.partial + (size_t)b * E + e);
-    a.out[e] = s;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    int b = 0;
+    for (; b + 3 < nb; b += 4) {
+      s0 += __ldcg(a.partial + (size_t)b * E + e);
+      s1 += __ldcg(a.partial + (size_t)(b + 1) * E + e);
+      s2 += __ldcg(a.partial + (size_t)(b + 2) * E + e);
+      s3 += __ldcg(a.partial + (size_t)(b + 3) * E + e);
+    }
+    for (; b < nb; ++b) s0 += __ldcg(a.partial + (size_t)b * E + e);
+    a.out[e] = (s0 + s1) + (s2 + s3);
   }
   if (tid == 0) *a.counter = 0u;
 }
@@ -712,7 +722,12 @@ struct Solver {
     a.out = out; a.skip = nullptr;
     cudaStream_t st = side ? st2 : this->st;
     ++launches;
-    int blocks = (n + GR_ROWS - 1) / GR_ROWS;
+    // blocks by work, about 16k FMAs each (few blocks keep the final sum of
+    // the per-block partials short), at most grid_gram
+    const long long work = (long long)n * kx * ky;
+    int blocks = (int)((work + 16383) / 16384);
+    const int tiles = (n + GR_ROWS - 1) / GR_ROWS;
+    if (blocks > tiles) blocks = tiles;
     if (blocks > L.grid_gram) blocks = L.grid_gram;
     if (blocks < 1) blocks = 1;
     if (kx * ky <= RED_BLOCK) gram_kernel<1><<<blocks, RED_BLOCK, 0, st>>>(a);
