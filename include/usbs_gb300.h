@@ -63,6 +63,23 @@ int usbs_operator_apply(int n, long long nnz, const int* rowptr, const int* col,
                         const void* op_val, const void* x, void* y, int precision,
                         void* stream);
 
+/* y = Op x with the operator in the sliced-ELL layout built by
+ * usbs_gb300.problem.sell_layout: rows in windows of 256, sorted by length
+ * inside a window and cut into 32-row slices; slice s holds its entries
+ * column-major from sl_ptr[s] (sl_ptr has ceil(n/32)+1 ints, slices padded
+ * with column 0 / value 0); sl_row[32 s + r] is row r's position inside its
+ * window.  Same result as usbs_operator_apply on the CSR it was built from (up
+ * to summation order).  No counterpart in the reference (its operator is a
+ * BCOO matvec). */
+int usbs_operator_apply_sell(int n, const int* sl_ptr, const int* sl_col, const void* sl_val,
+                             const unsigned char* sl_row, const void* x, void* y, int precision,
+                             void* stream);
+
+/* dst[e] = src[map[e]] (0 where map[e] < 0), `total` entries of the
+ * `precision` type: the CSR operator values moved into sliced-ELL order. */
+int usbs_gather_values(long long total, const int* map, const void* src, void* dst,
+                       int precision, void* stream);
+
 /* out[c] = sum_j sum_{t in c} t_a[t] U[t_row[t], j] U[t_col[t], j], c < m:
  * apply_A_operator_slim (k = 1) / apply_A_operator_batched (k columns),
  * solver/utils.py:11-16 and 27-31.  U column-major n x k with leading

@@ -186,3 +186,39 @@ def test_operator_apply_ragged_csr(cuda, shape, precision):
     scale = np.abs(Mv).sum(axis=1).A1 * np.abs(xr).max() + 1e-300
     tol = 1e-13 if precision == 64 else 2e-6
     assert np.all(np.abs(got - ref) <= tol * scale)
+
+
+@pytest.mark.parametrize("shape", [(1, 1, 0, 0), (257, 3, 0, 0), (1000, 7, 3, 40),
+                                   (5003, 2, 2, 4000), (4099, 12, 1, 300)])
+@pytest.mark.parametrize("precision", [64, 32])
+def test_sell_apply_matches_csr(cuda, shape, precision):
+    """usbs_operator_apply_sell on the sliced-ELL layout equals the CSR apply."""
+    import ctypes
+    import torch
+    from usbs_gb300 import _lib
+    from usbs_gb300.problem import sell_layout
+    lib = _lib.load()
+    M = _ragged_csr(*shape, seed=shape[0] + 1)
+    n = M.shape[0]
+    vt = torch.float64 if precision == 64 else torch.float32
+    L = sell_layout(M.indptr, M.indices)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    dev = lambda a, dt: torch.tensor(a, dtype=dt, device=cuda)
+    csr_val = dev(M.data, vt)
+    sl_val = torch.empty(max(L["stored"], 1), dtype=vt, device=cuda)
+    src = dev(L["sl_src"], torch.int32)
+    assert lib.usbs_gather_values(L["stored"], p(src), p(csr_val), p(sl_val), precision, s) == 0
+    x = dev(np.random.default_rng(5).standard_normal(n), vt)
+    y = torch.full((n,), float("nan"), dtype=vt, device=cuda)
+    assert lib.usbs_operator_apply_sell(n, p(dev(L["sl_ptr"], torch.int32)),
+                                        p(dev(L["sl_col"], torch.int32)), p(sl_val),
+                                        p(dev(L["sl_row"], torch.uint8)), p(x), p(y), precision,
+                                        s) == 0
+    torch.cuda.synchronize()
+    xr = x.double().cpu().numpy()
+    Mv = M.astype(np.float32).astype(np.float64) if precision == 32 else M
+    ref = Mv @ xr
+    scale = np.abs(Mv).sum(axis=1).A1 * np.abs(xr).max() + 1e-300
+    tol = 1e-13 if precision == 64 else 2e-6
+    assert np.all(np.abs(y.double().cpu().numpy() - ref) <= tol * scale)

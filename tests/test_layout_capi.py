@@ -117,3 +117,32 @@ def test_product_qap_builder_matches_oracle(l):
         _as_set(b.A_data, b.A_indices, b.b, b.b_ineq_mask)
     assert ta.keys() == tb.keys()
     assert max(abs(ta[k] - tb[k]) for k in ta) < 1e-12
+
+
+@pytest.mark.parametrize("shape", [(1, 1), (255, 3), (257, 7), (1000, 12), (3001, 2)])
+def test_sell_layout_covers_every_entry_once(shape):
+    n, avg = shape
+    rs = np.random.default_rng(n)
+    lens = rs.integers(0, 2 * avg + 1, size=n)
+    rowptr = np.concatenate([[0], np.cumsum(lens)])
+    col = rs.integers(0, n, size=int(rowptr[-1])).astype(np.int32)
+    L = P.sell_layout(rowptr, col)
+    src = L["sl_src"]
+    real = src[src >= 0]
+    assert np.array_equal(np.sort(real), np.arange(rowptr[-1]))        # each entry once
+    np.testing.assert_array_equal(L["sl_col"][src >= 0], col[real])
+    assert np.all(L["sl_col"][src < 0] == 0)
+    nsl = (n + 31) // 32
+    assert L["sl_ptr"].size == nsl + 1 and np.all(np.diff(L["sl_ptr"]) % 32 == 0)
+    # positions inside each window form a permutation of the window's slots
+    row = L["sl_row"].astype(np.int64)
+    for w0 in range(0, nsl * 32, 256):
+        seg = row[w0:w0 + 256]
+        assert np.array_equal(np.sort(seg), np.arange(seg.size))
+    # entry k of the row at sorted position q sits at sl_ptr[q // 32] + 32 k + q % 32
+    order = (np.arange(n) // 256) * 256 + row[:n]
+    for q in rs.integers(0, n, size=min(n, 50)):
+        r = order[q]
+        for k in range(lens[r]):
+            e = L["sl_ptr"][q // 32] + 32 * k + q % 32
+            assert src[e] == rowptr[r] + k

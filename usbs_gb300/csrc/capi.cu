@@ -123,6 +123,21 @@ int usbs_operator_apply(int n, long long nnz, const int* rowptr, const int* col,
                   (cudaStream_t)stream);
 }
 
+int usbs_operator_apply_sell(int n, const int* sl_ptr, const int* sl_col, const void* sl_val,
+                             const unsigned char* sl_row, const void* x, void* y, int precision,
+                             void* stream) {
+  if (precision != 32 && precision != 64) { set_error("precision must be 32 or 64"); return -2; }
+  if (n < 0) { set_error("n < 0"); return -2; }
+  return sell_spmv(n, sl_ptr, sl_col, sl_val, sl_row, x, y, precision, (cudaStream_t)stream);
+}
+
+int usbs_gather_values(long long total, const int* map, const void* src, void* dst,
+                       int precision, void* stream) {
+  if (precision != 32 && precision != 64) { set_error("precision must be 32 or 64"); return -2; }
+  if (total < 0) { set_error("total < 0"); return -2; }
+  return gather_values(total, map, src, dst, precision, (cudaStream_t)stream);
+}
+
 int usbs_apply_A_operator(int m, int k, const int* con_ptr, const int* t_row, const int* t_col,
                           const double* t_a, const double* U, int ldu, double* out,
                           void* stream) {

@@ -55,6 +55,12 @@ int assemble_operator(int nnz, const double* c_val, double alpha_c, const int* s
 // y = M x  for CSR M (values double or float), optional per-row partial dots
 int csr_spmv(int n, long long nnz, const int* rowptr, const int* col, const void* val,
              const void* x, void* y, int prec, int sm_count, cudaStream_t stream);
+// y = M x for M in the sliced-ELL layout (windows of 256 rows, 32-row slices)
+int sell_spmv(int n, const int* sl_ptr, const int* col, const void* val,
+              const unsigned char* sl_row, const void* x, void* y, int prec, cudaStream_t stream);
+// dst[e] = src[map[e]], 0 where map[e] < 0
+int gather_values(long long total, const int* map, const void* src, void* dst, int prec,
+                  cudaStream_t stream);
 // out[c] += sum over triples of constraint c: a * u[i] . u[j]   (k columns, ld)
 int apply_A_operator(int m, const int* con_ptr, const int* t_row, const int* t_col,
                      const double* a, const double* U, int ldu, int k, double* out,

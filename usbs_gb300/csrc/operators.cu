@@ -101,6 +101,95 @@ int csr_spmv(int n, long long nnz, const int* rowptr, const int* col, const void
   return 0;
 }
 
+// ------------------------------------------------------------------------
+// Sliced-ELL operator apply.  Rows are grouped in windows of SELL_WIN = 256
+// rows; inside a window they are sorted by length (longest first) and cut into
+// 8 slices of 32 rows.  A slice stores its entries column-major (entry k of
+// the slice's row r at sl_ptr[s] + 32 k + r), padded to the slice's longest
+// row with column 0 and value 0.  One block per window, one warp per slice,
+// lane = row: every load of col / val is a coalesced 128-byte line, and all of
+// a row's loads are independent (no rowptr -> col -> x chain).  sl_row[32 s + r]
+// is the row's position inside its window; results pass through shared memory
+// so y is written in the original order, coalesced.
+constexpr int SELL_WIN = 256;
+
+template <typename VT>
+__global__ void __launch_bounds__(SELL_WIN) sell_spmv_kernel(int n, const int* __restrict__ sl_ptr,
+                                                           const int* __restrict__ col,
+                                                           const VT* __restrict__ val,
+                                                           const unsigned char* __restrict__ sl_row,
+                                                           const VT* __restrict__ x,
+                                                           VT* __restrict__ y) {
+  __shared__ VT ys[SELL_WIN];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int s = blockIdx.x * (SELL_WIN / 32) + warp;
+  const int w0 = blockIdx.x * SELL_WIN;
+  const int nslices = (n + 31) / 32;
+  VT acc = (VT)0;
+  if (s < nslices) {
+    const int base = sl_ptr[s], width = (sl_ptr[s + 1] - base) >> 5;
+    const int* cp = col + base + lane;
+    const VT* vp = val + base + lane;
+    int k = 0;
+    for (; k + 3 < width; k += 4) {
+      const int c0 = __ldg(cp + 32 * k), c1 = __ldg(cp + 32 * (k + 1)),
+                c2 = __ldg(cp + 32 * (k + 2)), c3 = __ldg(cp + 32 * (k + 3));
+      const VT v0 = __ldg(vp + 32 * k), v1 = __ldg(vp + 32 * (k + 1)),
+               v2 = __ldg(vp + 32 * (k + 2)), v3 = __ldg(vp + 32 * (k + 3));
+      const VT x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
+      acc += v0 * x0;
+      acc += v1 * x1;
+      acc += v2 * x2;
+      acc += v3 * x3;
+    }
+    for (; k < width; ++k) acc += __ldg(vp + 32 * k) * __ldg(x + __ldg(cp + 32 * k));
+    ys[sl_row[32 * s + lane]] = acc;
+  }
+  __syncthreads();
+  const int r = w0 + threadIdx.x;
+  if (r < n) y[r] = ys[threadIdx.x];
+}
+
+int sell_spmv(int n, const int* sl_ptr, const int* col, const void* val,
+              const unsigned char* sl_row, const void* x, void* y, int prec, cudaStream_t stream) {
+  if (n <= 0) return 0;
+  const int blocks = (n + SELL_WIN - 1) / SELL_WIN;
+  if (prec == 64)
+    sell_spmv_kernel<double><<<blocks, SELL_WIN, 0, stream>>>(n, sl_ptr, col, (const double*)val,
+                                                            sl_row, (const double*)x, (double*)y);
+  else
+    sell_spmv_kernel<float><<<blocks, SELL_WIN, 0, stream>>>(n, sl_ptr, col, (const float*)val,
+                                                           sl_row, (const float*)x, (float*)y);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) { set_error("sell_spmv: %s", cudaGetErrorString(e)); return -5; }
+  return 0;
+}
+
+// dst[e] = src[map[e]] (0 where map[e] < 0): operator values from CSR to sliced-ELL order
+template <typename VT>
+__global__ void gather_values_kernel(long long total, const int* __restrict__ map,
+                                     const VT* __restrict__ src, VT* __restrict__ dst) {
+  for (long long e = blockIdx.x * (long long)blockDim.x + threadIdx.x; e < total;
+       e += (long long)gridDim.x * blockDim.x) {
+    const int m = map[e];
+    dst[e] = (m >= 0) ? src[m] : (VT)0;
+  }
+}
+
+int gather_values(long long total, const int* map, const void* src, void* dst, int prec,
+                  cudaStream_t stream) {
+  if (total <= 0) return 0;
+  long long b = (total + 255) / 256;
+  const int blocks = (int)(b < 152 * 16 ? b : 152 * 16);
+  if (prec == 64)
+    gather_values_kernel<double><<<blocks, 256, 0, stream>>>(total, map, (const double*)src, (double*)dst);
+  else
+    gather_values_kernel<float><<<blocks, 256, 0, stream>>>(total, map, (const float*)src, (float*)dst);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) { set_error("gather_values: %s", cudaGetErrorString(e)); return -5; }
+  return 0;
+}
+
 // out[c] = sum_{t in constraint c} a_t * U[i_t, :] . U[j_t, :]    (one warp per constraint)
 __global__ void A_operator_kernel(int m, const int* __restrict__ con_ptr,
                                   const int* __restrict__ t_row, const int* __restrict__ t_col,

@@ -114,3 +114,53 @@ class DeviceProblem:
 
     def h2d_bytes(self):
         return sum(getattr(self.host, f).nbytes for f in self.FIELDS)
+
+
+SELL_WINDOW = 256   # rows per window (one CUDA block)
+SELL_SLICE = 32     # rows per slice (one warp)
+
+
+def sell_layout(rowptr, col):
+    """Sliced-ELL layout of a CSR pattern for usbs_operator_apply_sell.
+
+    Rows are taken in windows of 256, sorted by length (longest first, stable)
+    inside their window and cut into 32-row slices; slice s stores its entries
+    column-major from ``sl_ptr[s]``, padded to its longest row.  Returns a dict
+    of int32 ``sl_ptr`` (slices + 1), int32 ``sl_col`` and ``sl_src`` (the CSR
+    position of every stored entry, -1 for padding), and uint8 ``sl_row`` (each
+    sorted row's position inside its window; padding lanes get their own,
+    unused position)."""
+    rowptr = np.asarray(rowptr, dtype=np.int64)
+    col = np.asarray(col)
+    n = rowptr.size - 1
+    lens = np.diff(rowptr)
+    nsl = (n + SELL_SLICE - 1) // SELL_SLICE
+    npos = nsl * SELL_SLICE
+    # sorted order inside each window
+    win = np.arange(n) // SELL_WINDOW
+    order = np.lexsort((np.arange(n), -lens, win))          # window, then length desc, then row
+    srows = np.full(npos, -1, dtype=np.int64)
+    srows[:n] = order
+    slens = np.zeros(npos, dtype=np.int64)
+    slens[:n] = lens[order]
+    widths = slens.reshape(nsl, SELL_SLICE).max(axis=1)
+    sl_ptr = np.zeros(nsl + 1, dtype=np.int64)
+    np.cumsum(widths * SELL_SLICE, out=sl_ptr[1:])
+    total = int(sl_ptr[-1])
+    if total > np.iinfo(np.int32).max:
+        raise ValueError("sliced-ELL layout exceeds 2^31 entries")
+    sl_col = np.zeros(total, dtype=np.int32)
+    sl_src = np.full(total, -1, dtype=np.int32)
+    pos = np.arange(n)
+    rep = np.repeat(pos, slens[:n])                           # sorted position of each entry
+    first = np.repeat(np.cumsum(slens[:n]) - slens[:n], slens[:n])
+    k = np.arange(rep.size) - first                           # entry index inside its row
+    dst = sl_ptr[rep // SELL_SLICE] + SELL_SLICE * k + (rep % SELL_SLICE)
+    src = rowptr[srows[rep]] + k
+    sl_col[dst] = col[src]
+    sl_src[dst] = src
+    sl_row = np.empty(npos, dtype=np.uint8)
+    sl_row[:n] = order - (np.arange(n) // SELL_WINDOW) * SELL_WINDOW
+    sl_row[n:] = np.arange(n, npos) % SELL_WINDOW
+    return dict(sl_ptr=sl_ptr.astype(np.int32), sl_col=sl_col, sl_src=sl_src, sl_row=sl_row,
+                stored=total)
