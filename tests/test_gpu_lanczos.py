@@ -222,3 +222,37 @@ def test_sell_apply_matches_csr(cuda, shape, precision):
     scale = np.abs(Mv).sum(axis=1).A1 * np.abs(xr).max() + 1e-300
     tol = 1e-13 if precision == 64 else 2e-6
     assert np.all(np.abs(y.double().cpu().numpy() - ref) <= tol * scale)
+
+
+# The cooperative team kernel (problems too large for one cluster): unstaged
+# (x in shared memory, n = 15,625 in FP64) and staged (Q tiles streamed by bulk
+# copies, n > 20,480 in FP64 / 40,960 in FP32)
+@pytest.mark.parametrize("side,precision", [(125, 64), (150, 64), (210, 32)])
+def test_eigsh_team_kernel_matches_oracle(cuda, side, precision):
+    from usbs_gb300 import _lib, api
+    from usbs_gb300.problem import DeviceProblem, layout
+    Wg = wl.er_graph(side * side, 4 * side * side, side)
+    st = omaxcut.initialize_state(Wg, 4)
+    n = st.C.shape[0]
+    assert _lib.load().usbs_lanczos_kernel(n, 32, precision) == 0     # team kernel
+    prob = DeviceProblem(layout(st.C, st.A_data, st.A_indices, m=n), cuda)
+    y = np.random.default_rng(3).standard_normal(n) * 0.5
+    q0 = orng.default_q0(n)
+    nd, restarts, tol = 4, 60, (1e-8 if precision == 64 else 1e-5)
+    ov, oV, ost = olz.eigsh_smallest(n, (-st.C).tocsr(), st.A_data, st.A_indices, y, q0, nd, 32,
+                                     restarts, tol)
+    gv, gV, info = api.eigsh_smallest(n, prob, None, None, y, q0, nd, 32, restarts, tol,
+                                      c_scale=-1.0, precision=precision, return_info=True)
+    gv, gV = _np(gv), _np(gV).astype(np.float64)
+    assert info.status == 0
+    scale = np.abs(ov).max()
+    if precision == 64:
+        assert ost["nconv"] >= nd
+        np.testing.assert_allclose(gv, ov, rtol=1e-9, atol=1e-9 * scale)
+        for j in range(nd):
+            assert abs(gV[:, j] @ oV[:, j]) > 1 - 1e-10, j
+    else:
+        assert np.abs(gv - ov).max() < 1e-4 * scale
+    Op = ((-st.C) + sp.diags(y)).tocsr()
+    r = np.linalg.norm(Op @ gV - gV * gv[None, :], axis=0)
+    assert r.max() < (1e-6 if precision == 64 else 1e-2) * scale

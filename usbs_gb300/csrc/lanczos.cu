@@ -36,6 +36,7 @@ constexpr int LZ_XS_BYTES = 160 * 1024;   // dynamic shared memory for a staged 
 template <typename VT>
 struct TeamDesc {
   int n, ld, m, num_desired, max_restarts, lanes, first_cta, nctas, xsmem;
+  int stages;            // > 0: phases stream Q tiles through shared memory (bulk copies)
   double tol;
   const int* rowptr;
   const int* col;
@@ -251,6 +252,178 @@ __device__ void phase_spmv(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0, int 
   block_reduce_cols(acc, i + 1, sh, part_out, P.nctas);
 }
 
+// ---------------------------------------------------------------- staged tiles
+// Large problems (x not staged in shared memory): each phase streams its
+// tiles' rows of the needed Q columns and of one work vector into shared
+// memory with bulk async copies issued by thread 0, `stages` tiles ahead, so
+// a CTA reads its rows of the basis at streaming rate instead of one DRAM
+// round trip per tile.  Stage layout: STG_COLS columns of LZ_BLOCK values
+// (Q columns 0..MP1-1, the vector in column MP1).
+constexpr int STG_COLS = MP1 + 1;
+
+template <typename VT>
+struct Stager {
+  VT* base;          // stages x STG_COLS x LZ_BLOCK values
+  uint64_t* bar;     // one mbarrier per stage
+  int S;
+  unsigned ph;       // parity of each stage's next phase (identical in every thread)
+  __device__ VT* stage(int s) const { return base + (size_t)s * STG_COLS * LZ_BLOCK; }
+};
+
+// thread 0: rows of tile `tile` of Q[:, 0:ncols] and, if vec, of vec into stage s
+template <typename VT>
+__device__ void stg_issue(const TeamDesc<VT>& P, Stager<VT>& G, int s, int tile, int ncols,
+                          const VT* vec) {
+  constexpr int E16 = 16 / (int)sizeof(VT);
+  const int r0 = tile * LZ_BLOCK;
+  const int rows = min(LZ_BLOCK, P.n - r0);
+  // ld is a multiple of 32 >= n, so the padded rows stay inside each column
+  const unsigned bytes = (unsigned)(((rows + E16 - 1) / E16) * E16 * (int)sizeof(VT));
+  VT* st = G.stage(s);
+  // order this CTA's earlier generic stores (of Q and the vectors) and its
+  // reads of the stage before the async copies
+  asm volatile("fence.proxy.async;" ::: "memory");
+  mbar_arrive_expect_tx(&G.bar[s], bytes * (unsigned)(ncols + (vec ? 1 : 0)));
+  for (int c = 0; c < ncols; ++c)
+    bulk_g2s(st + (size_t)c * LZ_BLOCK, P.Q + (size_t)c * P.ld + r0, bytes, &G.bar[s]);
+  if (vec) bulk_g2s(st + (size_t)MP1 * LZ_BLOCK, vec + r0, bytes, &G.bar[s]);
+}
+
+// body(tile, stage) for tiles [t0, t1), copies pipelined `stages` deep.  On a
+// wait that runs past its limit: records ST_BARRIER_TIMEOUT, waits (bounded)
+// for the copies still in flight and returns false; the CTA then leaves at
+// its next team barrier.
+template <typename VT, typename F>
+__device__ bool stg_loop(const TeamDesc<VT>& P, Stager<VT>& G, int t0, int t1, int ncols,
+                         const VT* vec, F&& body) {
+  const uint64_t LIMIT = 1000000000ull;
+  const int S = G.S;
+  if (threadIdx.x == 0)
+    for (int j = 0; j < S && t0 + j < t1; ++j) stg_issue(P, G, j, t0 + j, ncols, vec);
+  for (int t = t0; t < t1; ++t) {
+    const int s = (t - t0) % S;
+    const unsigned par = (G.ph >> s) & 1u;
+    const bool ok = mbar_wait(&G.bar[s], par, LIMIT);
+    if (__syncthreads_or(!ok)) {
+      // drain: this tile's copies and those of the later tiles already issued
+      mbar_wait(&G.bar[s], par, LIMIT);
+      G.ph ^= (1u << s);
+      for (int tt = t + 1; tt < t1 && tt < t + S; ++tt) {
+        const int s2 = (tt - t0) % S;
+        mbar_wait(&G.bar[s2], (G.ph >> s2) & 1u, LIMIT);
+        G.ph ^= (1u << s2);
+      }
+      if (threadIdx.x == 0) atomicOr(P.status, ST_BARRIER_TIMEOUT);
+      __syncthreads();
+      return false;
+    }
+    G.ph ^= (1u << s);
+    body(t, (const VT*)G.stage(s));
+    __syncthreads();
+    if (threadIdx.x == 0 && t + S < t1) stg_issue(P, G, s, t + S, ncols, vec);
+  }
+  return true;
+}
+
+// staged phase A: as phase_spmv, with Q[:, c] (and xsrc's own rows) from the stage
+template <typename VT>
+__device__ void stg_phase_spmv(const TeamDesc<VT>& P, LzShared<VT>& sh, Stager<VT>& G, int t0,
+                               int t1, int i, const VT* xsrc, VT xscale, bool wq, VT* vout,
+                               double* part_out) {
+  typedef typename Acc<VT>::type AT;
+  AT acc[MP1];
+#pragma unroll
+  for (int c = 0; c < MP1; ++c) acc[c] = (AT)0;
+  const int tid = threadIdx.x, L = P.lanes;
+  const size_t ld = (size_t)P.ld;
+  const int ncols = wq ? i : i + 1;
+  stg_loop(P, G, t0, t1, ncols, wq ? xsrc : nullptr, [&](int tile, const VT* stq) {
+    const int base = tile * LZ_BLOCK;
+    switch (L) {
+      case 1: spmv_tile<VT, 1>(P, sh, base, xsrc, nullptr, false); break;
+      case 2: spmv_tile<VT, 2>(P, sh, base, xsrc, nullptr, false); break;
+      case 4: spmv_tile<VT, 4>(P, sh, base, xsrc, nullptr, false); break;
+      case 8: spmv_tile<VT, 8>(P, sh, base, xsrc, nullptr, false); break;
+      case 16: spmv_tile<VT, 16>(P, sh, base, xsrc, nullptr, false); break;
+      default: spmv_tile<VT, 32>(P, sh, base, xsrc, nullptr, false); break;
+    }
+    __syncthreads();
+    const int row = base + tid;
+    if (row < P.n) {
+      const VT y = (VT)sh.u.st.ys[tid] * xscale;
+      vout[row] = y;
+      VT xn = (VT)0;
+      if (wq) {
+        xn = stq[(size_t)MP1 * LZ_BLOCK + tid] * xscale;
+        P.Q[(size_t)i * ld + row] = xn;
+      }
+#pragma unroll
+      for (int c = 0; c < MP1; ++c) {
+        if (c <= i) {
+          const VT qc = (wq && c == i) ? xn : stq[(size_t)c * LZ_BLOCK + tid];
+          acc[c] += (AT)qc * (AT)y;
+        }
+      }
+    }
+  });
+  block_reduce_cols(acc, i + 1, sh, part_out, P.nctas);
+}
+
+// staged phase B: buf -= Q h (c < nv); acc[c] = Q[:, c] . buf
+template <typename VT>
+__device__ void stg_phase_update_dot(const TeamDesc<VT>& P, LzShared<VT>& sh, Stager<VT>& G,
+                                     int t0, int t1, int nv, VT* buf, double* part_out) {
+  typedef typename Acc<VT>::type AT;
+  AT acc[MP1];
+#pragma unroll
+  for (int c = 0; c < MP1; ++c) acc[c] = (AT)0;
+  const int tid = threadIdx.x;
+  stg_loop(P, G, t0, t1, nv, buf, [&](int tile, const VT* stq) {
+    const int row = tile * LZ_BLOCK + tid;
+    if (row < P.n) {
+      VT qr[MP1];
+      VT s = (VT)0;
+#pragma unroll
+      for (int c = 0; c < MP1; ++c) {
+        if (c < nv) {
+          qr[c] = stq[(size_t)c * LZ_BLOCK + tid];
+          s += qr[c] * sh.hv[c];
+        }
+      }
+      const VT q1 = stq[(size_t)MP1 * LZ_BLOCK + tid] - s;
+      buf[row] = q1;
+#pragma unroll
+      for (int c = 0; c < MP1; ++c)
+        if (c < nv) acc[c] += (AT)qr[c] * (AT)q1;
+    }
+  });
+  block_reduce_cols(acc, nv, sh, part_out, P.nctas);
+}
+
+// staged phase C: buf -= Q h (c < nv); part_out[0] = sum buf^2 over own rows
+template <typename VT>
+__device__ void stg_phase_update_norm(const TeamDesc<VT>& P, LzShared<VT>& sh, Stager<VT>& G,
+                                      int t0, int t1, int nv, VT* buf, double* part_out) {
+  typedef typename Acc<VT>::type AT;
+  AT nrm = (AT)0;
+  const int tid = threadIdx.x;
+  stg_loop(P, G, t0, t1, nv, buf, [&](int tile, const VT* stq) {
+    const int row = tile * LZ_BLOCK + tid;
+    if (row < P.n) {
+      VT s = (VT)0;
+#pragma unroll
+      for (int c = 0; c < MP1; ++c)
+        if (c < nv) s += stq[(size_t)c * LZ_BLOCK + tid] * sh.hv[c];
+      const VT q2 = stq[(size_t)MP1 * LZ_BLOCK + tid] - s;
+      buf[row] = q2;
+      nrm += (AT)q2 * (AT)q2;
+    }
+  });
+  AT one[MP1];
+  one[0] = nrm;
+  block_reduce_cols(one, 1, sh, part_out, P.nctas);
+}
+
 // Breakdown pass a: buf = hash_normal(key) for own rows, acc[c] = Q[:, c] . buf (c < nv)
 template <typename VT>
 __device__ void phase_random(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0, int t1, int nv,
@@ -459,7 +632,7 @@ __device__ void restart_select(const D& P, LzShared<VT>& sh, int k, bool write_o
 }
 
 template <typename VT>
-__global__ void __launch_bounds__(LZ_BLOCK)
+__global__ void __launch_bounds__(LZ_BLOCK, 1)
 lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
   __shared__ LzShared<VT> sh;
   int team = 0;
@@ -494,6 +667,18 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
   } while (0)
   if (rank == 0 && tid < MAXM) { sh.alpha[tid] = 0.0; sh.beta[tid] = 0.0; }
   if (tid == 0) sh.eig_cycles = 0;
+  // staged tiles (large problems): stages of STG_COLS x LZ_BLOCK values, then
+  // one mbarrier per stage, in the dynamic shared memory
+  extern __shared__ __align__(16) unsigned char lz_dyn[];
+  Stager<VT> G;
+  G.S = P.stages;
+  G.ph = 0u;
+  G.base = (VT*)lz_dyn;
+  G.bar = (uint64_t*)(lz_dyn + (size_t)(P.stages > 0 ? P.stages : 0) * STG_COLS * LZ_BLOCK * sizeof(VT));
+  if (P.stages > 0 && tid == 0) {
+    for (int j = 0; j < P.stages; ++j) mbar_init(&G.bar[j], 1);
+    mbar_init_fence();
+  }
   __syncthreads();
   int prev = 0;          // vbuf slot holding the latest unnormalised vector
   VT invb = (VT)1;       // its normalisation
@@ -533,21 +718,24 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
       }
       VT* vout = P.vbuf + (size_t)cur * ld;
       LZ_MARK(1);
-      phase_spmv(P, sh, t0, t1, i, xsrc, invb, wq, vout, part0 + rank);
+      if (P.stages) stg_phase_spmv(P, sh, G, t0, t1, i, xsrc, invb, wq, vout, part0 + rank);
+      else phase_spmv(P, sh, t0, t1, i, xsrc, invb, wq, vout, part0 + rank);
       LZ_MARK(2);
       if (!bar.sync()) return;
       LZ_MARK(0);
       reduce_part(part0, R, i + 1, sh);
       LZ_MARK(1);
       const double h1i = sh.h[i];
-      phase_update_dot(P, sh, t0, t1, i + 1, vout, part1 + rank);
+      if (P.stages) stg_phase_update_dot(P, sh, G, t0, t1, i + 1, vout, part1 + rank);
+      else phase_update_dot(P, sh, t0, t1, i + 1, vout, part1 + rank);
       LZ_MARK(3);
       if (!bar.sync()) return;
       LZ_MARK(0);
       reduce_part(part1, R, i + 1, sh);
       LZ_MARK(1);
       if (rank == 0 && tid == 0) sh.alpha[i] = h1i + sh.h[i];
-      phase_update_norm(P, sh, t0, t1, i + 1, vout, part2 + rank);
+      if (P.stages) stg_phase_update_norm(P, sh, G, t0, t1, i + 1, vout, part2 + rank);
+      else phase_update_norm(P, sh, t0, t1, i + 1, vout, part2 + rank);
       LZ_MARK(4);
       if (!bar.sync()) return;
       LZ_MARK(0);
@@ -1175,6 +1363,21 @@ static int run_typed(const DeviceInfo& di, const LanczosProblem* probs, int coun
       t.lanes = lanczos_lanes(p.n, p.nnz);
       t.xsmem = ((size_t)p.n * sizeof(VT) <= (size_t)LZ_XS_BYTES) ? 1 : 0;
       if (t.xsmem && (size_t)p.n * sizeof(VT) > dyn) dyn = (size_t)p.n * sizeof(VT);
+      // staged tiles when x is not staged: bulk copies need ld a multiple of 32
+      // (16-byte aligned column starts, padded rows inside the column) and
+      // 16-byte aligned Q and work vectors
+      t.stages = 0;
+      const size_t stage_bytes = (size_t)STG_COLS * LZ_BLOCK * sizeof(VT);
+      if (!t.xsmem && p.ld % 32 == 0 && ((uintptr_t)p.Q & 15u) == 0 &&
+          ((uintptr_t)p.work & 15u) == 0) {
+        int S = (int)(((size_t)LZ_XS_BYTES - 64) / stage_bytes);
+        if (S > 4) S = 4;
+        if (S >= 2) {
+          t.stages = S;
+          const size_t need = (size_t)S * stage_bytes + (size_t)S * sizeof(uint64_t);
+          if (need > dyn) dyn = need;
+        }
+      }
       t.first_cta = first;
       t.nctas = want[i];
       t.rowptr = p.rowptr; t.col = p.col; t.val = (const VT*)p.val;

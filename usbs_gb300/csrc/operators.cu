@@ -130,19 +130,21 @@ __global__ void __launch_bounds__(SELL_WIN) sell_spmv_kernel(int n, const int* _
     const int base = sl_ptr[s], width = (sl_ptr[s + 1] - base) >> 5;
     const int* cp = col + base + lane;
     const VT* vp = val + base + lane;
-    int k = 0;
-    for (; k + 3 < width; k += 4) {
-      const int c0 = __ldg(cp + 32 * k), c1 = __ldg(cp + 32 * (k + 1)),
-                c2 = __ldg(cp + 32 * (k + 2)), c3 = __ldg(cp + 32 * (k + 3));
-      const VT v0 = __ldg(vp + 32 * k), v1 = __ldg(vp + 32 * (k + 1)),
-               v2 = __ldg(vp + 32 * (k + 2)), v3 = __ldg(vp + 32 * (k + 3));
-      const VT x0 = __ldg(x + c0), x1 = __ldg(x + c1), x2 = __ldg(x + c2), x3 = __ldg(x + c3);
-      acc += v0 * x0;
-      acc += v1 * x1;
-      acc += v2 * x2;
-      acc += v3 * x3;
+    // the first SELL_PF entries of the row: every col / val load, then every
+    // x gather, in flight at once; longer rows finish in a plain loop
+    constexpr int SELL_PF = 16;
+    int c[SELL_PF];
+    VT v[SELL_PF], xv[SELL_PF];
+#pragma unroll
+    for (int u = 0; u < SELL_PF; ++u) {
+      c[u] = (u < width) ? __ldg(cp + 32 * u) : 0;
+      v[u] = (u < width) ? __ldg(vp + 32 * u) : (VT)0;
     }
-    for (; k < width; ++k) acc += __ldg(vp + 32 * k) * __ldg(x + __ldg(cp + 32 * k));
+#pragma unroll
+    for (int u = 0; u < SELL_PF; ++u) xv[u] = (u < width) ? __ldg(x + c[u]) : (VT)0;
+#pragma unroll
+    for (int u = 0; u < SELL_PF; ++u) acc += v[u] * xv[u];
+    for (int k = SELL_PF; k < width; ++k) acc += __ldg(vp + 32 * k) * __ldg(x + __ldg(cp + 32 * k));
     ys[sl_row[32 * s + lane]] = acc;
   }
   __syncthreads();
