@@ -294,6 +294,25 @@ def profile_case(args):
         r = spmv_gbs(device, reps=1)
         print(json.dumps({"profile_case": "spmv", "kernel_launches_timed": 1, **r}))
         return 0
+    if args.profile_case == "eigsh-rgg":
+        from usbs_gb300 import api, workloads as wl
+        from usbs_gb300.problem import DeviceProblem, layout
+        from usbs_gb300.problems import maxcut
+        from usbs_gb300.rng import default_q0
+        W = wl.rgg_knn_graph(10 ** 6, 6, 0)
+        st = maxcut.initialize_state(W, 1)
+        n = st.C.shape[0]
+        prob = DeviceProblem(layout(st.C, st.A_data, st.A_indices, m=n), device)
+        out = []
+        for nd in (10, 10):
+            t0 = time.perf_counter()
+            _, _, inf = api.eigsh_smallest(n, prob, None, None, np.zeros(n), default_q0(n), nd, 32,
+                                           10, 1e-7, c_scale=-1.0, precision=32, return_info=True)
+            torch.cuda.synchronize()
+            out.append({"ms": 1e3 * (time.perf_counter() - t0), "matvecs": inf.matvecs,
+                        "phase_kcycles": inf.phase_kcycles})
+        print(json.dumps({"profile_case": "eigsh-rgg", "calls": out}))
+        return 0
     from usbs_gb300 import solver
     from usbs_gb300.problems import maxcut
     from usbs_gb300.rng import default_q0
@@ -319,10 +338,11 @@ def main():
     ap.add_argument("--cpu-iters", type=int, default=24)
     ap.add_argument("--no-spmv", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
-    ap.add_argument("--profile-case", choices=["usbs", "spmv"], default=None,
+    ap.add_argument("--profile-case", choices=["usbs", "spmv", "eigsh-rgg"], default=None,
                     help="run one piece of the workload once, untimed (for ncu captures): "
                          "'usbs' = --iters-per-step outer iterations on the torus instance, "
-                         "'spmv' = the RGG operator apply (3 launches)")
+                         "'spmv' = the RGG operator apply, "
+                         "'eigsh-rgg' = two FP32 eigsh calls (team kernel) on the 10^6-node RGG")
     args = ap.parse_args()
     if args.profile_case:
         return profile_case(args)

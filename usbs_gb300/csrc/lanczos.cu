@@ -37,6 +37,8 @@ template <typename VT>
 struct TeamDesc {
   int n, ld, m, num_desired, max_restarts, lanes, first_cta, nctas, xsmem;
   int stages;            // > 0: phases stream Q tiles through shared memory (bulk copies)
+  int stage_csr;         // the stages also carry each tile's CSR slice (phase A)
+  long long nnz;
   double tol;
   const int* rowptr;
   const int* col;
@@ -261,32 +263,113 @@ __device__ void phase_spmv(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0, int 
 // (Q columns 0..MP1-1, the vector in column MP1).
 constexpr int STG_COLS = MP1 + 1;
 
+// CSR slice of one tile staged beside its Q rows (FP32 stages only)
+constexpr int STG_CAP = 4096;   // entries of a tile's CSR slice that fit in a stage
+struct StgHdr {
+  int rcnt;       // staged rowptr entries (from the tile's first row)
+  int p0;         // first entry of the tile
+  int ca0, ca1;   // staged col range [ca0, ca1)
+  int va0, va1;   // staged val range [va0, va1)
+  int pad[2];
+};
 template <typename VT>
-struct Stager {
-  VT* base;          // stages x STG_COLS x LZ_BLOCK values
-  uint64_t* bar;     // one mbarrier per stage
-  int S;
-  unsigned ph;       // parity of each stage's next phase (identical in every thread)
-  __device__ VT* stage(int s) const { return base + (size_t)s * STG_COLS * LZ_BLOCK; }
+struct StgLayout {   // byte offsets inside one stage
+  static constexpr size_t q = 0;
+  static constexpr size_t rp = (size_t)STG_COLS * LZ_BLOCK * sizeof(VT);
+  static constexpr size_t col = rp + (size_t)(LZ_BLOCK + 4) * sizeof(int);
+  static constexpr size_t val = col + (size_t)(STG_CAP + 8) * sizeof(int);
+  static constexpr size_t hdr = val + (size_t)(STG_CAP + 8) * sizeof(VT);
+  static constexpr size_t with_csr = hdr + sizeof(StgHdr);
+  static constexpr size_t q_only = rp;
 };
 
-// thread 0: rows of tile `tile` of Q[:, 0:ncols] and, if vec, of vec into stage s
+template <typename VT>
+struct Stager {
+  unsigned char* base;   // stages of `bytes` each
+  uint64_t* bar;         // one mbarrier per stage
+  size_t bytes;          // bytes per stage (Q only, or Q + CSR slice)
+  int S;
+  int csr;               // stages carry the tile's CSR slice (phase A)
+  int nx_p0, nx_p1;      // thread 0: entry range of the next tile to issue (prefetched)
+  unsigned ph;           // parity of each stage's next phase (identical in every thread)
+  __device__ VT* stage(int s) const { return (VT*)(base + (size_t)s * bytes); }
+  __device__ unsigned char* raw(int s) const { return base + (size_t)s * bytes; }
+};
+
+// warp 0: rows of tile `tile` of Q[:, 0:ncols] and, if vec, of vec into stage
+// s; lane 0 arms the stage's mbarrier with the byte count, then the lanes
+// issue the copies in parallel (copy j by lane j mod 32)
 template <typename VT>
 __device__ void stg_issue(const TeamDesc<VT>& P, Stager<VT>& G, int s, int tile, int ncols,
-                          const VT* vec) {
+                          const VT* vec, bool csr = false) {
   constexpr int E16 = 16 / (int)sizeof(VT);
+  const int lane = threadIdx.x & 31;
   const int r0 = tile * LZ_BLOCK;
   const int rows = min(LZ_BLOCK, P.n - r0);
   // ld is a multiple of 32 >= n, so the padded rows stay inside each column
   const unsigned bytes = (unsigned)(((rows + E16 - 1) / E16) * E16 * (int)sizeof(VT));
   VT* st = G.stage(s);
+  unsigned tx = bytes * (unsigned)(ncols + (vec ? 1 : 0));
+  // CSR slice of the tile (phase A of FP32 stages): rowptr[r0 ..], col and val
+  // over [p0, p1), each widened to 16-byte boundaries inside its array; the
+  // few elements past an array's last full 16-byte block, and every entry of
+  // a tile larger than STG_CAP, are read from global memory by the consumers
+  unsigned rb = 0, cb = 0, vb = 0;
+  StgHdr h;
+  if (csr) {
+    typedef StgLayout<VT> SL;
+    const int p0 = __shfl_sync(0xffffffffu, G.nx_p0, 0);
+    const int p1 = __shfl_sync(0xffffffffu, G.nx_p1, 0);
+    int rcnt = (rows + 1 + 3) & ~3;
+    const int rmax = ((P.n + 1) & ~3) - r0;
+    if (rcnt > rmax) rcnt = rmax > 0 ? rmax : 0;
+    const long long nnz = P.nnz;
+    const bool fits = (p1 - p0) <= STG_CAP;
+    int ca0 = p0 & ~3, ca1 = (p1 + 3) & ~3;
+    const int cfull = (int)(nnz & ~3LL);
+    if (ca1 > cfull) ca1 = cfull;
+    if (!fits || ca1 < ca0) ca1 = ca0;
+    int va0 = p0 & ~(E16 - 1), va1 = (p1 + E16 - 1) & ~(E16 - 1);
+    const int vfull = (int)(nnz & ~(long long)(E16 - 1));
+    if (va1 > vfull) va1 = vfull;
+    if (!fits || va1 < va0) va1 = va0;
+    h.rcnt = rcnt; h.p0 = p0; h.ca0 = ca0; h.ca1 = ca1; h.va0 = va0; h.va1 = va1;
+    if (lane == 0) *(StgHdr*)(G.raw(s) + SL::hdr) = h;
+    rb = (unsigned)rcnt * 4u;
+    cb = (unsigned)(ca1 - ca0) * 4u;
+    vb = (unsigned)(va1 - va0) * (unsigned)sizeof(VT);
+    tx += rb + cb + vb;
+  }
   // order this CTA's earlier generic stores (of Q and the vectors) and its
   // reads of the stage before the async copies
   asm volatile("fence.proxy.async;" ::: "memory");
-  mbar_arrive_expect_tx(&G.bar[s], bytes * (unsigned)(ncols + (vec ? 1 : 0)));
-  for (int c = 0; c < ncols; ++c)
-    bulk_g2s(st + (size_t)c * LZ_BLOCK, P.Q + (size_t)c * P.ld + r0, bytes, &G.bar[s]);
-  if (vec) bulk_g2s(st + (size_t)MP1 * LZ_BLOCK, vec + r0, bytes, &G.bar[s]);
+  if (lane == 0) mbar_arrive_expect_tx(&G.bar[s], tx);
+  __syncwarp();
+  // streamed once per phase: evict_first, so the copies do not push the SpMV's
+  // x (gathered with evict_last) out of L2
+  const uint64_t pol = l2_evict_first_policy();
+  const int ncopies = ncols + (vec ? 1 : 0) + (csr ? 3 : 0);
+  for (int j = lane; j < ncopies; j += 32) {
+    if (j < ncols) {
+      bulk_g2s_hint(st + (size_t)j * LZ_BLOCK, P.Q + (size_t)j * P.ld + r0, bytes, &G.bar[s], pol);
+    } else if (vec && j == ncols) {
+      bulk_g2s_hint(st + (size_t)MP1 * LZ_BLOCK, vec + r0, bytes, &G.bar[s], pol);
+    } else {
+      typedef StgLayout<VT> SL;
+      const int k = j - ncols - (vec ? 1 : 0);   // 0 rowptr, 1 col, 2 val
+      if (k == 0 && rb) bulk_g2s_hint(G.raw(s) + SL::rp, P.rowptr + r0, rb, &G.bar[s], pol);
+      if (k == 1 && cb) bulk_g2s_hint(G.raw(s) + SL::col, P.col + h.ca0, cb, &G.bar[s], pol);
+      if (k == 2 && vb) bulk_g2s_hint(G.raw(s) + SL::val, P.val + h.va0, vb, &G.bar[s], pol);
+    }
+  }
+}
+
+// thread 0: entry range of tile `tile` (loads left in flight until the next issue)
+template <typename VT>
+__device__ __forceinline__ void stg_prefetch_range(const TeamDesc<VT>& P, Stager<VT>& G, int tile) {
+  const int r0 = tile * LZ_BLOCK;
+  G.nx_p0 = P.rowptr[r0];
+  G.nx_p1 = P.rowptr[min(r0 + LZ_BLOCK, P.n)];
 }
 
 // body(tile, stage) for tiles [t0, t1), copies pipelined `stages` deep.  On a
@@ -295,11 +378,16 @@ __device__ void stg_issue(const TeamDesc<VT>& P, Stager<VT>& G, int s, int tile,
 // its next team barrier.
 template <typename VT, typename F>
 __device__ bool stg_loop(const TeamDesc<VT>& P, Stager<VT>& G, int t0, int t1, int ncols,
-                         const VT* vec, F&& body) {
+                         const VT* vec, F&& body, bool csr = false) {
   const uint64_t LIMIT = 1000000000ull;
   const int S = G.S;
-  if (threadIdx.x == 0)
-    for (int j = 0; j < S && t0 + j < t1; ++j) stg_issue(P, G, j, t0 + j, ncols, vec);
+  if (threadIdx.x < 32) {
+    for (int j = 0; j < S && t0 + j < t1; ++j) {
+      if (csr && threadIdx.x == 0) stg_prefetch_range(P, G, t0 + j);
+      stg_issue(P, G, j, t0 + j, ncols, vec, csr);
+    }
+    if (csr && threadIdx.x == 0 && t0 + S < t1) stg_prefetch_range(P, G, t0 + S);
+  }
   for (int t = t0; t < t1; ++t) {
     const int s = (t - t0) % S;
     const unsigned par = (G.ph >> s) & 1u;
@@ -318,11 +406,97 @@ __device__ bool stg_loop(const TeamDesc<VT>& P, Stager<VT>& G, int t0, int t1, i
       return false;
     }
     G.ph ^= (1u << s);
-    body(t, (const VT*)G.stage(s));
+    body(t, s);
     __syncthreads();
-    if (threadIdx.x == 0 && t + S < t1) stg_issue(P, G, s, t + S, ncols, vec);
+    if (threadIdx.x < 32 && t + S < t1) {
+      stg_issue(P, G, s, t + S, ncols, vec, csr);
+      if (csr && threadIdx.x == 0 && t + S + 1 < t1) stg_prefetch_range(P, G, t + S + 1);
+    }
   }
   return true;
+}
+
+// SpMV of one 256-row tile from its staged CSR slice (rowptr, col, val in
+// shared memory; x gathered from global memory), L lanes per row, groups of up
+// to 4 passes as in spmv_tile
+template <typename VT, int L>
+__device__ __forceinline__ void spmv_tile_stg(const TeamDesc<VT>& P, LzShared<VT>& sh, int base,
+                                              const unsigned char* stg, const VT* xsrc) {
+  typedef typename Acc<VT>::type AT;
+  typedef StgLayout<VT> SL;
+  constexpr int GPP = LZ_BLOCK / L;
+  constexpr int CH = L < 4 ? L : 4;
+  const StgHdr h = *(const StgHdr*)(stg + SL::hdr);
+  const int* rp = (const int*)(stg + SL::rp);
+  const int* cs = (const int*)(stg + SL::col);
+  VT* vs = (VT*)(stg + SL::val);
+  const int tid = threadIdx.x, g = tid / L, lig = tid - (tid / L) * L;
+  const int rows = min(LZ_BLOCK, P.n - base);
+  // fully staged tile: every product v x[c] of the tile at once (about nnz /
+  // 256 independent gathers per thread), written over its own value in the
+  // stage, then one thread per row sums its row's products
+  if (rows + 1 <= h.rcnt) {
+    const int p0 = rp[0], p1 = rp[rows];
+    if (p1 <= h.ca1 && p1 <= h.va1) {
+      const uint64_t keep = l2_evict_last_policy();
+      constexpr int U = 8;
+      for (int pb = p0 + tid; pb < p1; pb += U * LZ_BLOCK) {
+        int c[U];
+        VT xv[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int p = pb + u * LZ_BLOCK;
+          c[u] = (p < p1) ? cs[p - h.ca0] : 0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) xv[u] = ldcg_pol(xsrc + c[u], keep);
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int p = pb + u * LZ_BLOCK;
+          if (p < p1) vs[p - h.va0] = vs[p - h.va0] * xv[u];
+        }
+      }
+      __syncthreads();
+      if (tid < rows) {
+        AT sacc = (AT)0;
+        const int e = rp[tid + 1];
+        for (int p = rp[tid]; p < e; ++p) sacc += (AT)vs[p - h.va0];
+        sh.u.st.ys[tid] = (double)sacc;
+      }
+      return;
+    }
+  }
+  auto colv = [&](int p, int& c, VT& v) {
+    c = (p < h.ca1) ? cs[p - h.ca0] : P.col[p];
+    v = (p < h.va1) ? vs[p - h.va0] : P.val[p];
+  };
+#pragma unroll 1
+  for (int q0 = 0; q0 < L; q0 += CH) {
+    int pb[CH], pe[CH];
+#pragma unroll
+    for (int q = 0; q < CH; ++q) {
+      const int lr = (q0 + q) * GPP + g;
+      const int row = base + lr;
+      pb[q] = 0; pe[q] = 0;
+      if (row < P.n) {
+        pb[q] = ((lr < h.rcnt) ? rp[lr] : P.rowptr[row]) + lig;
+        pe[q] = (lr + 1 < h.rcnt) ? rp[lr + 1] : P.rowptr[row + 1];
+      }
+    }
+#pragma unroll
+    for (int q = 0; q < CH; ++q) {
+      AT s = (AT)0;
+      for (int p = pb[q]; p < pe[q]; p += L) {
+        int c;
+        VT v;
+        colv(p, c, v);
+        s += (AT)v * (AT)__ldcg(xsrc + c);
+      }
+#pragma unroll
+      for (int o = L >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+      if (lig == 0) sh.u.st.ys[(q0 + q) * GPP + g] = (double)s;
+    }
+  }
 }
 
 // staged phase A: as phase_spmv, with Q[:, c] (and xsrc's own rows) from the stage
@@ -337,15 +511,29 @@ __device__ void stg_phase_spmv(const TeamDesc<VT>& P, LzShared<VT>& sh, Stager<V
   const int tid = threadIdx.x, L = P.lanes;
   const size_t ld = (size_t)P.ld;
   const int ncols = wq ? i : i + 1;
-  stg_loop(P, G, t0, t1, ncols, wq ? xsrc : nullptr, [&](int tile, const VT* stq) {
+  const bool csr = G.csr != 0;
+  stg_loop(P, G, t0, t1, ncols, wq ? xsrc : nullptr, [&](int tile, int sidx) {
+    const VT* stq = G.stage(sidx);
     const int base = tile * LZ_BLOCK;
-    switch (L) {
-      case 1: spmv_tile<VT, 1>(P, sh, base, xsrc, nullptr, false); break;
-      case 2: spmv_tile<VT, 2>(P, sh, base, xsrc, nullptr, false); break;
-      case 4: spmv_tile<VT, 4>(P, sh, base, xsrc, nullptr, false); break;
-      case 8: spmv_tile<VT, 8>(P, sh, base, xsrc, nullptr, false); break;
-      case 16: spmv_tile<VT, 16>(P, sh, base, xsrc, nullptr, false); break;
-      default: spmv_tile<VT, 32>(P, sh, base, xsrc, nullptr, false); break;
+    if (csr) {
+      const unsigned char* stg = G.raw(sidx);
+      switch (L) {
+        case 1: spmv_tile_stg<VT, 1>(P, sh, base, stg, xsrc); break;
+        case 2: spmv_tile_stg<VT, 2>(P, sh, base, stg, xsrc); break;
+        case 4: spmv_tile_stg<VT, 4>(P, sh, base, stg, xsrc); break;
+        case 8: spmv_tile_stg<VT, 8>(P, sh, base, stg, xsrc); break;
+        case 16: spmv_tile_stg<VT, 16>(P, sh, base, stg, xsrc); break;
+        default: spmv_tile_stg<VT, 32>(P, sh, base, stg, xsrc); break;
+      }
+    } else {
+      switch (L) {
+        case 1: spmv_tile<VT, 1>(P, sh, base, xsrc, nullptr, false); break;
+        case 2: spmv_tile<VT, 2>(P, sh, base, xsrc, nullptr, false); break;
+        case 4: spmv_tile<VT, 4>(P, sh, base, xsrc, nullptr, false); break;
+        case 8: spmv_tile<VT, 8>(P, sh, base, xsrc, nullptr, false); break;
+        case 16: spmv_tile<VT, 16>(P, sh, base, xsrc, nullptr, false); break;
+        default: spmv_tile<VT, 32>(P, sh, base, xsrc, nullptr, false); break;
+      }
     }
     __syncthreads();
     const int row = base + tid;
@@ -365,7 +553,7 @@ __device__ void stg_phase_spmv(const TeamDesc<VT>& P, LzShared<VT>& sh, Stager<V
         }
       }
     }
-  });
+  }, csr);
   block_reduce_cols(acc, i + 1, sh, part_out, P.nctas);
 }
 
@@ -378,7 +566,8 @@ __device__ void stg_phase_update_dot(const TeamDesc<VT>& P, LzShared<VT>& sh, St
 #pragma unroll
   for (int c = 0; c < MP1; ++c) acc[c] = (AT)0;
   const int tid = threadIdx.x;
-  stg_loop(P, G, t0, t1, nv, buf, [&](int tile, const VT* stq) {
+  stg_loop(P, G, t0, t1, nv, buf, [&](int tile, int sidx) {
+    const VT* stq = G.stage(sidx);
     const int row = tile * LZ_BLOCK + tid;
     if (row < P.n) {
       VT qr[MP1];
@@ -407,7 +596,8 @@ __device__ void stg_phase_update_norm(const TeamDesc<VT>& P, LzShared<VT>& sh, S
   typedef typename Acc<VT>::type AT;
   AT nrm = (AT)0;
   const int tid = threadIdx.x;
-  stg_loop(P, G, t0, t1, nv, buf, [&](int tile, const VT* stq) {
+  stg_loop(P, G, t0, t1, nv, buf, [&](int tile, int sidx) {
+    const VT* stq = G.stage(sidx);
     const int row = tile * LZ_BLOCK + tid;
     if (row < P.n) {
       VT s = (VT)0;
@@ -672,9 +862,12 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
   extern __shared__ __align__(16) unsigned char lz_dyn[];
   Stager<VT> G;
   G.S = P.stages;
+  G.csr = P.stage_csr;
   G.ph = 0u;
-  G.base = (VT*)lz_dyn;
-  G.bar = (uint64_t*)(lz_dyn + (size_t)(P.stages > 0 ? P.stages : 0) * STG_COLS * LZ_BLOCK * sizeof(VT));
+  G.nx_p0 = G.nx_p1 = 0;
+  G.base = lz_dyn;
+  G.bytes = P.stage_csr ? (StgLayout<VT>::with_csr + 15) / 16 * 16 : StgLayout<VT>::q_only;
+  G.bar = (uint64_t*)(lz_dyn + (size_t)(P.stages > 0 ? P.stages : 0) * G.bytes);
   if (P.stages > 0 && tid == 0) {
     for (int j = 0; j < P.stages; ++j) mbar_init(&G.bar[j], 1);
     mbar_init_fence();
@@ -1367,13 +1560,21 @@ static int run_typed(const DeviceInfo& di, const LanczosProblem* probs, int coun
       // (16-byte aligned column starts, padded rows inside the column) and
       // 16-byte aligned Q and work vectors
       t.stages = 0;
-      const size_t stage_bytes = (size_t)STG_COLS * LZ_BLOCK * sizeof(VT);
+      t.stage_csr = 0;
       if (!t.xsmem && p.ld % 32 == 0 && ((uintptr_t)p.Q & 15u) == 0 &&
           ((uintptr_t)p.work & 15u) == 0) {
+        // FP32 stages also carry the tile's CSR slice when two of them fit
+        // (bulk copies of rowptr / col / val need 16-byte aligned arrays)
+        const size_t csr_bytes = (StgLayout<VT>::with_csr + 15) / 16 * 16;
+        const bool csr_ok = sizeof(VT) == 4 && ((((uintptr_t)p.rowptr) | ((uintptr_t)p.col) |
+                                                 ((uintptr_t)p.val)) & 15u) == 0 &&
+                            2 * csr_bytes + 64 <= (size_t)LZ_XS_BYTES;
+        const size_t stage_bytes = csr_ok ? csr_bytes : StgLayout<VT>::q_only;
         int S = (int)(((size_t)LZ_XS_BYTES - 64) / stage_bytes);
         if (S > 4) S = 4;
         if (S >= 2) {
           t.stages = S;
+          t.stage_csr = csr_ok ? 1 : 0;
           const size_t need = (size_t)S * stage_bytes + (size_t)S * sizeof(uint64_t);
           if (need > dyn) dyn = need;
         }
@@ -1381,6 +1582,7 @@ static int run_typed(const DeviceInfo& di, const LanczosProblem* probs, int coun
       t.first_cta = first;
       t.nctas = want[i];
       t.rowptr = p.rowptr; t.col = p.col; t.val = (const VT*)p.val;
+      t.nnz = p.nnz;
       t.Q = (VT*)p.Q;
       char* w = (char*)p.work;
       t.vbuf = (VT*)w; w += align256(2 * (size_t)p.ld * sizeof(VT));
