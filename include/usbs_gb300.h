@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define USBS_GB300_ABI_VERSION 1
+#define USBS_GB300_ABI_VERSION 2
 
 /* ABI version of the loaded library (USBS_GB300_ABI_VERSION). */
 int usbs_abi_version(void);
@@ -234,6 +234,13 @@ typedef struct usbs_state {
   int lanczos_launches;
   double lanczos_ms, lanczos_bytes;
   long long kernel_launches;
+  /* the state at the latest condition check, written before the callback
+   * runs, in the trace-record layout (usbs_solve: t, primal_obj, obj_ub,
+   * obj_gap, infeas_gap, max_infeas, pen_dual_obj, cand_pen_dual_obj,
+   * lb_spec_est, eig0, descent, eta, trS, tr_X, IPM iterations x2,
+   * bar_primal_obj, tr_X_bar, b.y; usbs_cgal_solve: its first 8 trace fields);
+   * the scaled problem's values, as the reference's cond_func sees them */
+  double cond[20];
 } usbs_state;
 
 /* Called on the host at every condition check (after the device has caught
@@ -282,6 +289,34 @@ size_t usbs_cgal_workspace_bytes(const usbs_problem* problem, const usbs_cgal_pa
 int usbs_cgal_solve(const usbs_problem* problem, const usbs_cgal_params* params,
                     usbs_state* state, void* workspace, size_t workspace_bytes,
                     usbs_cond_callback callback, void* callback_user, void* stream);
+
+/* ---------------------------------------------------------------- rounding */
+
+/* Workspace bytes of usbs_reconstruct_from_sketch / usbs_maxcut_round for n
+ * rows and a sketch of s <= 32 columns (0 for unsupported sizes). */
+size_t usbs_round_workspace_bytes(int n, int s);
+
+/* reconstruct_from_sketch (utils/common.py:99-116): the Nystrom factors of
+ * the sketch P = X Omega.  Omega and P are n x s, column-major with leading
+ * dimension ld.  E (n x s, lde; may be NULL) receives the left singular
+ * vectors of P_rho L^-T, Lambda (s; may be NULL) max(Rho^2 - rho, 0), both in
+ * the reference's order (Rho descending; each column of E up to its sign).
+ * Where B = sym(Omega^T P_rho) is not positive definite, E and Lambda are NaN
+ * as jnp.linalg.cholesky makes them.  Stream-ordered; device pointers. */
+int usbs_reconstruct_from_sketch(int n, int s, const double* Omega, const double* P, int ld,
+                                 double approx_eps, double* E, int lde, double* Lambda,
+                                 void* workspace, size_t workspace_bytes, void* stream);
+
+/* compute_max_cut (utils/maxcut_helpers.py:292-302): *value (device) =
+ * max_j w_j^T C w_j with w_j = +1 where column j of the reconstructed E is
+ * positive and -1 elsewhere, for the CSR matrix C (the unscaled objective,
+ * both triangles).  column_values (s; may be NULL) receives every w_j^T C w_j,
+ * signs (n; may be NULL) the sign words (bit j set: +1).  approx_eps is the
+ * reference's 1e-6.  Stream-ordered; device pointers. */
+int usbs_maxcut_round(int n, int s, const double* Omega, const double* P, int ld,
+                      const int* rowptr, const int* col, const double* val, double approx_eps,
+                      double* value, double* column_values, unsigned* signs, void* workspace,
+                      size_t workspace_bytes, void* stream);
 
 #ifdef __cplusplus
 }

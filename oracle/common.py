@@ -46,7 +46,13 @@ def reconstruct_from_sketch(Omega, P, approx_eps=1e-6):
     P_rho = P + rho * Omega
     B = Omega.T @ P_rho
     B = 0.5 * (B + B.T)
-    L = np.linalg.cholesky(B)
+    try:
+        L = np.linalg.cholesky(B)
+    except np.linalg.LinAlgError:
+        # jnp.linalg.cholesky returns NaNs for a matrix that is not positive
+        # definite (a zero sketch, for one), and the NaNs flow through
+        s = P.shape[1]
+        return np.full((n, s), np.nan), np.full(s, np.nan)
     E, Rho, _ = np.linalg.svd(np.linalg.lstsq(L, P_rho.T, rcond=None)[0].T, full_matrices=False)
     Lam = np.clip(Rho ** 2 - rho, 0, np.inf)
     return E, Lam

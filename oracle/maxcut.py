@@ -1,5 +1,6 @@
-"""MaxCut SDP builder (oracle).  Restates ``utils/maxcut_helpers.py:26-92`` and the
-implicit / dual-only warm starts (``utils/maxcut_helpers.py:95-161, 232-289``).
+"""MaxCut SDP builder (oracle).  Restates ``utils/maxcut_helpers.py:26-92``, the
+implicit / dual-only warm starts (``utils/maxcut_helpers.py:95-161, 232-289``) and
+the rounding callback ``compute_max_cut`` (``utils/maxcut_helpers.py:292-302``).
 
 Input ``W`` is the (symmetric or not) weighted adjacency matrix, as the reference
 reads it from a .mat file.  C = 1/4 (diag(W 1) - W), symmetrised; constraints
@@ -9,7 +10,7 @@ diag(X) = 1 as (i, i, i) triples.  ``Omega`` defaults to
 import numpy as np
 import scipy.sparse as sp
 
-from .common import SDPState, scale_sdp_state, unscale_sdp_state
+from .common import SDPState, reconstruct_from_sketch, scale_sdp_state, unscale_sdp_state
 from .rng import hash_normal_matrix
 
 
@@ -106,3 +107,15 @@ def get_dual_only_warm_start_state(old, W, sketch_dim, Omega=None):
                   SCALE_C=1.0 / np.linalg.norm(C.data), SCALE_X=1.0 / float(n),
                   SCALE_A=np.ones(m))
     return scale_sdp_state(st)
+
+
+def compute_max_cut(P, Omega, callback_static_args, callback_nonstatic_args):
+    """Largest cut among the sign patterns of the sketch's reconstructed
+    eigenvectors (utils/maxcut_helpers.py:292-302): callback_nonstatic_args is
+    the unscaled C; returns max_j w_j^T C w_j over w_j = sign(E[:, j]) (+1 where
+    E > 0, -1 elsewhere, NaN included)."""
+    C = sp.csr_matrix(callback_nonstatic_args, dtype=np.float64)
+    E, _ = reconstruct_from_sketch(np.asarray(Omega, float), np.asarray(P, float))
+    with np.errstate(invalid="ignore"):
+        W_bin = 2.0 * (E > 0).astype(float) - 1.0
+    return float(np.max(np.einsum("ij,ij->j", W_bin, C @ W_bin)))

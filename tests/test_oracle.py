@@ -154,3 +154,35 @@ def test_lb_ipm_is_a_lower_model_value():
     # bundle model: b.y + trace_ub * max(lambda_max(V^T (C - A*y) V), 0)
     model = y.sum() + trace_ub * max(lam[-1], 0.0)
     assert abs(lb - model) < 1e-5 * (1 + abs(model))
+
+
+def test_reconstruct_from_sketch_recovers_low_rank():
+    """utils/common.py:99-116 on the sketch of a rank-3 PSD matrix: the Nystrom
+    factors give X back up to the rho shift (rho ~ n 1e-6 lambda_max here)."""
+    from oracle import common as ocommon
+    rng = np.random.default_rng(11)
+    n, s = 200, 8
+    V = np.linalg.qr(rng.standard_normal((n, 3)))[0]
+    X = (V * np.array([5.0, 2.0, 1.0])) @ V.T
+    Om = rng.standard_normal((n, s))
+    E, lam = ocommon.reconstruct_from_sketch(Om, X @ Om)
+    assert np.all(np.diff(lam) <= 0.0)
+    assert np.allclose(lam[:3], [5.0, 2.0, 1.0], rtol=1e-2)
+    assert np.abs(lam[3:]).max() < 1e-12
+    assert np.abs((E * lam) @ E.T - X).max() < 1e-2
+
+
+def test_compute_max_cut_known_answers():
+    """utils/maxcut_helpers.py:292-302: the sketch of v v^T for the 2-colouring
+    of an even torus cuts every edge; a zero sketch (Cholesky fails, NaN
+    signs) gives the all -1 vector, whose Laplacian cut value is 0."""
+    from usbs_gb300 import workloads as wl
+    side = 10
+    W = wl.torus_graph(side, 0, weights="unit")
+    n = W.shape[0]
+    i = np.arange(n)
+    v = np.where(((i // side) + (i % side)) % 2 == 0, 1.0, -1.0)
+    C = omaxcut.laplacian_objective(W)
+    Om = np.random.default_rng(1).standard_normal((n, 6))
+    assert omaxcut.compute_max_cut(np.outer(v, v @ Om), Om, None, C) == W.nnz / 2
+    assert omaxcut.compute_max_cut(np.zeros((n, 6)), Om, None, C) == 0.0

@@ -38,6 +38,11 @@ SIGNATURES = {
     "usbs_solve": (c_int, [P, P, P, P, c_size_t, P, P, P]),
     "usbs_cgal_workspace_bytes": (c_size_t, [P, P]),
     "usbs_cgal_solve": (c_int, [P, P, P, P, c_size_t, P, P, P]),
+    "usbs_round_workspace_bytes": (c_size_t, [c_int, c_int]),
+    "usbs_reconstruct_from_sketch": (c_int, [c_int, c_int, P, P, c_int, c_double, P, c_int, P, P,
+                                             c_size_t, P]),
+    "usbs_maxcut_round": (c_int, [c_int, c_int, P, P, c_int, P, P, P, c_double, P, P, P, P,
+                                  c_size_t, P]),
 }
 
 
@@ -60,7 +65,7 @@ def load(build_if_missing=True):
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.usbs_abi_version() != 1:
+    if lib.usbs_abi_version() != 2:
         raise LibraryError("libusbs_gb300 ABI version mismatch")
     _lib = lib
     return lib

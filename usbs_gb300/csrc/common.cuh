@@ -210,6 +210,11 @@ __device__ __forceinline__ double ldcg_pol(const double* p, uint64_t pol) {
 __device__ __forceinline__ void fence_proxy_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
+// this thread's earlier global stores ordered before later async-proxy (bulk
+// copy) reads of them, once the reader has synchronised with this thread
+__device__ __forceinline__ void fence_proxy_async_global() {
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+}
 
 // splitmix64 (Vigna) and Box-Muller: the counter-based normal generator that the
 // host side and the tests restate bit-for-bit in their integer part.

@@ -36,8 +36,10 @@ constexpr int LZ_XS_BYTES = 160 * 1024;   // dynamic shared memory for a staged 
 template <typename VT>
 struct TeamDesc {
   int n, ld, m, num_desired, max_restarts, lanes, first_cta, nctas, xsmem;
-  int stages;            // > 0: phases stream Q tiles through shared memory (bulk copies)
+  int stages;            // non-zero: phases stream Q tiles through shared memory (bulk copies)
   int stage_csr;         // the stages also carry each tile's CSR slice (phase A)
+  int stg_budget;        // bytes of the stage area (a multiple of 128)
+  int stg_cap;           // CSR slice capacity (entries, a multiple of 64)
   long long nnz;
   double tol;
   const int* rowptr;
@@ -259,12 +261,11 @@ __device__ void phase_spmv(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0, int 
 // tiles' rows of the needed Q columns and of one work vector into shared
 // memory with bulk async copies issued by thread 0, `stages` tiles ahead, so
 // a CTA reads its rows of the basis at streaming rate instead of one DRAM
-// round trip per tile.  Stage layout: STG_COLS columns of LZ_BLOCK values
-// (Q columns 0..MP1-1, the vector in column MP1).
-constexpr int STG_COLS = MP1 + 1;
-
-// CSR slice of one tile staged beside its Q rows (FP32 stages only)
-constexpr int STG_CAP = 4096;   // entries of a tile's CSR slice that fit in a stage
+// round trip per tile.  The stage layout is planned per phase: the staged Q
+// columns, then the work vector, then (phase A, FP32) the tile's CSR slice,
+// so a phase that streams few columns keeps more tiles in flight.
+constexpr int STG_MAXS = 8;     // mbarriers, i.e. the deepest pipeline
+constexpr int STG_CAP = 4096;   // largest CSR slice (entries) a stage can carry
 struct StgHdr {
   int rcnt;       // staged rowptr entries (from the tile's first row)
   int p0;         // first entry of the tile
@@ -272,29 +273,50 @@ struct StgHdr {
   int va0, va1;   // staged val range [va0, va1)
   int pad[2];
 };
+// bytes of a stage's CSR slice part (rowptr, col, val, header) for `cap` entries
 template <typename VT>
-struct StgLayout {   // byte offsets inside one stage
-  static constexpr size_t q = 0;
-  static constexpr size_t rp = (size_t)STG_COLS * LZ_BLOCK * sizeof(VT);
-  static constexpr size_t col = rp + (size_t)(LZ_BLOCK + 4) * sizeof(int);
-  static constexpr size_t val = col + (size_t)(STG_CAP + 8) * sizeof(int);
-  static constexpr size_t hdr = val + (size_t)(STG_CAP + 8) * sizeof(VT);
-  static constexpr size_t with_csr = hdr + sizeof(StgHdr);
-  static constexpr size_t q_only = rp;
-};
+__host__ __device__ constexpr unsigned stg_csr_bytes(int cap) {
+  return (unsigned)(((LZ_BLOCK + 4) * 4 + (cap + 8) * 4 + (cap + 8) * (int)sizeof(VT) +
+                     (int)sizeof(StgHdr) + 127) / 128 * 128);
+}
+// bytes of the Q part of a stage: `cols` columns of LZ_BLOCK values
+template <typename VT>
+__host__ __device__ constexpr unsigned stg_q_bytes(int cols) {
+  return (unsigned)cols * LZ_BLOCK * (unsigned)sizeof(VT);
+}
 
 template <typename VT>
 struct Stager {
-  unsigned char* base;   // stages of `bytes` each
-  uint64_t* bar;         // one mbarrier per stage
-  size_t bytes;          // bytes per stage (Q only, or Q + CSR slice)
-  int S;
-  int csr;               // stages carry the tile's CSR slice (phase A)
+  unsigned char* base;   // the stage area, `budget` bytes
+  uint64_t* bar;         // STG_MAXS mbarriers
+  unsigned budget;
+  int cap;               // CSR slice capacity (entries) of a phase-A stage
+  int csr;               // phase A stages carry the tile's CSR slice
+  // plan of the running phase (identical in every thread)
+  unsigned bytes;        // bytes per stage
+  int S;                 // stages (tiles in flight)
+  int vcol;              // stage column of the work vector (= staged Q columns)
+  unsigned rp, col, val, hdr;   // CSR slice offsets inside a stage
   int nx_p0, nx_p1;      // thread 0: entry range of the next tile to issue (prefetched)
-  unsigned ph;           // parity of each stage's next phase (identical in every thread)
+  unsigned ph;           // parity of each mbarrier's next phase (identical in every thread)
   __device__ VT* stage(int s) const { return (VT*)(base + (size_t)s * bytes); }
   __device__ unsigned char* raw(int s) const { return base + (size_t)s * bytes; }
 };
+
+// stage layout and depth of a phase streaming `ncols` Q columns (+ the work
+// vector, + the CSR slice); the host sizes `budget` for two of the largest
+template <typename VT>
+__device__ __forceinline__ void stg_plan(Stager<VT>& G, int ncols, bool vec, bool csr) {
+  G.vcol = ncols;
+  const unsigned qb = stg_q_bytes<VT>(ncols + (vec ? 1 : 0));
+  G.rp = qb;
+  G.col = G.rp + (LZ_BLOCK + 4) * 4;
+  G.val = G.col + (unsigned)(G.cap + 8) * 4;
+  G.hdr = G.val + (unsigned)(G.cap + 8) * (unsigned)sizeof(VT);
+  G.bytes = csr ? qb + stg_csr_bytes<VT>(G.cap) : qb;
+  int S = (int)(G.budget / G.bytes);
+  G.S = S > STG_MAXS ? STG_MAXS : (S < 1 ? 1 : S);
+}
 
 // warp 0: rows of tile `tile` of Q[:, 0:ncols] and, if vec, of vec into stage
 // s; lane 0 arms the stage's mbarrier with the byte count, then the lanes
@@ -317,14 +339,13 @@ __device__ void stg_issue(const TeamDesc<VT>& P, Stager<VT>& G, int s, int tile,
   unsigned rb = 0, cb = 0, vb = 0;
   StgHdr h;
   if (csr) {
-    typedef StgLayout<VT> SL;
     const int p0 = __shfl_sync(0xffffffffu, G.nx_p0, 0);
     const int p1 = __shfl_sync(0xffffffffu, G.nx_p1, 0);
     int rcnt = (rows + 1 + 3) & ~3;
     const int rmax = ((P.n + 1) & ~3) - r0;
     if (rcnt > rmax) rcnt = rmax > 0 ? rmax : 0;
     const long long nnz = P.nnz;
-    const bool fits = (p1 - p0) <= STG_CAP;
+    const bool fits = (p1 - p0) <= G.cap;
     int ca0 = p0 & ~3, ca1 = (p1 + 3) & ~3;
     const int cfull = (int)(nnz & ~3LL);
     if (ca1 > cfull) ca1 = cfull;
@@ -334,15 +355,16 @@ __device__ void stg_issue(const TeamDesc<VT>& P, Stager<VT>& G, int s, int tile,
     if (va1 > vfull) va1 = vfull;
     if (!fits || va1 < va0) va1 = va0;
     h.rcnt = rcnt; h.p0 = p0; h.ca0 = ca0; h.ca1 = ca1; h.va0 = va0; h.va1 = va1;
-    if (lane == 0) *(StgHdr*)(G.raw(s) + SL::hdr) = h;
+    if (lane == 0) *(StgHdr*)(G.raw(s) + G.hdr) = h;
     rb = (unsigned)rcnt * 4u;
     cb = (unsigned)(ca1 - ca0) * 4u;
     vb = (unsigned)(va1 - va0) * (unsigned)sizeof(VT);
     tx += rb + cb + vb;
   }
-  // order this CTA's earlier generic stores (of Q and the vectors) and its
-  // reads of the stage before the async copies
-  asm volatile("fence.proxy.async;" ::: "memory");
+  // the stage's earlier generic accesses (header, products written over the
+  // values) before the async copies into it; the global data the copies read
+  // was fenced by its writers before the team barrier that precedes the phase
+  fence_proxy_async_smem();
   if (lane == 0) mbar_arrive_expect_tx(&G.bar[s], tx);
   __syncwarp();
   // streamed once per phase: evict_first, so the copies do not push the SpMV's
@@ -353,13 +375,12 @@ __device__ void stg_issue(const TeamDesc<VT>& P, Stager<VT>& G, int s, int tile,
     if (j < ncols) {
       bulk_g2s_hint(st + (size_t)j * LZ_BLOCK, P.Q + (size_t)j * P.ld + r0, bytes, &G.bar[s], pol);
     } else if (vec && j == ncols) {
-      bulk_g2s_hint(st + (size_t)MP1 * LZ_BLOCK, vec + r0, bytes, &G.bar[s], pol);
+      bulk_g2s_hint(st + (size_t)G.vcol * LZ_BLOCK, vec + r0, bytes, &G.bar[s], pol);
     } else {
-      typedef StgLayout<VT> SL;
       const int k = j - ncols - (vec ? 1 : 0);   // 0 rowptr, 1 col, 2 val
-      if (k == 0 && rb) bulk_g2s_hint(G.raw(s) + SL::rp, P.rowptr + r0, rb, &G.bar[s], pol);
-      if (k == 1 && cb) bulk_g2s_hint(G.raw(s) + SL::col, P.col + h.ca0, cb, &G.bar[s], pol);
-      if (k == 2 && vb) bulk_g2s_hint(G.raw(s) + SL::val, P.val + h.va0, vb, &G.bar[s], pol);
+      if (k == 0 && rb) bulk_g2s_hint(G.raw(s) + G.rp, P.rowptr + r0, rb, &G.bar[s], pol);
+      if (k == 1 && cb) bulk_g2s_hint(G.raw(s) + G.col, P.col + h.ca0, cb, &G.bar[s], pol);
+      if (k == 2 && vb) bulk_g2s_hint(G.raw(s) + G.val, P.val + h.va0, vb, &G.bar[s], pol);
     }
   }
 }
@@ -380,6 +401,7 @@ template <typename VT, typename F>
 __device__ bool stg_loop(const TeamDesc<VT>& P, Stager<VT>& G, int t0, int t1, int ncols,
                          const VT* vec, F&& body, bool csr = false) {
   const uint64_t LIMIT = 1000000000ull;
+  stg_plan(G, ncols, vec != nullptr, csr);
   const int S = G.S;
   if (threadIdx.x < 32) {
     for (int j = 0; j < S && t0 + j < t1; ++j) {
@@ -420,16 +442,16 @@ __device__ bool stg_loop(const TeamDesc<VT>& P, Stager<VT>& G, int t0, int t1, i
 // shared memory; x gathered from global memory), L lanes per row, groups of up
 // to 4 passes as in spmv_tile
 template <typename VT, int L>
-__device__ __forceinline__ void spmv_tile_stg(const TeamDesc<VT>& P, LzShared<VT>& sh, int base,
+__device__ __forceinline__ void spmv_tile_stg(const TeamDesc<VT>& P, LzShared<VT>& sh,
+                                              const Stager<VT>& G, int base,
                                               const unsigned char* stg, const VT* xsrc) {
   typedef typename Acc<VT>::type AT;
-  typedef StgLayout<VT> SL;
   constexpr int GPP = LZ_BLOCK / L;
   constexpr int CH = L < 4 ? L : 4;
-  const StgHdr h = *(const StgHdr*)(stg + SL::hdr);
-  const int* rp = (const int*)(stg + SL::rp);
-  const int* cs = (const int*)(stg + SL::col);
-  VT* vs = (VT*)(stg + SL::val);
+  const StgHdr h = *(const StgHdr*)(stg + G.hdr);
+  const int* rp = (const int*)(stg + G.rp);
+  const int* cs = (const int*)(stg + G.col);
+  VT* vs = (VT*)(stg + G.val);
   const int tid = threadIdx.x, g = tid / L, lig = tid - (tid / L) * L;
   const int rows = min(LZ_BLOCK, P.n - base);
   // fully staged tile: every product v x[c] of the tile at once (about nnz /
@@ -456,6 +478,7 @@ __device__ __forceinline__ void spmv_tile_stg(const TeamDesc<VT>& P, LzShared<VT
           if (p < p1) vs[p - h.va0] = vs[p - h.va0] * xv[u];
         }
       }
+      fence_proxy_async_smem();   // the stage is refilled by bulk copies later
       __syncthreads();
       if (tid < rows) {
         AT sacc = (AT)0;
@@ -518,12 +541,12 @@ __device__ void stg_phase_spmv(const TeamDesc<VT>& P, LzShared<VT>& sh, Stager<V
     if (csr) {
       const unsigned char* stg = G.raw(sidx);
       switch (L) {
-        case 1: spmv_tile_stg<VT, 1>(P, sh, base, stg, xsrc); break;
-        case 2: spmv_tile_stg<VT, 2>(P, sh, base, stg, xsrc); break;
-        case 4: spmv_tile_stg<VT, 4>(P, sh, base, stg, xsrc); break;
-        case 8: spmv_tile_stg<VT, 8>(P, sh, base, stg, xsrc); break;
-        case 16: spmv_tile_stg<VT, 16>(P, sh, base, stg, xsrc); break;
-        default: spmv_tile_stg<VT, 32>(P, sh, base, stg, xsrc); break;
+        case 1: spmv_tile_stg<VT, 1>(P, sh, G, base, stg, xsrc); break;
+        case 2: spmv_tile_stg<VT, 2>(P, sh, G, base, stg, xsrc); break;
+        case 4: spmv_tile_stg<VT, 4>(P, sh, G, base, stg, xsrc); break;
+        case 8: spmv_tile_stg<VT, 8>(P, sh, G, base, stg, xsrc); break;
+        case 16: spmv_tile_stg<VT, 16>(P, sh, G, base, stg, xsrc); break;
+        default: spmv_tile_stg<VT, 32>(P, sh, G, base, stg, xsrc); break;
       }
     } else {
       switch (L) {
@@ -542,7 +565,7 @@ __device__ void stg_phase_spmv(const TeamDesc<VT>& P, LzShared<VT>& sh, Stager<V
       vout[row] = y;
       VT xn = (VT)0;
       if (wq) {
-        xn = stq[(size_t)MP1 * LZ_BLOCK + tid] * xscale;
+        xn = stq[(size_t)G.vcol * LZ_BLOCK + tid] * xscale;
         P.Q[(size_t)i * ld + row] = xn;
       }
 #pragma unroll
@@ -579,7 +602,7 @@ __device__ void stg_phase_update_dot(const TeamDesc<VT>& P, LzShared<VT>& sh, St
           s += qr[c] * sh.hv[c];
         }
       }
-      const VT q1 = stq[(size_t)MP1 * LZ_BLOCK + tid] - s;
+      const VT q1 = stq[(size_t)G.vcol * LZ_BLOCK + tid] - s;
       buf[row] = q1;
 #pragma unroll
       for (int c = 0; c < MP1; ++c)
@@ -604,7 +627,7 @@ __device__ void stg_phase_update_norm(const TeamDesc<VT>& P, LzShared<VT>& sh, S
 #pragma unroll
       for (int c = 0; c < MP1; ++c)
         if (c < nv) s += stq[(size_t)c * LZ_BLOCK + tid] * sh.hv[c];
-      const VT q2 = stq[(size_t)MP1 * LZ_BLOCK + tid] - s;
+      const VT q2 = stq[(size_t)G.vcol * LZ_BLOCK + tid] - s;
       buf[row] = q2;
       nrm += (AT)q2 * (AT)q2;
     }
@@ -832,6 +855,13 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
   const int rank = (int)blockIdx.x - P.first_cta, R = P.nctas;
   const int tid = threadIdx.x;
   TeamBarrier bar{P.bar, R, P.status};
+  // staged phases read Q and the work vectors with bulk copies (async proxy):
+  // every thread fences its generic global stores before each team barrier
+  const bool staged = P.stages != 0;
+  auto team_sync = [&]() -> bool {
+    if (staged) fence_proxy_async_global();
+    return bar.sync();
+  };
   const int n = P.n, m = P.m;
   const size_t ld = (size_t)P.ld;
   const int ntiles = (n + LZ_BLOCK - 1) / LZ_BLOCK;
@@ -857,19 +887,22 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
   } while (0)
   if (rank == 0 && tid < MAXM) { sh.alpha[tid] = 0.0; sh.beta[tid] = 0.0; }
   if (tid == 0) sh.eig_cycles = 0;
-  // staged tiles (large problems): stages of STG_COLS x LZ_BLOCK values, then
-  // one mbarrier per stage, in the dynamic shared memory
-  extern __shared__ __align__(16) unsigned char lz_dyn[];
+  // staged tiles (large problems): the stage area (laid out per phase), then
+  // STG_MAXS mbarriers, in the dynamic shared memory
+  extern __shared__ __align__(128) unsigned char lz_dyn[];
   Stager<VT> G;
-  G.S = P.stages;
+  G.budget = (unsigned)P.stg_budget;
+  G.cap = P.stg_cap;
   G.csr = P.stage_csr;
+  G.S = 0;
+  G.bytes = 0;
+  G.vcol = 0;
   G.ph = 0u;
   G.nx_p0 = G.nx_p1 = 0;
   G.base = lz_dyn;
-  G.bytes = P.stage_csr ? (StgLayout<VT>::with_csr + 15) / 16 * 16 : StgLayout<VT>::q_only;
-  G.bar = (uint64_t*)(lz_dyn + (size_t)(P.stages > 0 ? P.stages : 0) * G.bytes);
-  if (P.stages > 0 && tid == 0) {
-    for (int j = 0; j < P.stages; ++j) mbar_init(&G.bar[j], 1);
+  G.bar = (uint64_t*)(lz_dyn + (size_t)G.budget);
+  if (P.stages && tid == 0) {
+    for (int j = 0; j < STG_MAXS; ++j) mbar_init(&G.bar[j], 1);
     mbar_init_fence();
   }
   __syncthreads();
@@ -894,13 +927,13 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
           ++breakdowns;
           VT* buf = P.vbuf + (size_t)prev * ld;
           phase_random(P, sh, t0, t1, i, (uint64_t)i, buf, part0 + rank);
-          if (!bar.sync()) return;
+          if (!team_sync()) return;
           reduce_part(part0, R, i, sh);
           phase_update_dot(P, sh, t0, t1, i, buf, part1 + rank);
-          if (!bar.sync()) return;
+          if (!team_sync()) return;
           reduce_part(part1, R, i, sh);
           phase_update_norm(P, sh, t0, t1, i, buf, part2 + rank);
-          if (!bar.sync()) return;
+          if (!team_sync()) return;
           reduce_part(part2, R, 1, sh);
           invb = (VT)(1.0 / sqrt(sh.h[0]));
         } else {
@@ -914,7 +947,7 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
       if (P.stages) stg_phase_spmv(P, sh, G, t0, t1, i, xsrc, invb, wq, vout, part0 + rank);
       else phase_spmv(P, sh, t0, t1, i, xsrc, invb, wq, vout, part0 + rank);
       LZ_MARK(2);
-      if (!bar.sync()) return;
+      if (!team_sync()) return;
       LZ_MARK(0);
       reduce_part(part0, R, i + 1, sh);
       LZ_MARK(1);
@@ -922,7 +955,7 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
       if (P.stages) stg_phase_update_dot(P, sh, G, t0, t1, i + 1, vout, part1 + rank);
       else phase_update_dot(P, sh, t0, t1, i + 1, vout, part1 + rank);
       LZ_MARK(3);
-      if (!bar.sync()) return;
+      if (!team_sync()) return;
       LZ_MARK(0);
       reduce_part(part1, R, i + 1, sh);
       LZ_MARK(1);
@@ -930,7 +963,7 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
       if (P.stages) stg_phase_update_norm(P, sh, G, t0, t1, i + 1, vout, part2 + rank);
       else phase_update_norm(P, sh, t0, t1, i + 1, vout, part2 + rank);
       LZ_MARK(4);
-      if (!bar.sync()) return;
+      if (!team_sync()) return;
       LZ_MARK(0);
       prev = cur;
       cur ^= 1;
@@ -947,13 +980,13 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
         ++breakdowns;
         VT* buf = P.vbuf + (size_t)prev * ld;
         phase_random(P, sh, t0, t1, m, (uint64_t)m, buf, part0 + rank);
-        if (!bar.sync()) return;
+        if (!team_sync()) return;
         reduce_part(part0, R, m, sh);
         phase_update_dot(P, sh, t0, t1, m, buf, part1 + rank);
-        if (!bar.sync()) return;
+        if (!team_sync()) return;
         reduce_part(part1, R, m, sh);
         phase_update_norm(P, sh, t0, t1, m, buf, part2 + rank);
-        if (!bar.sync()) return;
+        if (!team_sync()) return;
         reduce_part(part2, R, 1, sh);
         invb = (VT)(1.0 / sqrt(sh.h[0]));
       } else {
@@ -966,7 +999,7 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
       restart_select<false>(P, sh, k);
       clk_restart += clock64() - c0;
     }
-    if (!bar.sync()) return;
+    if (!team_sync()) return;
     const int kn = __ldcg(P.ctl + 0);
     nconv = __ldcg(P.ctl + 1);
     for (int e = tid; e < m * MAXM; e += LZ_BLOCK) {
@@ -998,7 +1031,7 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
     k = kn;
     sum_kn += kn;
     ++restart;
-    if (!bar.sync()) return;
+    if (!team_sync()) return;
     if (timing) tmark = clock64();   // restart time is reported separately (ctl[6])
   }
   if (rank == 0 && tid == 0) {
@@ -1511,6 +1544,18 @@ int lanczos_team_size(const DeviceInfo& di, int n, int prec) {
   return want;
 }
 
+// team kernel: dynamic shared memory it may use (x staged, or the stage area
+// plus its mbarriers) and the stage area itself
+template <typename VT>
+constexpr size_t tm_dyn_max() {
+  return (227 * 1024 - sizeof(LzShared<VT>) - 1024) / 128 * 128;
+}
+template <typename VT>
+constexpr unsigned tm_budget() {
+  return (unsigned)((tm_dyn_max<VT>() - STG_MAXS * sizeof(uint64_t)) / 128 * 128);
+}
+static_assert(tm_dyn_max<double>() >= (size_t)LZ_XS_BYTES, "staged x must fit");
+
 template <typename VT>
 static int run_typed(const DeviceInfo& di, const LanczosProblem* probs, int count,
                      cudaStream_t stream) {
@@ -1561,21 +1606,28 @@ static int run_typed(const DeviceInfo& di, const LanczosProblem* probs, int coun
       // 16-byte aligned Q and work vectors
       t.stages = 0;
       t.stage_csr = 0;
+      t.stg_budget = 0;
+      t.stg_cap = 0;
       if (!t.xsmem && p.ld % 32 == 0 && ((uintptr_t)p.Q & 15u) == 0 &&
           ((uintptr_t)p.work & 15u) == 0) {
-        // FP32 stages also carry the tile's CSR slice when two of them fit
-        // (bulk copies of rowptr / col / val need 16-byte aligned arrays)
-        const size_t csr_bytes = (StgLayout<VT>::with_csr + 15) / 16 * 16;
+        // the stage area takes the shared memory the kernel leaves; every
+        // phase keeps at least two of its largest stages in flight.  FP32
+        // stages also carry the tile's CSR slice, sized for 1.5x the mean
+        // tile (bulk copies of rowptr / col / val need 16-byte aligned arrays)
+        const unsigned budget = tm_budget<VT>();
+        const long long mean_tile = p.nnz * LZ_BLOCK / (p.n > 0 ? p.n : 1);
+        long long cap = (mean_tile * 3 / 2 + 63) / 64 * 64;
+        cap = cap < 512 ? 512 : (cap > STG_CAP ? STG_CAP : cap);
+        const unsigned qmax = stg_q_bytes<VT>(MP1 + 1);
         const bool csr_ok = sizeof(VT) == 4 && ((((uintptr_t)p.rowptr) | ((uintptr_t)p.col) |
                                                  ((uintptr_t)p.val)) & 15u) == 0 &&
-                            2 * csr_bytes + 64 <= (size_t)LZ_XS_BYTES;
-        const size_t stage_bytes = csr_ok ? csr_bytes : StgLayout<VT>::q_only;
-        int S = (int)(((size_t)LZ_XS_BYTES - 64) / stage_bytes);
-        if (S > 4) S = 4;
-        if (S >= 2) {
-          t.stages = S;
+                            2 * (qmax + stg_csr_bytes<VT>((int)cap)) <= budget;
+        if (2 * qmax <= budget) {
+          t.stages = 1;
           t.stage_csr = csr_ok ? 1 : 0;
-          const size_t need = (size_t)S * stage_bytes + (size_t)S * sizeof(uint64_t);
+          t.stg_budget = (int)budget;
+          t.stg_cap = (int)cap;
+          const size_t need = (size_t)budget + STG_MAXS * sizeof(uint64_t);
           if (need > dyn) dyn = need;
         }
       }
@@ -1601,7 +1653,7 @@ static int run_typed(const DeviceInfo& di, const LanczosProblem* probs, int coun
     static bool attr_set = false;
     if (!attr_set) {
       cudaFuncSetAttribute((const void*)lanczos_team_kernel<VT>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, LZ_XS_BYTES);
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tm_dyn_max<VT>());
       attr_set = true;
     }
     cudaError_t e = cudaLaunchCooperativeKernel((const void*)lanczos_team_kernel<VT>,
@@ -1746,14 +1798,14 @@ int lanczos_occupancy(int prec) {
   int occ = 0;
   if (prec == 64) {
     cudaFuncSetAttribute((const void*)lanczos_team_kernel<double>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, LZ_XS_BYTES);
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tm_dyn_max<double>());
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lanczos_team_kernel<double>, LZ_BLOCK,
-                                                  LZ_XS_BYTES);
+                                                  tm_dyn_max<double>());
   } else {
     cudaFuncSetAttribute((const void*)lanczos_team_kernel<float>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, LZ_XS_BYTES);
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)tm_dyn_max<float>());
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, lanczos_team_kernel<float>, LZ_BLOCK,
-                                                  LZ_XS_BYTES);
+                                                  tm_dyn_max<float>());
   }
   return occ;
 }

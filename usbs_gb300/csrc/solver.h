@@ -49,6 +49,7 @@ enum ScalarSlot {
 enum TraceField {
   TR_T = 0, TR_PRIMAL, TR_OBJUB, TR_OBJGAP, TR_INFGAP, TR_MAXINF, TR_PEN, TR_CANDPEN, TR_LB,
   TR_LAM0, TR_DESCENT, TR_ETA, TR_TRS, TR_TRX, TR_QITERS, TR_LITERS, TR_BPO, TR_TRXBAR,
+  TR_BY,           // b . y after the iteration (the reference's printed dual_obj)
   TR_NUM = 20
 };
 

@@ -585,6 +585,7 @@ __global__ void post_kernel(PostArgs a) {
     r[TR_LB] = lb; r[TR_LAM0] = lam0; r[TR_DESCENT] = descent ? 1.0 : 0.0; r[TR_ETA] = eta;
     r[TR_TRS] = sc[SC_TRS]; r[TR_TRX] = trX_n; r[TR_QITERS] = sc[SC_QITERS];
     r[TR_LITERS] = sc[SC_LITERS]; r[TR_BPO] = bpo_n; r[TR_TRXBAR] = trXb_n;
+    r[TR_BY] = descent ? byc : sc[SC_BY];
   }
 }
 
@@ -1347,12 +1348,23 @@ int usbs_solve(const usbs_problem* P, const usbs_params* Pa, usbs_state* S, void
   };
   double curr_time = 0.0;
   auto cond = [&](int t, bool* go) -> int {
-    double g[3];
-    CK(X.read_scalars(g, SC_OBJGAP, 3));
+    double sc[SC_NUM];
+    CK(X.read_scalars(sc, 0, SC_NUM));
+    double* r = S->cond;
+    for (int f = 0; f < TR_NUM; ++f) r[f] = 0.0;
+    r[TR_T] = t; r[TR_PRIMAL] = sc[SC_PRIMAL]; r[TR_OBJUB] = sc[SC_OBJUB];
+    r[TR_OBJGAP] = sc[SC_OBJGAP]; r[TR_INFGAP] = sc[SC_INFGAP]; r[TR_MAXINF] = sc[SC_MAXINF];
+    r[TR_PEN] = sc[SC_PEN]; r[TR_CANDPEN] = sc[SC_CANDPEN]; r[TR_LB] = sc[SC_LBEST];
+    r[TR_LAM0] = sc[SC_LAM0]; r[TR_DESCENT] = t > 0 ? sc[SC_DESCENT] : 0.0;
+    r[TR_ETA] = sc[SC_ETA]; r[TR_TRS] = sc[SC_TRS]; r[TR_TRX] = sc[SC_TRX];
+    r[TR_QITERS] = sc[SC_QITERS]; r[TR_LITERS] = sc[SC_LITERS]; r[TR_BPO] = sc[SC_BPO];
+    r[TR_TRXBAR] = sc[SC_TRXBAR];
+    // b . y of the current y: y_cand after a descent step (the post kernel's rule)
+    r[TR_BY] = (t > 0 && sc[SC_DESCENT] != 0.0) ? sc[SC_BYC] : sc[SC_BY];
     if (cb) cb(cb_user, t);
     *go = (t == 0) || ((curr_time < Pa->max_time) &&
-                       (g[0] > Pa->obj_gap_eps || g[1] > Pa->infeas_gap_eps ||
-                        g[2] > Pa->max_infeas_eps));
+                       (sc[SC_OBJGAP] > Pa->obj_gap_eps || sc[SC_INFGAP] > Pa->infeas_gap_eps ||
+                        sc[SC_MAXINF] > Pa->max_infeas_eps));
     return 0;
   };
   const std::vector<long long> sched = cond_schedule(Pa->max_iters, Pa->cond_exp_base);
@@ -1540,8 +1552,13 @@ int usbs_cgal_solve(const usbs_problem* P, const usbs_cgal_params* Pa, usbs_stat
     return 0;
   };
   auto cond = [&](int t, bool* go) -> int {
-    double g[3];
-    CK(read(g, CG_OBJGAP, 3));
+    double sc[CG_NUM];
+    CK(read(sc, 0, CG_NUM));
+    const double* g = sc + CG_OBJGAP;
+    double* r = S->cond;
+    for (int f = 0; f < TR_NUM; ++f) r[f] = 0.0;
+    r[0] = t; r[1] = sc[CG_EIG0]; r[2] = sc[CG_OBJGAP]; r[3] = sc[CG_INFGAP];
+    r[4] = sc[CG_MAXINF]; r[5] = sc[CG_PRIMAL]; r[6] = sc[CG_TRX]; r[7] = sc[CG_DSS];
     if (cb) cb(cb_user, t);
     *go = (t == 0) || ((curr_time < Pa->max_time) &&
                        (g[0] > Pa->obj_gap_eps || g[1] > Pa->infeas_gap_eps || g[2] > Pa->max_infeas_eps));

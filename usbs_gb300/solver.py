@@ -15,6 +15,7 @@ with FP64 subproblems, gaps and Rayleigh refinement), ``device``,
 :class:`DeviceProblem`, to skip the host layout step).
 """
 import ctypes
+import time
 
 import numpy as np
 import scipy.sparse as sp
@@ -59,7 +60,7 @@ class UsbsState(ctypes.Structure):
          ("pen_dual_obj", ctypes.c_double), ("elapsed", ctypes.c_double),
          ("status", ctypes.c_int), ("lanczos_launches", ctypes.c_int),
          ("lanczos_ms", ctypes.c_double), ("lanczos_bytes", ctypes.c_double),
-         ("kernel_launches", ctypes.c_longlong)]
+         ("kernel_launches", ctypes.c_longlong), ("cond", ctypes.c_double * 20)]
 
 
 class CgalParams(ctypes.Structure):
@@ -76,7 +77,29 @@ CALLBACK = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_int)
 
 TRACE_FIELDS = ["t", "primal_obj", "obj_ub", "obj_gap", "infeas_gap", "max_infeas",
                 "pen_dual_obj", "cand_pen_dual_obj", "lb_spec_est", "cand_eig0", "descent", "eta",
-                "trS", "tr_X", "quad_iters", "lb_iters", "bar_primal_obj", "tr_X_bar"]
+                "trS", "tr_X", "quad_iters", "lb_iters", "bar_primal_obj", "tr_X_bar", "dual_obj"]
+
+
+def log_line(rec, scale_c, scale_x, callback_val=None, curr_time=None):
+    """The line solver/usbs.py:514-530 prints at every condition check (field
+    names and order as the reference's), for the state record `rec` (trace
+    field names) of that check; curr_time defaults to the wall clock now."""
+    ct = time.time() if curr_time is None else curr_time
+    return (f"t: {int(rec['t'])} - curr_time: {ct} - pen_dual_obj: {rec['pen_dual_obj']}"
+            f" - cand_pen_dual_obj: {rec['cand_pen_dual_obj']} - lb_spec_est: {rec['lb_spec_est']}"
+            f" - primal_obj: {rec['primal_obj'] / (scale_c * scale_x)} - dual_obj: {rec['dual_obj']}"
+            f" - primal_obj_ub: {rec['obj_ub']} - obj_gap: {rec['obj_gap']}"
+            f" - infeas_gap: {rec['infeas_gap']} - max_infeas: {rec['max_infeas']}"
+            f" - callback_val: {callback_val}")
+
+
+def cgal_log_line(rec, scale_c, scale_x, callback_val=None, curr_time=None):
+    """The line solver/cgal.py:79-88 prints at every condition check."""
+    ct = time.time() if curr_time is None else curr_time
+    return (f"t: {int(rec['t'])} - curr_time: {ct} - primal_obj: "
+            f"{rec['primal_obj'] / (scale_c * scale_x)} - obj_gap: {rec['obj_gap']}"
+            f" - infeas_gap: {rec['infeas_gap']} - max_infeas: {rec['max_infeas']}"
+            f" - callback_val: {callback_val}")
 TRACE_WIDTH = 20
 
 
@@ -172,7 +195,9 @@ def usbs(sdp_state, n, m, trace_ub, trace_factor, rho, beta, k_curr, k_past, max
          lanczos_max_restarts, subprob_eps, subprob_max_iters, cond_exp_base=1.0,
          callback_fn=None, callback_static_args=None, callback_nonstatic_args=None, *, q0=None,
          precision=64, device="cuda", return_trace=False, return_info=False, instance=None,
-         stream=None, debug=None):
+         stream=None, debug=None, log=None):
+    """``log``: True prints, a callable receives, the reference's per-check
+    line (solver/usbs.py:514-530) at every condition check, t = 0 included."""
     import torch
     if not torch.cuda.is_available():
         raise RuntimeError("usbs_gb300.usbs needs a CUDA device (GB300); none is visible")
@@ -205,6 +230,7 @@ def usbs(sdp_state, n, m, trace_ub, trace_factor, rho, beta, k_curr, k_past, max
     q0t = _to_dev(default_q0(n) if q0 is None else q0, dev)
     trace = torch.zeros((max(max_iters, 1), TRACE_WIDTH), dtype=f64, device=dev) \
         if return_trace else None
+    log_fn = print if log is True else log
 
     prm = UsbsParams()
     prm.trace_ub, prm.trace_factor, prm.rho, prm.beta = trace_ub, trace_factor, rho, beta
@@ -233,6 +259,10 @@ def usbs(sdp_state, n, m, trace_ub, trace_factor, rho, beta, k_curr, k_past, max
         if callback_fn is not None and Om is not None:
             cb_val[t] = callback_fn(Pm[:, :n].t(), Om[:, :n].t(), callback_static_args,
                                     callback_nonstatic_args)
+        if log_fn is not None:
+            rec = {f: float(pst.cond[i]) for i, f in enumerate(TRACE_FIELDS)}
+            log_fn(log_line(rec, float(sdp_state.SCALE_C), float(sdp_state.SCALE_X),
+                            cb_val.get(t)))
 
     ccb = CALLBACK(_cb)
     st = stream if stream is not None else torch.cuda.current_stream(dev)
@@ -270,7 +300,7 @@ def cgal(sdp_state, n, m, trace_ub, beta0, max_iters, max_time, obj_gap_eps, inf
          max_infeas_eps, lanczos_inner_iterations, lanczos_max_restarts, subprob_eps,
          cond_exp_base=1.0, callback_fn=None, callback_static_args=None,
          callback_nonstatic_args=None, *, q0=None, precision=64, device="cuda",
-         return_trace=False, return_info=False, instance=None, stream=None):
+         return_trace=False, return_info=False, instance=None, stream=None, log=None):
     """cgal() of solver/cgal.py:21-243 (same positional arguments), run by the
     device driver ``usbs_cgal_solve``.  Returns the updated SDPState; with
     ``return_trace`` also a list of per-iteration records, with
@@ -324,10 +354,16 @@ def cgal(sdp_state, n, m, trace_ub, beta0, max_iters, max_time, obj_gap_eps, inf
     ws = torch.empty(need, dtype=torch.uint8, device=dev)
     cb_val = {}
 
+    log_fn = print if log is True else log
+
     def _cb(_user, t):
         if callback_fn is not None and Om is not None:
             cb_val[t] = callback_fn(Pm[:, :n].t(), Om[:, :n].t(), callback_static_args,
                                     callback_nonstatic_args)
+        if log_fn is not None:
+            rec = {f: float(pst.cond[i]) for i, f in enumerate(CGAL_TRACE_FIELDS)}
+            log_fn(cgal_log_line(rec, float(sdp_state.SCALE_C), float(sdp_state.SCALE_X),
+                                 cb_val.get(t)))
 
     ccb = CALLBACK(_cb)
     st = stream if stream is not None else torch.cuda.current_stream(dev)
