@@ -45,8 +45,13 @@ struct TeamDesc {
   const int* rowptr;
   const int* col;
   const VT* val;
-  VT* Q;
-  VT* vbuf;
+  VT* Q;                 // the caller's basis, ld x (m+1) column-major
+  // working basis: element (c, row) at Qw[qix(c, row)].  Staged teams keep it
+  // tile-major in the workspace (each 256-row tile's m+1 columns contiguous,
+  // so one bulk copy moves a tile's active columns); otherwise it is Q.
+  VT* Qw;
+  long long qts, qcs;    // tile and column strides (elements)
+  VT* vbuf;              // 3 flat vectors: two work vectors, then Q[:, k] of the cycle
   double* part;
   double* Ybuf;
   double* alpha;
@@ -55,6 +60,12 @@ struct TeamDesc {
   unsigned int* bar;
   int* status;
 };
+
+template <typename VT>
+__device__ __forceinline__ size_t qix(const TeamDesc<VT>& P, int c, int row) {
+  return (size_t)(row / LZ_BLOCK) * (size_t)P.qts + (size_t)c * (size_t)P.qcs +
+         (size_t)(row % LZ_BLOCK);
+}
 
 template <typename VT>
 struct TeamBatch {
@@ -241,12 +252,12 @@ __device__ void phase_spmv(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0, int 
       VT xn = (VT)0;
       if (wq) {
         xn = __ldcg(xsrc + row) * xscale;
-        P.Q[(size_t)i * ld + row] = xn;
+        P.Qw[qix(P, i, row)] = xn;
       }
 #pragma unroll
       for (int c = 0; c < MP1; ++c) {
         if (c <= i) {
-          const VT qc = (wq && c == i) ? xn : P.Q[(size_t)c * ld + row];
+          const VT qc = (wq && c == i) ? xn : P.Qw[qix(P, c, row)];
           acc[c] += (AT)qc * (AT)y;
         }
       }
@@ -331,7 +342,7 @@ __device__ void stg_issue(const TeamDesc<VT>& P, Stager<VT>& G, int s, int tile,
   // ld is a multiple of 32 >= n, so the padded rows stay inside each column
   const unsigned bytes = (unsigned)(((rows + E16 - 1) / E16) * E16 * (int)sizeof(VT));
   VT* st = G.stage(s);
-  unsigned tx = bytes * (unsigned)(ncols + (vec ? 1 : 0));
+  unsigned tx = stg_q_bytes<VT>(ncols) + (vec ? bytes : 0u);
   // CSR slice of the tile (phase A of FP32 stages): rowptr[r0 ..], col and val
   // over [p0, p1), each widened to 16-byte boundaries inside its array; the
   // few elements past an array's last full 16-byte block, and every entry of
@@ -370,14 +381,19 @@ __device__ void stg_issue(const TeamDesc<VT>& P, Stager<VT>& G, int s, int tile,
   // streamed once per phase: evict_first, so the copies do not push the SpMV's
   // x (gathered with evict_last) out of L2
   const uint64_t pol = l2_evict_first_policy();
-  const int ncopies = ncols + (vec ? 1 : 0) + (csr ? 3 : 0);
-  for (int j = lane; j < ncopies; j += 32) {
-    if (j < ncols) {
-      bulk_g2s_hint(st + (size_t)j * LZ_BLOCK, P.Q + (size_t)j * P.ld + r0, bytes, &G.bar[s], pol);
-    } else if (vec && j == ncols) {
+  // the tile's first ncols columns are contiguous in the tile-major basis
+  // (full 256-row columns; the last tile is padded): one copy
+  const int nq = ncols > 0 ? 1 : 0;
+  const int ncopies = nq + (vec ? 1 : 0) + (csr ? 3 : 0);
+  if (lane < ncopies) {
+    const int j = lane;
+    if (j < nq) {
+      bulk_g2s_hint(st, P.Qw + (size_t)tile * (size_t)P.qts, stg_q_bytes<VT>(ncols), &G.bar[s],
+                    pol);
+    } else if (vec && j == nq) {
       bulk_g2s_hint(st + (size_t)G.vcol * LZ_BLOCK, vec + r0, bytes, &G.bar[s], pol);
     } else {
-      const int k = j - ncols - (vec ? 1 : 0);   // 0 rowptr, 1 col, 2 val
+      const int k = j - nq - (vec ? 1 : 0);   // 0 rowptr, 1 col, 2 val
       if (k == 0 && rb) bulk_g2s_hint(G.raw(s) + G.rp, P.rowptr + r0, rb, &G.bar[s], pol);
       if (k == 1 && cb) bulk_g2s_hint(G.raw(s) + G.col, P.col + h.ca0, cb, &G.bar[s], pol);
       if (k == 2 && vb) bulk_g2s_hint(G.raw(s) + G.val, P.val + h.va0, vb, &G.bar[s], pol);
@@ -461,7 +477,7 @@ __device__ __forceinline__ void spmv_tile_stg(const TeamDesc<VT>& P, LzShared<VT
     const int p0 = rp[0], p1 = rp[rows];
     if (p1 <= h.ca1 && p1 <= h.va1) {
       const uint64_t keep = l2_evict_last_policy();
-      constexpr int U = 8;
+      constexpr int U = 16;   // one round of gathers for slices up to STG_CAP entries
       for (int pb = p0 + tid; pb < p1; pb += U * LZ_BLOCK) {
         int c[U];
         VT xv[U];
@@ -566,7 +582,7 @@ __device__ void stg_phase_spmv(const TeamDesc<VT>& P, LzShared<VT>& sh, Stager<V
       VT xn = (VT)0;
       if (wq) {
         xn = stq[(size_t)G.vcol * LZ_BLOCK + tid] * xscale;
-        P.Q[(size_t)i * ld + row] = xn;
+        P.Qw[qix(P, i, row)] = xn;
       }
 #pragma unroll
       for (int c = 0; c < MP1; ++c) {
@@ -653,7 +669,7 @@ __device__ void phase_random(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0, in
       buf[row] = r;
 #pragma unroll
       for (int c = 0; c < MP1; ++c)
-        if (c < nv) acc[c] += (AT)P.Q[(size_t)c * ld + row] * (AT)r;
+        if (c < nv) acc[c] += (AT)P.Qw[qix(P, c, row)] * (AT)r;
     }
   }
   block_reduce_cols(acc, nv, sh, part_out, P.nctas);
@@ -676,7 +692,7 @@ __device__ void phase_update_dot(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0
 #pragma unroll
       for (int c = 0; c < MP1; ++c) {
         if (c < nv) {
-          qr[c] = P.Q[(size_t)c * ld + row];
+          qr[c] = P.Qw[qix(P, c, row)];
           s += qr[c] * sh.hv[c];
         }
       }
@@ -703,7 +719,7 @@ __device__ void phase_update_norm(const TeamDesc<VT>& P, LzShared<VT>& sh, int t
       VT s = (VT)0;
 #pragma unroll
       for (int c = 0; c < MP1; ++c)
-        if (c < nv) s += P.Q[(size_t)c * ld + row] * sh.hv[c];
+        if (c < nv) s += P.Qw[qix(P, c, row)] * sh.hv[c];
       const VT q2 = buf[row] - s;
       buf[row] = q2;
       nrm += (AT)q2 * (AT)q2;
@@ -889,7 +905,7 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
   if (tid == 0) sh.eig_cycles = 0;
   // staged tiles (large problems): the stage area (laid out per phase), then
   // STG_MAXS mbarriers, in the dynamic shared memory
-  extern __shared__ __align__(128) unsigned char lz_dyn[];
+  extern __shared__ __align__(16) unsigned char lz_dyn[];
   Stager<VT> G;
   G.budget = (unsigned)P.stg_budget;
   G.cap = P.stg_cap;
@@ -905,7 +921,20 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
     for (int j = 0; j < STG_MAXS; ++j) mbar_init(&G.bar[j], 1);
     mbar_init_fence();
   }
+  // the start vector Q[:, 0]: flat copy for the first cycle's gathers and, for
+  // a tile-major working basis, its column 0 (own rows)
+  VT* xk = P.vbuf + 2 * ld;
+  const bool tiled = P.Qw != P.Q;
+  for (int tile = t0; tile < t1; ++tile) {
+    const int row = tile * LZ_BLOCK + tid;
+    if (row < n) {
+      const VT v = P.Q[row];
+      xk[row] = v;
+      if (tiled) P.Qw[qix(P, 0, row)] = v;
+    }
+  }
   __syncthreads();
+  if (!team_sync()) return;
   int prev = 0;          // vbuf slot holding the latest unnormalised vector
   VT invb = (VT)1;       // its normalisation
   while (nconv < P.num_desired && restart < P.max_restarts) {
@@ -914,7 +943,7 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
       const VT* xsrc;
       bool wq;
       if (i == k) {
-        xsrc = P.Q + (size_t)k * ld;
+        xsrc = xk;       // = Q[:, k]
         invb = (VT)1;
         wq = false;
       } else {
@@ -1007,25 +1036,25 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
       sh.u.Ys[e] = (c < kn) ? (VT)__ldcg(P.Ybuf + j * m + c) : (VT)0;
     }
     __syncthreads();
-    const VT* last = stepped ? (P.vbuf + (size_t)prev * ld) : (P.Q + (size_t)m * ld);
-    const VT lscale = stepped ? invb : (VT)1;
+    const VT* lastv = P.vbuf + (size_t)prev * ld;
     for (int tile = t0; tile < t1; ++tile) {
       const int row = tile * LZ_BLOCK + tid;
       if (row < n) {
         VT qr[MAXM];
 #pragma unroll
-        for (int j = 0; j < MAXM; ++j) qr[j] = (j < m) ? P.Q[(size_t)j * ld + row] : (VT)0;
-        const VT xl = last[row] * lscale;
+        for (int j = 0; j < MAXM; ++j) qr[j] = (j < m) ? P.Qw[qix(P, j, row)] : (VT)0;
+        const VT xl = stepped ? lastv[row] * invb : P.Qw[qix(P, m, row)];
         for (int c = 0; c < kn; ++c) {
           if (c >= m) break;
           VT s = (VT)0;
 #pragma unroll
           for (int j = 0; j < MAXM; ++j)
             if (j < m) s += qr[j] * sh.u.Ys[j * MAXM + c];
-          P.Q[(size_t)c * ld + row] = s;
+          P.Qw[qix(P, c, row)] = s;
         }
-        P.Q[(size_t)kn * ld + row] = xl;
-        if (kn != m) P.Q[(size_t)m * ld + row] = xl;
+        P.Qw[qix(P, kn, row)] = xl;
+        if (kn != m) P.Qw[qix(P, m, row)] = xl;
+        xk[row] = xl;
       }
     }
     k = kn;
@@ -1033,6 +1062,14 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
     ++restart;
     if (!team_sync()) return;
     if (timing) tmark = clock64();   // restart time is reported separately (ctl[6])
+  }
+  // a tile-major working basis back to the caller's column-major Q (own rows)
+  if (tiled && restart > 0) {
+    for (int c = 0; c <= m; ++c)
+      for (int tile = t0; tile < t1; ++tile) {
+        const int row = tile * LZ_BLOCK + tid;
+        if (row < n) P.Q[(size_t)c * ld + row] = P.Qw[qix(P, c, row)];
+      }
   }
   if (rank == 0 && tid == 0) {
     P.ctl[2] = restart;
@@ -1507,13 +1544,20 @@ lanczos_cluster_kernel(const __grid_constant__ ClusterBatch<VT> batch) {
 
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
+// tile-major working basis of a staged team (x too large for shared memory)
+static size_t team_basis_bytes(int n, int m, size_t vt) {
+  if ((size_t)n * vt <= (size_t)LZ_XS_BYTES) return 0;
+  const size_t tiles = ((size_t)n + LZ_BLOCK - 1) / LZ_BLOCK;
+  return align256(tiles * (size_t)(m + 1) * LZ_BLOCK * vt);
+}
+
 size_t lanczos_workspace_bytes(int n, int ld, int m, int prec, int nctas) {
-  (void)n; (void)m;
   const size_t vt = (prec == 64) ? 8 : 4;
-  size_t b = align256(2 * (size_t)ld * vt);
+  size_t b = align256(3 * (size_t)ld * vt);
   b += align256((size_t)3 * nctas * MP1 * sizeof(double));
   b += align256((size_t)MAXM * MAXM * sizeof(double));
   b += 256;  // barrier counters
+  b += team_basis_bytes(n, m, vt);
   return b;
 }
 
@@ -1601,15 +1645,13 @@ static int run_typed(const DeviceInfo& di, const LanczosProblem* probs, int coun
       t.lanes = lanczos_lanes(p.n, p.nnz);
       t.xsmem = ((size_t)p.n * sizeof(VT) <= (size_t)LZ_XS_BYTES) ? 1 : 0;
       if (t.xsmem && (size_t)p.n * sizeof(VT) > dyn) dyn = (size_t)p.n * sizeof(VT);
-      // staged tiles when x is not staged: bulk copies need ld a multiple of 32
-      // (16-byte aligned column starts, padded rows inside the column) and
-      // 16-byte aligned Q and work vectors
+      // staged tiles when x is not staged: bulk copies from the workspace (the
+      // work vectors and the tile-major basis) need it 16-byte aligned
       t.stages = 0;
       t.stage_csr = 0;
       t.stg_budget = 0;
       t.stg_cap = 0;
-      if (!t.xsmem && p.ld % 32 == 0 && ((uintptr_t)p.Q & 15u) == 0 &&
-          ((uintptr_t)p.work & 15u) == 0) {
+      if (!t.xsmem && p.ld % 32 == 0 && ((uintptr_t)p.work & 15u) == 0) {
         // the stage area takes the shared memory the kernel leaves; every
         // phase keeps at least two of its largest stages in flight.  FP32
         // stages also carry the tile's CSR slice, sized for 1.5x the mean
@@ -1637,10 +1679,20 @@ static int run_typed(const DeviceInfo& di, const LanczosProblem* probs, int coun
       t.nnz = p.nnz;
       t.Q = (VT*)p.Q;
       char* w = (char*)p.work;
-      t.vbuf = (VT*)w; w += align256(2 * (size_t)p.ld * sizeof(VT));
+      t.vbuf = (VT*)w; w += align256(3 * (size_t)p.ld * sizeof(VT));
       t.part = (double*)w; w += align256((size_t)3 * want[i] * MP1 * sizeof(double));
       t.Ybuf = (double*)w; w += align256((size_t)MAXM * MAXM * sizeof(double));
-      t.bar = (unsigned int*)w;
+      t.bar = (unsigned int*)w; w += 256;
+      // staged teams work on a tile-major copy of the basis (workspace)
+      if (t.stages) {
+        t.Qw = (VT*)w;
+        t.qts = (long long)(p.m + 1) * LZ_BLOCK;
+        t.qcs = LZ_BLOCK;
+      } else {
+        t.Qw = t.Q;
+        t.qts = LZ_BLOCK;
+        t.qcs = p.ld;
+      }
       t.alpha = p.alpha; t.beta = p.beta; t.ctl = p.ctl; t.status = p.status;
       first += want[i];
       if (cudaMemsetAsync(t.bar, 0, 2 * sizeof(unsigned int), stream) != cudaSuccess ||
