@@ -1,5 +1,5 @@
 """MaxCut SDP builder (oracle).  Restates ``utils/maxcut_helpers.py:26-92``, the
-implicit / dual-only warm starts (``utils/maxcut_helpers.py:95-161, 232-289``) and
+implicit / explicit / dual-only warm starts (``utils/maxcut_helpers.py:95-289``) and
 the rounding callback ``compute_max_cut`` (``utils/maxcut_helpers.py:292-302``).
 
 Input ``W`` is the (symmetric or not) weighted adjacency matrix, as the reference
@@ -80,6 +80,48 @@ def get_implicit_warm_start_state(old, W, sketch_dim, Omega_pad=None):
     primal_obj = old.primal_obj - old_diag @ old.z + new_diag @ z
     st = SDPState(C=C, A_indices=A_indices, A_data=A_data, b=b, b_ineq_mask=mask, X=X, P=P,
                   Omega=Om, y=y, z=z, tr_X=old.tr_X, primal_obj=primal_obj,
+                  SCALE_C=1.0 / np.linalg.norm(C.data), SCALE_X=1.0 / float(n),
+                  SCALE_A=np.ones(m))
+    return scale_sdp_state(st)
+
+
+def get_explicit_warm_start_state(old, W, sketch_dim, Omega=None):
+    """utils/maxcut_helpers.py:164-229: the old iterate made explicit: dense X
+    padded with zeros, or the sketch's Nystrom factors with their trace
+    corrected to tr_X (E padded with zero rows) re-sketched by a fresh Omega
+    (key n, in place of PRNGKey(n)); z, tr_X and primal_obj recomputed."""
+    from .common import apply_A_operator_mx
+    from .operators import apply_A_operator_batched
+    old = unscale_sdp_state(old)
+    C = laplacian_objective(W)
+    n = C.shape[0]
+    n_old = old.C.shape[0]
+    A_data, A_indices, b, mask = get_all_problem_data(n)
+    m = n
+    X, Om, P = old.X, old.Omega, old.P
+    if old.X is not None:
+        X = np.zeros((n, n))
+        X[:n_old, :n_old] = old.X
+        z = apply_A_operator_mx(n, m, A_data, A_indices, X)
+        tr_X = float(np.trace(X))
+        primal_obj = float((C @ X).trace())
+    if old.P is not None:
+        Om = hash_normal_matrix(n, n, sketch_dim) if Omega is None else np.asarray(Omega)
+        E, Lam = reconstruct_from_sketch(old.Omega, old.P)
+        tr_offset = (old.tr_X - np.sum(Lam)) / Lam.shape[0]
+        Lam_c = Lam + tr_offset
+        Ep = np.zeros((n, E.shape[1]))
+        Ep[:n_old] = E
+        with np.errstate(invalid="ignore"):
+            S = Ep * np.sqrt(Lam_c)[None, :]
+        P = S @ (S.T @ Om)
+        z = apply_A_operator_batched(m, A_data, A_indices, S)
+        tr_X = float(np.sum(Lam_c))
+        primal_obj = float(np.trace(S.T @ (C @ S)))
+    y = np.zeros(m)
+    y[:old.b.shape[0]] = old.y
+    st = SDPState(C=C, A_indices=A_indices, A_data=A_data, b=b, b_ineq_mask=mask, X=X, P=P,
+                  Omega=Om, y=y, z=z, tr_X=tr_X, primal_obj=primal_obj,
                   SCALE_C=1.0 / np.linalg.norm(C.data), SCALE_X=1.0 / float(n),
                   SCALE_A=np.ones(m))
     return scale_sdp_state(st)
