@@ -186,6 +186,40 @@ __global__ void svec_project_kernel(int m, const int* __restrict__ con_ptr,
   }
 }
 
+// The three weight vectors of the A* projections side by side after Pm's s
+// columns: W[:, 0] = y, W[:, 1] = z_bar, W[:, 2] = b - upsilon (m each).
+__global__ void pack3_kernel(int m, const double* __restrict__ y, const double* __restrict__ zbar,
+                             const double* __restrict__ bmu, double* __restrict__ W) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < m; c += gridDim.x * blockDim.x) {
+    W[c] = y[c];
+    W[(size_t)m + c] = zbar[c];
+    W[(size_t)2 * m + c] = bmu[c];
+  }
+}
+
+// svec(V^T A*(w) V) = sum_c w_c Pm[c, :] for the three weight vectors (GW,
+// s x 3 row-major) back to k x k blocks: GYmC = V^T A*(y) V - V^T C V,
+// GZ = V^T A*(z_bar) V, GB = V^T A*(b - upsilon) V (symmetric: the IPM reads
+// them through svec only).  One block.
+__global__ void unpack_proj_kernel(int k, const double* __restrict__ GW,
+                                   const double* __restrict__ GC, double* __restrict__ GYmC,
+                                   double* __restrict__ GZ, double* __restrict__ GB) {
+  for (int e = threadIdx.x; e < k * k; e += blockDim.x) {
+    const int i = e / k, j = e - (e / k) * k;
+    const int b = i > j ? i : j, c = i > j ? j : i;
+    const int a = b * (b + 1) / 2 + c;
+    const double w = (b == c) ? 1.0 : RSQ2_S;
+    GYmC[e] = w * GW[a * 3 + 0] - GC[e];
+    GZ[e] = w * GW[a * 3 + 1];
+    GB[e] = w * GW[a * 3 + 2];
+  }
+}
+
+// S_init = trace_ub * 0.99 I / (k + 1): the alternating minimisation's start
+__global__ void sinit_kernel(int k, double v, double* __restrict__ S) {
+  for (int e = threadIdx.x; e < k * k; e += blockDim.x) S[e] = (e % (k + 1) == 0) ? v : 0.0;
+}
+
 // AF[c] = sum_t a_t V[i_t] S+ V[j_t]^T = A(F F^T)_c and AFc[c] with Sc+
 // (solver/usbs.py:411-412, 570-571, 627, 639).  One thread per constraint.
 __global__ void quadform_kernel(int m, const int* __restrict__ con_ptr,
@@ -614,7 +648,7 @@ struct Arena {
 struct Layout {
   int n, m, k, kc, kp, s, ssk, ld, mL, vt, grid_red, grid_gram;
   // smalls offsets
-  int o_QB, o_GC, o_GYmC, o_GZ, o_GB, o_GYC, o_VtO, o_Sout, o_Ssub, o_W, o_Splus, o_Scplus,
+  int o_QB, o_GC, o_GYmC, o_GZ, o_GB, o_GYC, o_GW, o_VtO, o_Sout, o_Ssub, o_W, o_Splus, o_Scplus,
       o_Wpast, o_M, o_Mc, o_G, o_Rinv, o_GR1, o_GR2, o_GR, o_sc, n_smalls;
   // buffers
   double *smalls, *CV, *CV2, *Vn, *op64, *op64b, *bmu, *AF, *AFc, *ycand, *zbar, *ups, *Pm,
@@ -640,6 +674,7 @@ static int plan(const usbs_problem* P, const usbs_params* Pa, const DeviceInfo& 
   auto take = [&](int cnt) { int r = o; o += (cnt + 3) & ~3; return r; };
   L.o_QB = take(L.s * L.s); L.o_GC = take(L.k * L.k); L.o_GYmC = take(L.k * L.k);
   L.o_GZ = take(L.k * L.k); L.o_GB = take(L.k * L.k); L.o_GYC = take(L.k * L.k);
+  L.o_GW = take(L.s * 3);
   L.o_VtO = take(L.k * (L.ssk > 0 ? L.ssk : 1)); L.o_Sout = take(L.k * L.k);
   L.o_Ssub = take(L.k * L.k); L.o_W = take(L.k * L.k); L.o_Splus = take(L.k * L.k);
   L.o_Scplus = take(L.k * L.k); L.o_Wpast = take(L.k * L.k);
@@ -656,7 +691,7 @@ static int plan(const usbs_problem* P, const usbs_params* Pa, const DeviceInfo& 
   L.opL = (Pa->precision == 64) ? (void*)L.op64 : (void*)ar.take<float>((size_t)(P->nnz > 0 ? P->nnz : 1));
   L.bmu = ar.take<double>(L.m); L.AF = ar.take<double>(L.m); L.AFc = ar.take<double>(L.m);
   L.ycand = ar.take<double>(L.m); L.zbar = ar.take<double>(L.m); L.ups = ar.take<double>(L.m);
-  L.Pm = ar.take<double>((size_t)L.m * L.s);
+  L.Pm = ar.take<double>((size_t)L.m * (L.s + 3));   // Pm, then the 3 weight columns
   L.gpart = ar.take<double>((size_t)L.grid_gram * L.s * L.s);
   L.gpart2 = ar.take<double>((size_t)L.grid_gram * L.k * L.k);
   L.mpart = ar.take<double>((size_t)L.grid_red * 8);
@@ -763,6 +798,20 @@ struct Solver {
     CK(spmm(val, V, L.k, cv, side));
     return gram(V, L.ld, L.k, cv, L.ld, L.k, L.n, L.smalls + o, side);
   }
+  // GYmC, GZ, GB from Pm (svec_project output) and GC: pack the weights, one
+  // Gram Pm^T [y z_bar b-upsilon], unpack (this stream)
+  int a_proj3() {
+    double* W = L.Pm + (size_t)L.m * L.s;
+    ++launches;
+    pack3_kernel<<<mgrid(), RED_BLOCK, 0, st>>>(L.m, S->y, L.zbar, L.bmu, W);
+    CK(kerr("pack3"));
+    CK(gram(L.Pm, L.m, L.s, W, L.m, 3, L.m, L.smalls + L.o_GW));
+    ++launches;
+    unpack_proj_kernel<<<1, 128, 0, st>>>(L.k, L.smalls + L.o_GW, L.smalls + L.o_GC,
+                                          L.smalls + L.o_GYmC, L.smalls + L.o_GZ,
+                                          L.smalls + L.o_GB);
+    return kerr("unpack_proj");
+  }
   MvecArgs margs() {
     MvecArgs a;
     a.m = L.m; a.smalls = L.smalls; a.o_sc = L.o_sc; a.y = S->y; a.z = S->z; a.zbar = L.zbar;
@@ -865,16 +914,21 @@ static int body(Solver& X, int t) {
   cudaStream_t st = X.st;
   double* V = S->V;
   // ---- projections onto the bundle basis (solver/usbs.py:54-61) ----
-  CK(X.proj(1.0, nullptr, V, L.o_GC));                // V^T C V
-  CK(X.proj(-1.0, S->y, V, L.o_GYmC));                // V^T (A*(y) - C) V
-  CK(X.proj(0.0, L.zbar, V, L.o_GZ));                 // V^T A*(z_bar) V
+  // V^T C V on the second stream (C V then the Gram) while this stream forms
+  // Pm[c, :] = svec(V^T A_c V) (create_Q_base's rows) and, from the same Pm,
+  // the three A* projections: svec(V^T A*(w) V) = Pm^T w for w = y, z_bar and
+  // b - upsilon, one Gram against the packed weight columns.
+  if (cudaEventRecord(X.ev_fork, st) != cudaSuccess ||
+      cudaStreamWaitEvent(X.st2, X.ev_fork, 0) != cudaSuccess)
+    return kerr("fork");
+  CK(X.proj(1.0, nullptr, V, L.o_GC, 1));             // V^T C V
+  if (cudaEventRecord(X.ev_join, X.st2) != cudaSuccess) return kerr("join record");
   {
     MvecArgs ma = X.margs();
     ++X.launches;
     mvec_pre_kernel<<<X.mgrid(), RED_BLOCK, 0, st>>>(ma, Pa->trace_ub, L.k, 1);
     CK(kerr("mvec_pre"));
   }
-  CK(X.proj(0.0, L.bmu, V, L.o_GB));                  // V^T A*(b - upsilon) V
   {
     int blocks = (int)(((long long)L.m * 32 + 255) / 256);
     if (blocks > X.di.sm_count * 16) blocks = X.di.sm_count * 16;
@@ -884,16 +938,14 @@ static int body(Solver& X, int t) {
     CK(kerr("svec_project"));
     CK(X.gram(L.Pm, L.m, L.s, L.Pm, L.m, L.s, L.m, L.smalls + L.o_QB));   // create_Q_base
   }
+  if (cudaStreamWaitEvent(st, X.ev_join, 0) != cudaSuccess) return kerr("join");
+  CK(X.a_proj3());
   if (L.ssk > 0) CK(X.gram(V, L.ld, L.k, S->Omega, L.ld, L.ssk, L.n, L.smalls + L.o_VtO));
   // alternating-minimisation initial point: S_init = trace_ub * 0.99 I / (k+1)
-  {
-    std::vector<double> Si((size_t)L.k * L.k, 0.0);
-    for (int i = 0; i < L.k; ++i) Si[(size_t)i * L.k + i] = Pa->trace_ub * (0.99 * (1.0 / (L.k + 1.0)));
-    if (cudaMemcpyAsync(L.smalls + L.o_Ssub, Si.data(), Si.size() * sizeof(double),
-                        cudaMemcpyHostToDevice, st) != cudaSuccess)
-      return kerr("S init");
-    cudaStreamSynchronize(st);
-  }
+  ++X.launches;
+  sinit_kernel<<<1, 128, 0, st>>>(L.k, Pa->trace_ub * (0.99 * (1.0 / (L.k + 1.0))),
+                                  L.smalls + L.o_Ssub);
+  CK(kerr("S init"));
   // ---- subproblem: IPM + alternating minimisation over upsilon (solver/usbs.py:359-433) ----
   EigSArgs ea;
   ea.k = L.k; ea.k_curr = L.kc; ea.ssk = L.ssk; ea.smalls = L.smalls; ea.o_sc = L.o_sc;
@@ -928,7 +980,7 @@ static int body(Solver& X, int t) {
       mvec_pre_kernel<<<X.mgrid(), RED_BLOCK, 0, st>>>(mb, Pa->trace_ub, L.k, 0);
       CK(kerr("mvec_pre"));
     }
-    CK(X.proj(0.0, L.bmu, V, L.o_GB));
+    CK(X.a_proj3());                                  // V^T A*(b - upsilon) V refreshed
   }
   // ---- z, y_cand, infeasibility, z_bar (solver/usbs.py:582-583, 638-639, 648-652) ----
   {
