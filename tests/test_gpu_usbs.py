@@ -1,6 +1,7 @@
 """GPU parity of the device USBS iteration against the FP64 oracle."""
 import numpy as np
 import pytest
+import scipy.sparse as sp
 
 from oracle import maxcut as omaxcut
 from oracle import rng as orng
@@ -164,3 +165,75 @@ def test_usbs_qap_fp64_trace_matches_oracle(cuda):
                     "max_infeas", "tr_X"):
             assert _rel(a[key], b[key]) < tol, (a["t"], key, a[key], b[key])
     np.testing.assert_allclose(gout.y.cpu().numpy(), oout.y, rtol=1e-3, atol=1e-5)
+
+
+def test_usbs_isolated_nodes_first_iteration(cuda):
+    """Resolved configuration (Lanczos to 1e-9), one outer iteration, on a graph
+    with many isolated nodes (zero rows of C; the pattern keeps only the
+    constraint diagonal there).  The 131 isolated nodes all get the same
+    y_cand entry, so -C + A*(y_cand) has a 131-fold eigenvalue that Lanczos
+    resolves only to its tolerance, in the oracle as here: 1e-7."""
+    W = wl.er_graph(300, 120, 9)
+    assert (np.asarray(W.sum(axis=1)).ravel() == 0).sum() > 100
+    st, oout, ofin, otr, gout, gtr, info = _run_both(W, 1, 64, k_curr=4, k_past=1, eps=1e-9,
+                                                     restarts=200)
+    assert info["status"] == 0
+    for key in ("primal_obj", "obj_ub", "lb_spec_est", "pen_dual_obj", "cand_pen_dual_obj",
+                "tr_X"):
+        assert _rel(otr[0][key], gtr[0][key]) < 1e-7, (key, otr[0][key], gtr[0][key])
+
+
+def _hub_graph(seed=0):
+    """12 hubs with 10, 12, ..., 32 leaves of their own and 40 random
+    leaf-leaf edges: the 12 smallest eigenvalues of -C are about 0.5 apart."""
+    rows, cols, nxt = [], [], 12
+    for h in range(12):
+        for _ in range(10 + 2 * h):
+            rows.append(h)
+            cols.append(nxt)
+            nxt += 1
+    rs = np.random.default_rng(seed)
+    for _ in range(40):
+        a, b = rs.integers(12, nxt, 2)
+        if a != b:
+            rows.append(a)
+            cols.append(b)
+    W = sp.coo_matrix((np.ones(len(rows)), (rows, cols)), shape=(nxt, nxt))
+    return sp.csr_matrix(((W + W.T) > 0).astype(float))
+
+
+def test_usbs_largest_bundle_first_iteration_1e9(cuda):
+    """k = k_curr + k_past = 12, the largest bundle the IPM takes (svec
+    dimension 78), one outer iteration at 1e-9 on the quantities the IPMs
+    determine.  eigsh_smallest returns alpha[:num_desired] after the
+    saved-first reordering (solver/lanczos.py:224-227, 280-281): past k_left + 1
+    of them these are Ritz values from the top of the spectrum, chosen by
+    argmax of the gap ratio.  On a well separated spectrum that choice does not
+    depend on rounding, so both sides take the same start vectors."""
+    W = _hub_graph()
+    st, oout, ofin, otr, gout, gtr, info = _run_both(W, 1, 64, k_curr=11, k_past=1, eps=1e-9,
+                                                     restarts=200)
+    assert info["status"] == 0
+    # (eta is degenerate at t = 0: z_bar = 0 and bar_primal_obj = 0, and it does
+    # not enter the iteration)
+    for key in ("primal_obj", "lb_spec_est", "tr_X", "trS"):
+        assert _rel(otr[0][key], gtr[0][key]) < 1e-9, (key, otr[0][key], gtr[0][key])
+
+
+def test_usbs_zero_iterations_returns_the_start(cuda):
+    """max_iters = 0: the loop runs no body (utils/loop.py:80-115); the state
+    comes back unchanged."""
+    from usbs_gb300 import solver
+    W = wl.er_graph(200, 1000, 3)
+    st = omaxcut.initialize_state(W, 10)
+    n = st.C.shape[0]
+    rs = np.random.default_rng(1)
+    st = st._replace(y=rs.standard_normal(n), P=rs.standard_normal((n, 10)), tr_X=3.0,
+                     primal_obj=1.5)
+    out, info = solver.usbs(st, n, n, 2.0 * n, 2.0, S["rho"], S["beta"], 10, 1, 0, np.inf, -1.0,
+                            -1.0, -1.0, 32, 10, 1e-7, 100, q0=orng.default_q0(n),
+                            return_info=True)
+    assert info["iterations"] == 0
+    np.testing.assert_array_equal(out.y.cpu().numpy(), st.y)
+    np.testing.assert_array_equal(out.P.cpu().numpy(), st.P)
+    assert out.tr_X == 3.0 and out.primal_obj == 1.5
