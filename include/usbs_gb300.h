@@ -318,6 +318,24 @@ int usbs_maxcut_round(int n, int s, const double* Omega, const double* P, int ld
                       double* value, double* column_values, unsigned* signs, void* workspace,
                       size_t workspace_bytes, void* stream);
 
+/* Workspace bytes of usbs_qap_round for l facilities (l <= 64) and a sketch
+ * of s <= 32 columns (0 for unsupported sizes). */
+size_t usbs_qap_round_workspace_bytes(int l, int s);
+
+/* qap_round (utils/qap_helpers.py:624-653): the QAP rounding callback.  Omega
+ * and P are (l^2 + 1) x s, column-major with leading dimension ld; W (flow)
+ * and D (distance) are l x l row-major.  For each of the first min(l, s)
+ * columns of the reconstructed E and for its negative, an optimal assignment
+ * of the cost max(c) - c (c = +-E[1:, i] as an l x l row-major matrix, row =
+ * facility) and its objective trace(W P D P^T).  *value (device) = the
+ * smaller of the minimum over the positive and over the negative candidates.
+ * candidate_values (2 min(l, s) doubles, positive first) and candidate_perms
+ * (2 min(l, s) x l ints: the location of each facility) may be NULL.
+ * Stream-ordered; device pointers. */
+int usbs_qap_round(int l, int s, const double* Omega, const double* P, int ld, const double* W,
+                   const double* D, double approx_eps, double* value, double* candidate_values,
+                   int* candidate_perms, void* workspace, size_t workspace_bytes, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -132,3 +132,36 @@ def initialize_state(D, W, sketch_dim, Omega=None):
                   Omega=Om, y=np.zeros(m), z=np.zeros(m), tr_X=0.0, primal_obj=0.0,
                   SCALE_C=SCALE_C, SCALE_X=SCALE_X, SCALE_A=SCALE_A)
     return scale_sdp_state(st)
+
+
+def qap_round(P, Omega, callback_static_args, callback_nonstatic_args):
+    """The QAP rounding callback (utils/qap_helpers.py:624-653): for every
+    column of the reconstructed E (and its negative), an optimal assignment on
+    the l x l cost max(c) - c with c = +-E[1:, i] reshaped row-major (row =
+    facility, column = location), scored by trace(W P D P^T); returns the
+    smaller of the two minima.  The reference's assignment solver is its own
+    Munkres (utils/munkres.py:13-120); this restatement uses SciPy's
+    linear_sum_assignment, which returns the same assignment whenever the
+    optimum is unique (costs from a reconstructed sketch have no ties)."""
+    import pickle
+    from scipy.optimize import linear_sum_assignment
+    from .common import reconstruct_from_sketch
+    static = callback_static_args
+    l = int(pickle.loads(static)["l"]) if isinstance(static, (bytes, bytearray)) else int(static)
+    D = np.asarray(callback_nonstatic_args["D"], float)
+    W = np.asarray(callback_nonstatic_args["W"], float)
+    E, _ = reconstruct_from_sketch(np.asarray(Omega, float), np.asarray(P, float))
+    if not np.all(np.isfinite(E)):
+        return float("nan")
+
+    def score(c):
+        c = c.reshape(l, l)
+        r, col = linear_sum_assignment(c.max() - c)
+        perm = np.zeros((l, l))
+        perm[r, col] = 1.0
+        return float(np.trace(W @ perm @ D @ perm.T))
+
+    cols = E.shape[1]
+    min_pos = min(score(E[1:, i]) for i in range(min(l, cols)))
+    min_neg = min(score(-E[1:, i]) for i in range(min(l, cols)))
+    return min_pos if min_pos < min_neg else min_neg

@@ -75,3 +75,22 @@ def test_operator_entry_points_reject_bad_sizes(lib):
     assert rc == -2 and "bad sizes" in _err(lib)
     rc = lib.usbs_apply_A_adjoint(100, 2, FAKE, FAKE, FAKE, FAKE, FAKE, FAKE, 99, FAKE, 128, None)
     assert rc == -2 and "bad sizes" in _err(lib)
+
+
+def test_qap_round_rejects_bad_sizes(lib):
+    assert lib.usbs_qap_round_workspace_bytes(30, 30) > 0
+    assert lib.usbs_qap_round_workspace_bytes(65, 8) == 0
+    assert lib.usbs_qap_round_workspace_bytes(30, 33) == 0
+    ws = lib.usbs_qap_round_workspace_bytes(10, 10)
+    rc = lib.usbs_qap_round(65, 10, FAKE, FAKE, 4232, FAKE, FAKE, 1e-6, FAKE, None, None, FAKE,
+                            ws, None)
+    assert rc == -2 and "l=65" in _err(lib)
+    rc = lib.usbs_qap_round(10, 10, FAKE, FAKE, 101, None, FAKE, 1e-6, FAKE, None, None, FAKE, ws,
+                            None)
+    assert rc == -2 and "null" in _err(lib)
+    rc = lib.usbs_qap_round(10, 10, FAKE, FAKE, 100, FAKE, FAKE, 1e-6, FAKE, None, None, FAKE, ws,
+                            None)
+    assert rc == -2 and "ld=100" in _err(lib)
+    rc = lib.usbs_qap_round(10, 10, FAKE, FAKE, 101, FAKE, FAKE, 1e-6, FAKE, None, None, FAKE,
+                            ws - 8, None)
+    assert rc == -2 and "workspace" in _err(lib)

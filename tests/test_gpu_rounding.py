@@ -175,3 +175,94 @@ def test_cgal_log_lines(cuda):
                      r" - infeas_gap: \S+ - max_infeas: \S+ - callback_val: None$")
     assert len(lines) == 7 and all(pat.match(l) for l in lines), lines[:2]
     assert [int(pat.match(l).group(1)) for l in lines] == list(range(7))
+
+
+def _lifted_perm_sketch(l, s, seed):
+    """Sketch of x x^T for the lifted vector of a random assignment (x_0 = 1,
+    x[1 + loc + l fac] = 1) plus a small PSD perturbation."""
+    rng = np.random.default_rng(seed)
+    perm = rng.permutation(l)
+    x = np.zeros(l * l + 1)
+    x[0] = 1.0
+    x[1 + perm + l * np.arange(l)] = 1.0
+    V = rng.standard_normal((l * l + 1, 3))
+    X = np.outer(x, x) + 1e-3 * (V @ V.T)
+    Om = rng.standard_normal((l * l + 1, s))
+    return perm, X @ Om, Om
+
+
+def _qap_candidates_oracle(E, l, D, W):
+    from scipy.optimize import linear_sum_assignment
+    out = []
+    for sgn in (1.0, -1.0):
+        for i in range(min(l, E.shape[1])):
+            c = (sgn * E[1:, i]).reshape(l, l)
+            r, col = linear_sum_assignment(c.max() - c)
+            pm = np.zeros((l, l))
+            pm[r, col] = 1.0
+            out.append((float(np.trace(W @ pm @ D @ pm.T)), col.copy()))
+    return out
+
+
+def test_qap_round_recovers_the_encoded_assignment(cuda):
+    """The dominant column of E is the lifted assignment vector: its
+    candidate (positive or negative, by the column's sign) is that assignment."""
+    from usbs_gb300 import rounding
+    l = 8
+    D, W = wl.qap_instance(l, 3, grid=5)
+    perm, P, Om = _lifted_perm_sketch(l, l, 4)
+    val, cand, perms = rounding.qap_round_values(P, Om, l, D, W)
+    perms = perms.cpu().numpy()
+    pm = np.zeros((l, l))
+    pm[np.arange(l), perm] = 1.0
+    obj = float(np.trace(W @ pm @ D @ pm.T))
+    assert (perms[0] == perm).all() or (perms[l] == perm).all()
+    j = 0 if (perms[0] == perm).all() else l
+    assert float(cand[j].item()) == obj
+    assert float(val.item()) <= obj
+
+
+@pytest.mark.parametrize("l,s,seed", [(6, 6, 0), (9, 9, 1), (12, 8, 2)])
+def test_qap_round_matches_oracle(cuda, l, s, seed):
+    """Value exact (integer W, D); each column's pair of candidates (the sign
+    of an E column is arbitrary) equal to the oracle's."""
+    import pickle
+    from oracle import qap as oqap
+    from usbs_gb300 import rounding
+    D, W = wl.qap_instance(l, seed, grid=5)
+    rng = np.random.default_rng(seed)
+    V = rng.standard_normal((l * l + 1, 2 * l))
+    X = (V * np.linspace(3.0, 0.1, 2 * l)) @ V.T
+    Om = rng.standard_normal((l * l + 1, s))
+    P = X @ Om
+    oval = oqap.qap_round(P, Om, pickle.dumps({"l": l}), {"D": D, "W": W})
+    val, cand, perms = rounding.qap_round_values(P, Om, l, D, W)
+    assert float(val.item()) == oval
+    oE, _ = ocommon.reconstruct_from_sketch(Om, P)
+    oc = _qap_candidates_oracle(oE, l, D, W)
+    s2 = min(l, s)
+    cand = cand.cpu().numpy()
+    for i in range(s2):
+        assert sorted([cand[i], cand[s2 + i]]) == sorted([oc[i][0], oc[s2 + i][0]]), i
+    assert rounding.qap_round(P, Om, pickle.dumps({"l": l}), {"D": D, "W": W}) == oval
+
+
+def test_usbs_qap_rounding_callback(cuda):
+    """qap_round as usbs()'s callback on the QAP relaxation: its value at the
+    last check equals the oracle's qap_round on the returned sketch."""
+    import pickle
+    from oracle import qap as oqap
+    from usbs_gb300 import rounding, solver
+    l = 5
+    D, Wf = wl.qap_instance(l, 0, grid=5)
+    st = oqap.initialize_state(D, Wf, l)
+    n, m = st.C.shape[0], st.b.shape[0]
+    trace_ub = 2.0 * float(l + 1) * st.SCALE_X
+    static, nonstatic = pickle.dumps({"l": l}), {"D": D, "W": Wf}
+    iters = 4
+    out, info = solver.usbs(st, n, m, trace_ub, 2.0, 0.005, 0.25, 2, 0, iters, np.inf, -1.0, -1.0,
+                            -1.0, min(n, 32), 300, 1e-9, 100, 1.0, rounding.qap_round, static,
+                            nonstatic, q0=orng.default_q0(n), precision=64, return_info=True)
+    assert info["iterations"] == iters
+    P = out.P.cpu().numpy()
+    assert info["callback_vals"][iters] == oqap.qap_round(P, st.Omega, static, nonstatic)

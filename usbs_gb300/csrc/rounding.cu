@@ -1,6 +1,6 @@
-// Sketch reconstruction and the MaxCut rounding callback on the device
-// (reference: utils/common.py:99-116 reconstruct_from_sketch,
-// utils/maxcut_helpers.py:292-302 compute_max_cut).
+// Sketch reconstruction and the rounding callbacks on the device (reference:
+// utils/common.py:99-116 reconstruct_from_sketch, utils/maxcut_helpers.py:
+// 292-302 compute_max_cut, utils/qap_helpers.py:624-653 qap_round).
 //
 // The reference forms P_rho = P + rho Omega with rho = sqrt(n) eps ||P||_2,
 // B = sym(Omega^T P_rho), L = chol(B), M = P_rho L^-T (its lstsq), the thin SVD
@@ -333,6 +333,127 @@ __global__ void rd_final_kernel(int s, int nblocks, const double* __restrict__ c
   }
 }
 
+// ---------------------------------------------------------------- QAP rounding
+// qap_round (utils/qap_helpers.py:624-653): for column i of E (i < min(l, s))
+// and both signs, the l x l cost max(c) - c with c = +-E[1:, i] reshaped
+// row-major (row = facility, column = location), an optimal assignment, and
+// its objective trace(W P D P^T) = sum_fg W[f][g] D[pi(f)][pi(g)].  One warp
+// per (column, sign): the shortest-augmenting-path Hungarian method with
+// row and column potentials (Kuhn 1955, Munkres 1957; O(l^3)), lanes owning
+// columns j = lane, lane + 32, ...  Every loop is bounded by l + 1.  A
+// non-finite cost (E is NaN where the reconstruction's Cholesky failed)
+// gives a NaN candidate, as min/compare over NaN does in the reference.
+constexpr int QAP_MAXL = 64;
+
+__global__ void __launch_bounds__(32) qap_lap_kernel(int l, int s2, const double* __restrict__ E,
+                                                      int lde, const double* __restrict__ W,
+                                                      const double* __restrict__ D,
+                                                      double* __restrict__ vals,
+                                                      int* __restrict__ perms) {
+  __shared__ double a[QAP_MAXL * QAP_MAXL];
+  __shared__ double u[QAP_MAXL + 1], v[QAP_MAXL + 1], minv[QAP_MAXL + 1];
+  __shared__ int p[QAP_MAXL + 1], way[QAP_MAXL + 1], used[QAP_MAXL + 1], pi[QAP_MAXL];
+  const int lane = threadIdx.x, n = l, nn = l * l;
+  const int col = blockIdx.x % s2;
+  const double sgn = (blockIdx.x < s2) ? 1.0 : -1.0;
+  const double INF = __longlong_as_double(0x7ff0000000000000LL);
+  const double NaN = __longlong_as_double(0x7ff8000000000000LL);
+  // cost = max(c) - c
+  double mx = -INF;
+  bool finite = true;
+  for (int e = lane; e < nn; e += 32) {
+    const double c = sgn * E[(size_t)col * lde + 1 + e];
+    finite = finite && isfinite(c);
+    a[e] = c;
+    mx = fmax(mx, c);
+  }
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  finite = __all_sync(0xffffffffu, finite);
+  if (!finite) {
+    if (lane == 0) vals[blockIdx.x] = NaN;
+    for (int r = lane; r < n; r += 32) perms[(size_t)blockIdx.x * l + r] = -1;
+    return;
+  }
+  for (int e = lane; e < nn; e += 32) a[e] = mx - a[e];
+  for (int j = lane; j <= n; j += 32) { u[j] = 0.0; v[j] = 0.0; p[j] = 0; way[j] = 0; }
+  __syncwarp();
+  bool good = true;
+  for (int i = 1; i <= n && good; ++i) {
+    if (lane == 0) p[0] = i;
+    for (int j = lane; j <= n; j += 32) { minv[j] = INF; used[j] = 0; }
+    __syncwarp();
+    int j0 = 0;
+    bool closed = false;
+    for (int it = 0; it <= n && !closed; ++it) {
+      if (lane == 0) used[j0] = 1;
+      __syncwarp();
+      const int i0 = p[j0];
+      const double ui0 = u[i0];
+      double best = INF;
+      int bj = 0x7fffffff;
+      for (int j = lane; j <= n; j += 32) {
+        if (j >= 1 && !used[j]) {
+          const double cur = a[(i0 - 1) * n + (j - 1)] - ui0 - v[j];
+          if (cur < minv[j]) { minv[j] = cur; way[j] = j0; }
+          if (minv[j] < best || (minv[j] == best && j < bj)) { best = minv[j]; bj = j; }
+        }
+      }
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oj = __shfl_xor_sync(0xffffffffu, bj, o);
+        if (ob < best || (ob == best && oj < bj)) { best = ob; bj = oj; }
+      }
+      __syncwarp();
+      if (bj == 0x7fffffff) { good = false; break; }
+      for (int j = lane; j <= n; j += 32) {
+        if (used[j]) { u[p[j]] += best; v[j] -= best; }
+        else minv[j] -= best;
+      }
+      __syncwarp();
+      j0 = bj;
+      closed = (p[j0] == 0);
+    }
+    if (!closed) good = false;
+    if (good && lane == 0) {
+      int jj = j0;
+      for (int g = 0; g <= n && jj != 0; ++g) {
+        const int j1 = way[jj];
+        p[jj] = p[j1];
+        jj = j1;
+      }
+    }
+    __syncwarp();
+  }
+  if (!good) {
+    if (lane == 0) vals[blockIdx.x] = NaN;
+    for (int r = lane; r < n; r += 32) perms[(size_t)blockIdx.x * l + r] = -1;
+    return;
+  }
+  for (int j = lane + 1; j <= n; j += 32) pi[p[j] - 1] = j - 1;   // facility -> location
+  __syncwarp();
+  double acc = 0.0;
+  for (int f = lane; f < n; f += 32) {
+    const int pf = pi[f];
+    for (int g = 0; g < n; ++g) acc += W[f * l + g] * D[pf * l + pi[g]];
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  if (lane == 0) vals[blockIdx.x] = acc;
+  for (int r = lane; r < n; r += 32) perms[(size_t)blockIdx.x * l + r] = pi[r];
+}
+
+// min over the positive candidates, min over the negative ones (NaN
+// propagating, as jnp.min), then the reference's select(min_pos < min_neg)
+__global__ void qap_final_kernel(int s2, const double* __restrict__ vals, double* __restrict__ out) {
+  if (threadIdx.x != 0) return;
+  double mp = vals[0], mn = vals[s2];
+  for (int i = 1; i < s2; ++i) {
+    mp = (isnan(mp) || isnan(vals[i])) ? __longlong_as_double(0x7ff8000000000000LL) : fmin(mp, vals[i]);
+    const double w = vals[s2 + i];
+    mn = (isnan(mn) || isnan(w)) ? __longlong_as_double(0x7ff8000000000000LL) : fmin(mn, w);
+  }
+  *out = (mp < mn) ? mp : mn;
+}
+
 static int rd_blocks(long long work, long long per_block, int cap) {
   long long b = (work + per_block - 1) / per_block;
   if (b > cap) b = cap;
@@ -422,6 +543,49 @@ int usbs_maxcut_round(int n, int s, const double* Omega, const double* P, int ld
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) {
     set_error("maxcut_round: launch failed: %s", cudaGetErrorString(e));
+    return -5;
+  }
+  return 0;
+}
+
+size_t usbs_qap_round_workspace_bytes(int l, int s) {
+  if (l < 1 || l > QAP_MAXL || s < 1 || s > RD_MAXS) return 0;
+  const int n = l * l + 1, s2 = s < l ? s : l;
+  return rd_bytes(n, s) + rd_align((size_t)n * s * sizeof(double)) +
+         rd_align((size_t)2 * s2 * sizeof(double)) + rd_align((size_t)2 * s2 * l * sizeof(int));
+}
+
+int usbs_qap_round(int l, int s, const double* Omega, const double* P, int ld, const double* W,
+                   const double* D, double approx_eps, double* value, double* candidate_values,
+                   int* candidate_perms, void* workspace, size_t workspace_bytes, void* stream) {
+  if (l < 1 || l > QAP_MAXL) {
+    set_error("qap_round: l=%d must be in [1, %d]", l, QAP_MAXL);
+    return -2;
+  }
+  const int n = l * l + 1;
+  int rc = rd_check(n, s, ld, Omega, P, workspace, workspace_bytes, "qap_round");
+  if (rc) return rc;
+  if (!W || !D || !value) { set_error("qap_round: null pointer"); return -2; }
+  const size_t need = usbs_qap_round_workspace_bytes(l, s);
+  if (workspace_bytes < need) {
+    set_error("qap_round: workspace of %zu bytes, %zu needed", workspace_bytes, need);
+    return -2;
+  }
+  const int s2 = s < l ? s : l;
+  RoundWs w = rd_carve(workspace, n, s);
+  char* q = (char*)workspace + rd_bytes(n, s);
+  double* E = (double*)q; q += rd_align((size_t)n * s * sizeof(double));
+  double* vals = candidate_values ? candidate_values : (double*)q;
+  q += rd_align((size_t)2 * s2 * sizeof(double));
+  int* perms = candidate_perms ? candidate_perms : (int*)q;
+  cudaStream_t st = (cudaStream_t)stream;
+  rc = rd_reconstruct(n, s, Omega, P, ld, approx_eps, w, E, n, st);
+  if (rc) return rc;
+  qap_lap_kernel<<<2 * s2, 32, 0, st>>>(l, s2, E, n, W, D, vals, perms);
+  qap_final_kernel<<<1, 32, 0, st>>>(s2, vals, value);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    set_error("qap_round: launch failed: %s", cudaGetErrorString(e));
     return -5;
   }
   return 0;

@@ -4,6 +4,9 @@
 * ``compute_max_cut(P, Omega, callback_static_args, callback_nonstatic_args)``:
   utils/maxcut_helpers.py:292-302, the reference's rounding callback, with its
   signature, so it plugs into ``usbs_gb300.solver.usbs(callback_fn=...)``.
+* ``qap_round(P, Omega, callback_static_args, callback_nonstatic_args)``:
+  utils/qap_helpers.py:624-653, the QAP rounding callback (static args: the
+  pickled ``{"l": l}``; non-static: ``{"D": D, "W": W}``).
 
 Both run through the C ABI (``usbs_reconstruct_from_sketch``,
 ``usbs_maxcut_round``): one pass over the sketch for its Gram matrices, the
@@ -130,4 +133,62 @@ def compute_max_cut(P, Omega, callback_static_args, callback_nonstatic_args):
     """utils/maxcut_helpers.py:292-302: the largest cut w^T C w among the sign
     patterns w = sign(E[:, j]) of the reconstructed sketch (as a float)."""
     value, _, _ = max_cut_values(P, Omega, callback_nonstatic_args)
+    return float(value.item())
+
+
+_DENSE_CACHE = []        # [(matrix object, device tensor)], most recent last
+
+
+def _device_dense(M, device):
+    torch = _torch()
+    if isinstance(M, torch.Tensor):
+        return M.to(device=device, dtype=torch.float64).contiguous()
+    for obj, t in _DENSE_CACHE:
+        if obj is M:
+            return t
+    t = torch.as_tensor(np.ascontiguousarray(np.asarray(M, dtype=np.float64)), device=device)
+    _DENSE_CACHE.append((M, t))
+    del _DENSE_CACHE[:-4]
+    return t
+
+
+def qap_round_values(P, Omega, l, D, W, approx_eps=1e-6, device=None):
+    """(value, candidate values, candidate permutations) of qap_round as CUDA
+    tensors: the candidates are the first min(l, s) columns of E, then their
+    negatives; a permutation gives each facility's location."""
+    torch = _torch()
+    dev = torch.device(device) if device is not None else (
+        P.device if isinstance(P, torch.Tensor) and P.is_cuda else torch.device("cuda"))
+    o, p, n, s, ld = _operands(Omega, P, dev)
+    l = int(l)
+    if n != l * l + 1:
+        raise ValueError(f"qap_round: the sketch has {n} rows, l^2 + 1 = {l * l + 1} expected")
+    Dt, Wt = _device_dense(D, dev), _device_dense(W, dev)
+    if tuple(Dt.shape) != (l, l) or tuple(Wt.shape) != (l, l):
+        raise ValueError("qap_round: D and W must be l x l")
+    lib = _lib.load()
+    wsb = int(lib.usbs_qap_round_workspace_bytes(l, s))
+    if wsb == 0:
+        raise ValueError(f"qap_round: unsupported sizes l={l} s={s} (l <= 64, s <= 32)")
+    s2 = min(l, s)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+    out = torch.empty(1 + 2 * s2, dtype=torch.float64, device=dev)
+    perms = torch.empty((2 * s2, l), dtype=torch.int32, device=dev)
+    st = torch.cuda.current_stream(dev).cuda_stream
+    rc = lib.usbs_qap_round(l, s, _ptr(o), _ptr(p), ld, _ptr(Wt), _ptr(Dt), float(approx_eps),
+                            _ptr(out), ctypes.c_void_p(out.data_ptr() + 8), _ptr(perms), _ptr(ws),
+                            wsb, ctypes.c_void_p(st))
+    _lib.check(rc, "usbs_qap_round")
+    return out[0], out[1:], perms
+
+
+def qap_round(P, Omega, callback_static_args, callback_nonstatic_args):
+    """utils/qap_helpers.py:624-653: the smallest QAP objective among the
+    assignments read off the reconstructed sketch's columns (as a float)."""
+    import pickle
+    st = callback_static_args
+    l = pickle.loads(st)["l"] if isinstance(st, (bytes, bytearray)) else (
+        st["l"] if isinstance(st, dict) else int(st))
+    value, _, _ = qap_round_values(P, Omega, l, callback_nonstatic_args["D"],
+                                   callback_nonstatic_args["W"])
     return float(value.item())
