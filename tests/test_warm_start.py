@@ -81,3 +81,83 @@ def test_explicit_warm_start_sketch_matches_oracle(cuda):
     old = _solved_state(Wo, 10)
     _same(pmaxcut.explicit_warm_start(old, Wn, 10),
           omaxcut.get_explicit_warm_start_state(old, Wn, 10), rtol=1e-8)
+
+
+# ---- QAP (utils/qap_helpers.py:384-621) ----
+
+def _same_qap(a, b, rtol):
+    """As _same, with the constraint triples compared as a set: the package's
+    builder lists the same (constraint, i, j, a) triples in another order."""
+    def sorted_triples(st):
+        idx = np.asarray(st.A_indices)
+        o = np.lexsort((idx[:, 2], idx[:, 1], idx[:, 0]))
+        return idx[o], np.asarray(st.A_data)[o]
+    ia, da = sorted_triples(a)
+    ib, db = sorted_triples(b)
+    np.testing.assert_array_equal(ia, ib)
+    np.testing.assert_allclose(da, db, rtol=rtol)
+    _same(a._replace(A_indices=None, A_data=None), b._replace(A_indices=None, A_data=None), rtol)
+
+def _qap_solved(l_old, l, sketch_dim, seed=3):
+    """A solved-looking QAP state on the first l_old facilities of an l-facility
+    instance, and that instance's (D, W)."""
+    from oracle import common as ocommon
+    from oracle import qap as oqap
+    D, W = wl.qap_instance(l, seed, grid=6)
+    st = oqap.initialize_state(D[:l_old, :l_old], W[:l_old, :l_old], sketch_dim)
+    us = ocommon.unscale_sdp_state(st)
+    n, m = us.C.shape[0], us.b.shape[0]
+    rng = np.random.default_rng(seed)
+    V = rng.standard_normal((n, 2 * l))
+    X = (V * np.linspace(2.0, 0.1, 2 * l)) @ V.T
+    us = us._replace(X=X if sketch_dim == -1 else None,
+                     P=None if sketch_dim == -1 else X @ us.Omega,
+                     y=rng.standard_normal(m), z=rng.standard_normal(m),
+                     tr_X=float(np.trace(X)), primal_obj=float((us.C @ X).trace()))
+    return ocommon.scale_sdp_state(us), D, W
+
+
+@pytest.mark.parametrize("sketch_dim", ["l", -1])
+def test_qap_implicit_and_dual_only_warm_starts_match_oracle(sketch_dim):
+    from oracle import qap as oqap
+    from usbs_gb300.problems import qap as pqap
+    l_old, l = 4, 6
+    sd = l if sketch_dim == "l" else -1
+    old, D, W = _qap_solved(l_old, l, sd)
+    _same_qap(pqap.implicit_warm_start(old, D, W, sd),
+              oqap.get_implicit_warm_start_state(old, D, W, sd), rtol=1e-9)
+    _same_qap(pqap.dual_only_warm_start(old, D, W, sd),
+              oqap.get_dual_only_warm_start_state(old, D, W, sd), rtol=1e-9)
+
+
+def test_qap_explicit_warm_start_dense_matches_oracle():
+    from oracle import qap as oqap
+    from usbs_gb300.problems import qap as pqap
+    old, D, W = _qap_solved(4, 6, -1)
+    _same_qap(pqap.explicit_warm_start(old, D, W, -1),
+              oqap.get_explicit_warm_start_state(old, D, W, -1), rtol=1e-9)
+
+
+def test_qap_warm_start_moves_the_lifted_indices():
+    """Facility f at location i of the old instance (index 1 + i + l_old f)
+    lands on 1 + i + l f; the new facility's rows stay empty."""
+    from usbs_gb300.problems import qap as pqap
+    l_old, l = 3, 4
+    old, D, W = _qap_solved(l_old, l, -1)
+    new = pqap.implicit_warm_start(old, D, W, -1)
+    Xo = np.asarray(old.X) / old.SCALE_X
+    Xn = np.asarray(new.X) / new.SCALE_X
+    for f in range(l_old):
+        for i in range(l_old):
+            a, b = 1 + i + l_old * f, 1 + i + l * f
+            assert Xn[b, 0] == pytest.approx(Xo[a, 0], rel=1e-12)
+    assert not Xn[1 + (l - 1) + l * np.arange(l), :].any()
+
+
+@pytest.mark.gpu
+def test_qap_explicit_warm_start_sketch_matches_oracle(cuda):
+    from oracle import qap as oqap
+    from usbs_gb300.problems import qap as pqap
+    old, D, W = _qap_solved(4, 6, 6)
+    _same_qap(pqap.explicit_warm_start(old, D, W, 6),
+              oqap.get_explicit_warm_start_state(old, D, W, 6), rtol=1e-8)

@@ -1,4 +1,5 @@
-"""QAP SDP relaxation instances (reference: utils/qap_helpers.py:157-381).
+"""QAP SDP relaxation instances (reference: utils/qap_helpers.py:157-381) and
+their warm starts (implicit, explicit, dual-only: utils/qap_helpers.py:384-621).
 
 The lifted variable Y is (l^2 + 1) x (l^2 + 1): row/column 0 is the homogenising
 coordinate and index 1 + i + l j stands for "facility j at location i".  The
@@ -100,8 +101,9 @@ def constraints(C_rows, C_cols, N):
             np.concatenate([f[3] for f in fams]))
 
 
-def initialize_state(D, W, sketch_dim, Omega=None):
-    """Scaled cold-start state of the QAP relaxation (utils/qap_helpers.py:321-381)."""
+def _problem(D, W):
+    """(C, A_data, A_indices, b, mask, SCALE_C, SCALE_X, SCALE_A) of the
+    relaxation, unscaled (utils/qap_helpers.py:321-370)."""
     D = np.asarray(D, float)
     W = np.asarray(W, float)
     r, c, v, N = objective_pattern(D, W)
@@ -117,7 +119,13 @@ def initialize_state(D, W, sketch_dim, Omega=None):
                           shape=(m, N * N))
     lam = eigsh(A_mat @ A_mat.T, k=1, which="LM", return_eigenvectors=False,
                 maxiter=np.iinfo(np.int32).max)[0]
-    sa = sa / np.sqrt(lam)
+    return C, A_data, A_idx, b, mask, scale_c, scale_x, sa / np.sqrt(lam)
+
+
+def initialize_state(D, W, sketch_dim, Omega=None):
+    """Scaled cold-start state of the QAP relaxation (utils/qap_helpers.py:321-381)."""
+    C, A_data, A_idx, b, mask, scale_c, scale_x, sa = _problem(D, W)
+    N, m = C.shape[0], b.shape[0]
     if sketch_dim == -1:
         X, P, Om = np.zeros((N, N)), None, None
     elif sketch_dim > 0:
@@ -129,3 +137,136 @@ def initialize_state(D, W, sketch_dim, Omega=None):
                   Omega=Om, y=np.zeros(m), z=np.zeros(m), tr_X=0.0, primal_obj=0.0,
                   SCALE_C=scale_c, SCALE_X=scale_x, SCALE_A=sa)
     return scale_sdp_state(st)
+
+
+# ---------------------------------------------------------------- warm starts
+# A solved instance with old_l facilities warm-starts one with l = old_l +
+# num_drop (utils/qap_helpers.py:395-621): lifted index a = 1 + loc + old_l fac
+# moves to a + num_drop * fac, and each old constraint to the new constraint
+# whose triples its own match, found by walking both triple lists in order
+# (utils/qap_helpers.py:384-392), here in (constraint, i, j) order.  The walk
+# stops at the last old triple, and old constraints it never matches keep no
+# dual (the reference leaves those map entries uninitialised).
+
+def _host(x):
+    return x.detach().cpu().numpy() if hasattr(x, "detach") else np.asarray(x, float)
+
+
+def _index_map(a, l, num_drop):
+    a = np.asarray(a, np.int64)
+    return a + num_drop * np.clip((a - 1) // (l - num_drop), 0, None)
+
+
+def _constraint_map(old_idx, new_idx, old_m):
+    # both lists in (constraint, i, j) order: on the reference's listing this
+    # gives its map, and it does not depend on how a state lists its triples
+    old_idx = old_idx[np.lexsort((old_idx[:, 2], old_idx[:, 1], old_idx[:, 0]))]
+    new_idx = np.asarray(new_idx)
+    new_idx = new_idx[np.lexsort((new_idx[:, 2], new_idx[:, 1], new_idx[:, 0]))]
+    cmap = np.full(old_m, -1, np.int64)
+    o = 0
+    for cur in range(new_idx.shape[0]):
+        if o >= old_idx.shape[0]:
+            break
+        if new_idx[cur, 1] == old_idx[o, 1] and new_idx[cur, 2] == old_idx[o, 2]:
+            cmap[old_idx[o, 0]] = new_idx[cur, 0]
+            o += 1
+    return cmap
+
+
+def _carry(old, D, W, sketch_dim):
+    old = old._replace(y=_host(old.y), z=_host(old.z))
+    from ..state import unscale_sdp_state
+    old = unscale_sdp_state(old)
+    C, A_data, A_idx, b, mask, scale_c, scale_x, sa = _problem(D, W)
+    n, m = C.shape[0], b.shape[0]
+    old_l = int(round(np.sqrt(old.C.shape[0] - 1)))
+    l = int(round(np.sqrt(n - 1)))
+    if sketch_dim not in (-1, l):
+        raise ValueError(f"sketch_dim must be -1 or l = {l}")
+    num_drop = l - old_l
+    oidx = np.asarray(old.A_indices, np.int64).copy()
+    oidx[:, 1:] = _index_map(oidx[:, 1:], l, num_drop)
+    cmap = _constraint_map(oidx, A_idx, np.asarray(old.b).shape[0])
+    keep = cmap >= 0
+
+    def dual(v):
+        out = np.zeros(m)
+        out[cmap[keep]] = np.asarray(v, float)[keep]
+        return out
+    return old, (C, A_data, A_idx, b, mask, scale_c, scale_x, sa), l, num_drop, dual
+
+
+def _state(prob, X, P, Om, y, z, tr_X, primal):
+    C, A_data, A_idx, b, mask, scale_c, scale_x, sa = prob
+    return scale_sdp_state(SDPState(C=C, A_indices=A_idx, A_data=A_data, b=b, b_ineq_mask=mask,
+                                    X=X, P=P, Omega=Om, y=y, z=z, tr_X=tr_X, primal_obj=primal,
+                                    SCALE_C=scale_c, SCALE_X=scale_x, SCALE_A=sa))
+
+
+def implicit_warm_start(old, D, W, sketch_dim):
+    """utils/qap_helpers.py:395-467: X, P and Omega's rows moved to the new
+    lifted indices (new rows of Omega drawn fresh, key n), y and z carried by
+    the constraint map, tr_X and primal_obj kept."""
+    old, prob, l, num_drop, dual = _carry(old, D, W, sketch_dim)
+    n = prob[0].shape[0]
+    X, P, Om = None, None, None
+    if old.X is not None:
+        Xo = np.asarray(old.X, float)
+        r, c = np.nonzero(Xo)
+        X = np.zeros((n, n))
+        X[_index_map(r, l, num_drop), _index_map(c, l, num_drop)] = Xo[r, c]
+    if old.P is not None:
+        rows = _index_map(np.arange(np.asarray(old.P).shape[0]), l, num_drop)
+        Om = hash_normal_matrix(n, n, sketch_dim)
+        Om[rows] = _host(old.Omega)
+        P = np.zeros_like(Om)
+        P[rows] = np.asarray(old.P, float)
+    return _state(prob, X, P, Om, dual(old.y), dual(old.z), old.tr_X, old.primal_obj)
+
+
+def explicit_warm_start(old, D, W, sketch_dim, device="cuda"):
+    """utils/qap_helpers.py:469-553: the old iterate made explicit (dense X
+    moved to the new indices, or the sketch's Nystrom factors reconstructed on
+    the device, trace-corrected, moved and re-sketched by a fresh Omega, key
+    n); z, tr_X and primal_obj recomputed; y carried by the constraint map."""
+    old, prob, l, num_drop, dual = _carry(old, D, W, sketch_dim)
+    C, A_data, A_idx = prob[0], prob[1], prob[2]
+    n, m = C.shape[0], prob[3].shape[0]
+    X, P, Om = None, None, None
+    if old.X is not None:
+        Xo = np.asarray(old.X, float)
+        r, c = np.nonzero(Xo)
+        X = np.zeros((n, n))
+        X[_index_map(r, l, num_drop), _index_map(c, l, num_drop)] = Xo[r, c]
+        z = np.bincount(A_idx[:, 0], weights=A_data * X[A_idx[:, 1], A_idx[:, 2]], minlength=m)
+        tr_X = float(np.trace(X))
+        primal = float((C @ X).trace())
+    if old.P is not None:
+        from ..rounding import reconstruct_from_sketch
+        Om = hash_normal_matrix(n, n, sketch_dim)
+        E, lam = reconstruct_from_sketch(_host(old.Omega), np.asarray(old.P, float), device=device)
+        E, lam = E.cpu().numpy(), lam.cpu().numpy()
+        lam_c = lam + (old.tr_X - lam.sum()) / lam.shape[0]
+        S = np.zeros((n, E.shape[1]))
+        with np.errstate(invalid="ignore"):
+            S[_index_map(np.arange(E.shape[0]), l, num_drop)] = E * np.sqrt(lam_c)[None, :]
+        P = S @ (S.T @ Om)
+        prod = np.einsum("tj,tj->t", S[A_idx[:, 1]], S[A_idx[:, 2]])
+        z = np.bincount(A_idx[:, 0], weights=A_data * prod, minlength=m)
+        tr_X = float(lam_c.sum())
+        primal = float(np.einsum("ij,ij->", S, C @ S))
+    return _state(prob, X, P, Om, dual(old.y), z, tr_X, primal)
+
+
+def dual_only_warm_start(old, D, W, sketch_dim):
+    """utils/qap_helpers.py:556-621: only y, carried by the constraint map; a
+    cold iterate (Omega as the cold start draws it)."""
+    old, prob, l, num_drop, dual = _carry(old, D, W, sketch_dim)
+    n, m = prob[0].shape[0], prob[3].shape[0]
+    if sketch_dim == -1:
+        X, P, Om = np.zeros((n, n)), None, None
+    else:
+        Om = hash_normal_matrix(1, n, sketch_dim)
+        X, P = None, np.zeros_like(Om)
+    return _state(prob, X, P, Om, dual(old.y), np.zeros(m), 0.0, 0.0)
