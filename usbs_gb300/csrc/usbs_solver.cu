@@ -914,15 +914,12 @@ static int body(Solver& X, int t) {
   cudaStream_t st = X.st;
   double* V = S->V;
   // ---- projections onto the bundle basis (solver/usbs.py:54-61) ----
-  // V^T C V on the second stream (C V then the Gram) while this stream forms
-  // Pm[c, :] = svec(V^T A_c V) (create_Q_base's rows) and, from the same Pm,
-  // the three A* projections: svec(V^T A*(w) V) = Pm^T w for w = y, z_bar and
-  // b - upsilon, one Gram against the packed weight columns.
-  if (cudaEventRecord(X.ev_fork, st) != cudaSuccess ||
-      cudaStreamWaitEvent(X.st2, X.ev_fork, 0) != cudaSuccess)
-    return kerr("fork");
-  CK(X.proj(1.0, nullptr, V, L.o_GC, 1));             // V^T C V
-  if (cudaEventRecord(X.ev_join, X.st2) != cudaSuccess) return kerr("join record");
+  // V^T C V (C V, then the Gram); Pm[c, :] = svec(V^T A_c V) (create_Q_base's
+  // rows) and, from the same Pm, the three A* projections: svec(V^T A*(w) V) =
+  // Pm^T w for w = y, z_bar and b - upsilon, one Gram against the packed
+  // weight columns.  All on this stream: a fork here costs concurrent solves
+  // (several per GPU) more in queue waits than the overlap gains one solve.
+  CK(X.proj(1.0, nullptr, V, L.o_GC));                // V^T C V
   {
     MvecArgs ma = X.margs();
     ++X.launches;
@@ -938,7 +935,6 @@ static int body(Solver& X, int t) {
     CK(kerr("svec_project"));
     CK(X.gram(L.Pm, L.m, L.s, L.Pm, L.m, L.s, L.m, L.smalls + L.o_QB));   // create_Q_base
   }
-  if (cudaStreamWaitEvent(st, X.ev_join, 0) != cudaSuccess) return kerr("join");
   CK(X.a_proj3());
   if (L.ssk > 0) CK(X.gram(V, L.ld, L.k, S->Omega, L.ld, L.ssk, L.n, L.smalls + L.o_VtO));
   // alternating-minimisation initial point: S_init = trace_ub * 0.99 I / (k+1)
