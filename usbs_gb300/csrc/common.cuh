@@ -164,15 +164,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, uint64
     if ((it & 63u) == 0 && globaltimer_ns() - t0 > limit_ns) return false;
   }
 }
-// global -> shared bulk copy of `bytes` (multiple of 16, both addresses 16-byte
-// aligned), completion counted on `bar`
-__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, unsigned bytes,
-                                         uint64_t* bar) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-      ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
-      : "memory");
-}
 // L2 eviction-priority policies (createpolicy) and their use: streamed data is
 // marked evict_first so that it does not displace a small, re-read working set
 // (marked evict_last) from L2
@@ -186,6 +177,8 @@ __device__ __forceinline__ uint64_t l2_evict_last_policy() {
   asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
   return pol;
 }
+// global -> shared bulk copy of `bytes` (a multiple of 16, both addresses
+// 16-byte aligned) with an L2 policy, completion counted on `bar`
 __device__ __forceinline__ void bulk_g2s_hint(void* dst, const void* src, unsigned bytes,
                                               uint64_t* bar, uint64_t pol) {
   asm volatile(

@@ -357,110 +357,4 @@ __device__ inline void cta_refine_eig(const double* A, double* X, double* R, dou
   __syncthreads();
 }
 
-// Solve A x = b (n x n, row-major lda, in shared memory) by LU with partial
-// pivoting, executed by the whole CTA.  A and b are destroyed; x overwrites b.
-// `red` needs >= 2*blockDim/32 doubles and ints for the pivot search.
-// Returns false (uniformly) if a pivot is exactly zero.
-__device__ inline bool block_lu_solve(double* A, int lda, double* b, int n, double* redv, int* redi) {
-  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5;
-  const int nw = nt >> 5;
-  __shared__ int s_piv;
-  __shared__ int s_ok;
-  if (tid == 0) s_ok = 1;
-  for (int j = 0; j < n; ++j) {
-    // pivot search over rows j..n-1 of column j
-    double best = -1.0;
-    int bi = j;
-    for (int i = j + tid; i < n; i += nt) {
-      double a = fabs(A[i * lda + j]);
-      if (a > best) { best = a; bi = i; }
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-      double ob = __shfl_xor_sync(0xffffffffu, best, o);
-      int oi = __shfl_xor_sync(0xffffffffu, bi, o);
-      if (ob > best || (ob == best && oi < bi)) { best = ob; bi = oi; }
-    }
-    if (lane == 0) { redv[wid] = best; redi[wid] = bi; }
-    __syncthreads();
-    if (tid == 0) {
-      double bb = redv[0];
-      int ii = redi[0];
-      for (int w2 = 1; w2 < nw; ++w2)
-        if (redv[w2] > bb || (redv[w2] == bb && redi[w2] < ii)) { bb = redv[w2]; ii = redi[w2]; }
-      s_piv = ii;
-      if (bb == 0.0) s_ok = 0;
-    }
-    __syncthreads();
-    const int piv = s_piv;
-    if (piv != j) {
-      for (int c = tid; c < n; c += nt) {
-        double t = A[j * lda + c];
-        A[j * lda + c] = A[piv * lda + c];
-        A[piv * lda + c] = t;
-      }
-      if (tid == 0) { double t = b[j]; b[j] = b[piv]; b[piv] = t; }
-      __syncthreads();
-    }
-    const double inv = 1.0 / A[j * lda + j];
-    // multipliers (column j below the diagonal)
-    for (int i = j + 1 + tid; i < n; i += nt) A[i * lda + j] *= inv;
-    __syncthreads();
-    const int rows = n - j - 1, cols = n - j - 1;
-    for (int e = tid; e < rows * cols; e += nt) {
-      int i = j + 1 + e / cols, c = j + 1 + e % cols;
-      A[i * lda + c] -= A[i * lda + j] * A[j * lda + c];
-    }
-    for (int i = j + 1 + tid; i < n; i += nt) b[i] -= A[i * lda + j] * b[j];
-    __syncthreads();
-  }
-  // back substitution (column oriented)
-  for (int j = n - 1; j >= 0; --j) {
-    if (tid == 0) b[j] = b[j] / A[j * lda + j];
-    __syncthreads();
-    for (int i = tid; i < j; i += nt) b[i] -= A[i * lda + j] * b[j];
-    __syncthreads();
-  }
-  return s_ok != 0;
-}
-
-// Inverse of the n x n matrix A (row-major lda) by one warp: Gauss-Jordan with
-// partial pivoting.  Ainv (row-major ldi) receives the result; A is destroyed.
-__device__ inline bool warp_inverse(double* A, int lda, int n, double* Ainv, int ldi) {
-  const int lane = threadIdx.x & 31;
-  for (int i = 0; i < n; ++i)
-    if (lane < n) Ainv[i * ldi + lane] = (i == lane) ? 1.0 : 0.0;
-  __syncwarp();
-  bool ok = true;
-  for (int j = 0; j < n; ++j) {
-    double best = -1.0;
-    int bi = j;
-    for (int i = j; i < n; ++i) {
-      double a = fabs(A[i * lda + j]);
-      if (a > best) { best = a; bi = i; }
-    }
-    if (best == 0.0) ok = false;
-    if (bi != j && lane < n) {
-      double t = A[j * lda + lane]; A[j * lda + lane] = A[bi * lda + lane]; A[bi * lda + lane] = t;
-      t = Ainv[j * ldi + lane]; Ainv[j * ldi + lane] = Ainv[bi * ldi + lane];
-      Ainv[bi * ldi + lane] = t;
-    }
-    __syncwarp();
-    double inv = 1.0 / A[j * lda + j];
-    __syncwarp();
-    if (lane < n) { A[j * lda + lane] *= inv; Ainv[j * ldi + lane] *= inv; }
-    __syncwarp();
-    for (int i = 0; i < n; ++i) {
-      if (i == j) continue;
-      double f = A[i * lda + j];
-      __syncwarp();
-      if (lane < n) {
-        A[i * lda + lane] -= f * A[j * lda + lane];
-        Ainv[i * ldi + lane] -= f * Ainv[j * ldi + lane];
-      }
-      __syncwarp();
-    }
-  }
-  return ok;
-}
-
 }  // namespace usbs
