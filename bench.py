@@ -218,7 +218,58 @@ def spmv_gbs(device, reps=20):
             "kernel": "sell_spmv_kernel<float>", "ms": ms_sell, "gbs": gbs(ms_sell),
             "stored_over_nnz": stored / nnz,
             "csr_kernel": {"ms": ms_csr, "gbs": gbs(ms_csr)},
-            "sell_after_rcm_renumbering": {"ms": ms_rcm, "gbs": gbs(ms_rcm)}}
+            "sell_after_rcm_renumbering": {"ms": ms_rcm, "gbs": gbs(ms_rcm)},
+            "eigsh": eigsh_leg(device, prob, n, flush, flush_rd),
+            "eigsh_after_rcm_renumbering": eigsh_renumbered(device, st, n, flush, flush_rd)}
+
+
+def eigsh_renumbered(device, st, n, flush, flush_rd):
+    """eigsh_leg on the RCM-renumbered problem (usbs_gb300.renumber), the start
+    vector permuted with it."""
+    from usbs_gb300 import renumber
+    from usbs_gb300.problem import DeviceProblem, layout
+    from usbs_gb300.rng import default_q0
+    perm = renumber.rcm_permutation(st.C, st.A_indices, n)
+    Cp, idx = renumber.permute_problem(st.C, st.A_indices, perm)
+    prob = DeviceProblem(layout(Cp, st.A_data, idx, m=n), device)
+    return eigsh_leg(device, prob, n, flush, flush_rd, q0=default_q0(n)[perm])
+
+
+def eigsh_leg(device, prob, n, flush, flush_rd, q0=None):
+    """One eigsh_smallest call on the same 10^6-node operator (the team Lanczos
+    kernel, FP32, 10 eigenpairs, 32 inner vectors, 10 restarts, tolerance 1e-7),
+    L2 flushed first, timed with CUDA events on the launching stream, with its
+    algorithmic bytes from the kernel's own counters."""
+    import torch
+    from usbs_gb300 import api
+    from usbs_gb300.rng import default_q0
+    y = torch.zeros(n, dtype=torch.float64, device=device)
+    q0 = torch.as_tensor(default_q0(n) if q0 is None else q0, dtype=torch.float64,
+                         device=device)
+    call = lambda: api.eigsh_smallest(n, prob, None, None, y, q0, 10, 32, 10, 1e-7,
+                                      c_scale=-1.0, precision=32, return_info=True)
+    call()                                          # warm-up
+    flush.zero_()
+    flush_rd.sum()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    _, _, inf = call()
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    b, m = 4.0, 32
+    steps, restarts = inf.matvecs, inf.restarts
+    spmv = (4.0 + b) * prob.nnz + 4.0 * (n + 1) + 2.0 * b * n
+    cgs = 3.0 * b * n * inf.sum_active_columns + 6.0 * b * n * steps
+    rot = restarts * b * n * m + b * n * (inf.sum_saved + 2.0 * restarts)
+    alg = steps * spmv + cgs + rot
+    peak, kind = peaks()
+    vals, _, _ = call()
+    return {"kernel": "lanczos_team_kernel<float>", "ms": ms, "matvecs": steps,
+            "restarts": restarts, "eigenvalues_first3": [float(v) for v in vals[:3]],
+            "alg_bytes": alg, "gbs": alg / (ms * 1e-3) / 1e9,
+            "frac_of_" + kind: alg / (ms * 1e-3) / 1e9 / peak,
+            "phase_kcycles_bar_red_A_B_C": inf.phase_kcycles}
 
 
 def serving_stream(count, seed, n_lo=200, n_hi=2000):

@@ -237,3 +237,25 @@ def test_usbs_zero_iterations_returns_the_start(cuda):
     np.testing.assert_array_equal(out.y.cpu().numpy(), st.y)
     np.testing.assert_array_equal(out.P.cpu().numpy(), st.P)
     assert out.tr_X == 3.0 and out.primal_obj == 1.5
+
+
+def test_usbs_renumbered_matches_plain(cuda):
+    """usbs(renumber=True) solves the RCM-renumbered problem and returns the
+    result in the original numbering: the same iterates up to the order of
+    floating-point sums (resolved configuration, FP64)."""
+    from usbs_gb300 import solver
+    W = wl.er_graph(300, 4000, 7)
+    st = omaxcut.initialize_state(W, 10)
+    n = st.C.shape[0]
+    q0 = orng.default_q0(n)
+    kw = dict(q0=q0, precision=64, return_trace=True)
+    args = (st, n, n, 2.0 * n, 2.0, S["rho"], S["beta"], 4, 1, 2, np.inf, -1.0, -1.0, -1.0, 32,
+            200, 1e-9, S["subprob_max_iters"])
+    a, atr, _ = solver.usbs(*args, **kw)
+    b, btr, binfo = solver.usbs(*args, renumber=True, **kw)
+    assert binfo["status"] == 0
+    for key in ("primal_obj", "obj_ub", "lb_spec_est", "pen_dual_obj", "tr_X"):
+        assert _rel(atr[0][key], btr[0][key]) < 1e-9, (key, atr[0][key], btr[0][key])
+    np.testing.assert_allclose(b.P.cpu().numpy(), a.P.cpu().numpy(), rtol=1e-6,
+                               atol=1e-6 * np.abs(a.P.cpu().numpy()).max())
+    np.testing.assert_allclose(b.y.cpu().numpy(), a.y.cpu().numpy(), rtol=1e-6, atol=1e-8)

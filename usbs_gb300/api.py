@@ -136,6 +136,7 @@ class EigshInfo:
             self.status = (int(v) for v in raw[:6])
         self.restart_kcycles, self.total_kcycles = int(raw[6]), int(raw[7])
         self.phase_kcycles = [int(v) for v in raw[8:13]]
+        self.sum_active_columns, self.sum_saved = int(raw[13]), int(raw[14])
         self.eig_kcycles = int(raw[15])
 
     def __repr__(self):

@@ -190,20 +190,63 @@ def _dev_cols(x, rows, ld, cols, device, dtype):
     return out
 
 
+class _Renumbering:
+    """The permutation a renumbered solve runs under (none by default): the
+    callback's views of P and Omega and the returned state go back to the
+    original numbering."""
+
+    def __init__(self, orig=None, perm=None, dev=None):
+        self.orig, self.perm, self.inv_t = orig, perm, None
+        if perm is not None:
+            import torch
+            from .renumber import inverse
+            self.inv_t = torch.as_tensor(inverse(perm), device=dev)
+
+    def rows(self, *mats):
+        if self.inv_t is None:
+            return mats
+        return tuple(M.index_select(0, self.inv_t) for M in mats)
+
+    def restore(self, out, info):
+        if self.perm is None:
+            return out, info
+        from .renumber import unpermute_rows, unpermute_state
+        out = unpermute_state(out, self.orig, self.perm)
+        if "V" in info:
+            info["V"] = unpermute_rows(info["V"], self.perm)
+        return out, info
+
+
+def _renumbered(sdp_state, n, q0, flag, instance, dev):
+    """(state to solve, its start vector, _Renumbering) for renumber=flag."""
+    if not flag:
+        return sdp_state, q0, _Renumbering()
+    if instance is not None:
+        raise ValueError("renumber=True builds its own device instance")
+    from .renumber import permute_state, rcm_permutation
+    perm = rcm_permutation(sdp_state.C, sdp_state.A_indices, n)
+    q = default_q0(n) if q0 is None else _host(q0)
+    return permute_state(sdp_state, perm), np.asarray(q)[perm], _Renumbering(sdp_state, perm, dev)
+
+
 def usbs(sdp_state, n, m, trace_ub, trace_factor, rho, beta, k_curr, k_past, max_iters, max_time,
          obj_gap_eps, infeas_gap_eps, max_infeas_eps, lanczos_inner_iterations,
          lanczos_max_restarts, subprob_eps, subprob_max_iters, cond_exp_base=1.0,
          callback_fn=None, callback_static_args=None, callback_nonstatic_args=None, *, q0=None,
          precision=64, device="cuda", return_trace=False, return_info=False, instance=None,
-         stream=None, debug=None, log=None):
+         stream=None, debug=None, log=None, renumber=False):
     """``log``: True prints, a callable receives, the reference's per-check
-    line (solver/usbs.py:514-530) at every condition check, t = 0 included."""
+    line (solver/usbs.py:514-530) at every condition check, t = 0 included.
+    ``renumber``: solve the RCM-renumbered problem (locality for the device's
+    sparse gathers) and return the result in the original numbering; the
+    callback still sees P and Omega in the original numbering."""
     import torch
     if not torch.cuda.is_available():
         raise RuntimeError("usbs_gb300.usbs needs a CUDA device (GB300); none is visible")
     lib = _lib.load()
     _sigs(lib)
     dev = torch.device(device)
+    sdp_state, q0, ren = _renumbered(sdp_state, n, q0, renumber, instance, dev)
     inst = instance if instance is not None else DeviceInstance(sdp_state, dev)
     k = k_curr + k_past
     ld = (n + 31) // 32 * 32
@@ -257,8 +300,8 @@ def usbs(sdp_state, n, m, trace_ub, trace_factor, rho, beta, k_curr, k_past, max
 
     def _cb(_user, t):
         if callback_fn is not None and Om is not None:
-            cb_val[t] = callback_fn(Pm[:, :n].t(), Om[:, :n].t(), callback_static_args,
-                                    callback_nonstatic_args)
+            cb_val[t] = callback_fn(*ren.rows(Pm[:, :n].t(), Om[:, :n].t()),
+                                    callback_static_args, callback_nonstatic_args)
         if log_fn is not None:
             rec = {f: float(pst.cond[i]) for i, f in enumerate(TRACE_FIELDS)}
             log_fn(log_line(rec, float(sdp_state.SCALE_C), float(sdp_state.SCALE_X),
@@ -283,6 +326,7 @@ def usbs(sdp_state, n, m, trace_ub, trace_factor, rho, beta, k_curr, k_past, max
                 V=V[:, :n].t(), lanczos_launches=pst.lanczos_launches,
                 lanczos_ms=pst.lanczos_ms, lanczos_bytes=pst.lanczos_bytes,
                 kernel_launches=pst.kernel_launches)
+    out, info = ren.restore(out, info)
     if return_trace:
         tr = trace[:pst.iterations].cpu().numpy()
         recs = [{f: float(r[i]) for i, f in enumerate(TRACE_FIELDS)} for r in tr]
@@ -300,7 +344,8 @@ def cgal(sdp_state, n, m, trace_ub, beta0, max_iters, max_time, obj_gap_eps, inf
          max_infeas_eps, lanczos_inner_iterations, lanczos_max_restarts, subprob_eps,
          cond_exp_base=1.0, callback_fn=None, callback_static_args=None,
          callback_nonstatic_args=None, *, q0=None, precision=64, device="cuda",
-         return_trace=False, return_info=False, instance=None, stream=None, log=None):
+         return_trace=False, return_info=False, instance=None, stream=None, log=None,
+         renumber=False):
     """cgal() of solver/cgal.py:21-243 (same positional arguments), run by the
     device driver ``usbs_cgal_solve``.  Returns the updated SDPState; with
     ``return_trace`` also a list of per-iteration records, with
@@ -312,6 +357,7 @@ def cgal(sdp_state, n, m, trace_ub, beta0, max_iters, max_time, obj_gap_eps, inf
     lib = _lib.load()
     _sigs(lib)
     dev = torch.device(device)
+    sdp_state, q0, ren = _renumbered(sdp_state, n, q0, renumber, instance, dev)
     inst = instance if instance is not None else DeviceInstance(sdp_state, dev)
     ld = (n + 31) // 32 * 32
     f64 = torch.float64
@@ -358,8 +404,8 @@ def cgal(sdp_state, n, m, trace_ub, beta0, max_iters, max_time, obj_gap_eps, inf
 
     def _cb(_user, t):
         if callback_fn is not None and Om is not None:
-            cb_val[t] = callback_fn(Pm[:, :n].t(), Om[:, :n].t(), callback_static_args,
-                                    callback_nonstatic_args)
+            cb_val[t] = callback_fn(*ren.rows(Pm[:, :n].t(), Om[:, :n].t()),
+                                    callback_static_args, callback_nonstatic_args)
         if log_fn is not None:
             rec = {f: float(pst.cond[i]) for i, f in enumerate(CGAL_TRACE_FIELDS)}
             log_fn(cgal_log_line(rec, float(sdp_state.SCALE_C), float(sdp_state.SCALE_X),
@@ -380,6 +426,7 @@ def cgal(sdp_state, n, m, trace_ub, beta0, max_iters, max_time, obj_gap_eps, inf
     info = dict(iterations=pst.iterations, obj_gap=pst.obj_gap, infeas_gap=pst.infeas_gap,
                 max_infeas=pst.max_infeas, elapsed=pst.elapsed, status=pst.status,
                 callback_vals=cb_val, kernel_launches=pst.kernel_launches)
+    out, info = ren.restore(out, info)
     if return_trace:
         tr = trace[:pst.iterations].cpu().numpy()
         recs = [{f: float(r[i]) for i, f in enumerate(CGAL_TRACE_FIELDS)} for r in tr]
