@@ -291,6 +291,38 @@ def serving_stream(count, seed, n_lo=200, n_hi=2000):
     return out
 
 
+def qap_leg(device, iters=10):
+    """The QAP relaxation with l = 30 facilities (lifted order 901, about 3.4e5
+    constraints; synthetic flow U{0..10}, Manhattan distances on a 10 x 10
+    grid) at the reference's QAP settings: outer iterations per second of the
+    device solver in each precision, after one warm-up call."""
+    import torch
+    from usbs_gb300 import solver, workloads as wl
+    from usbs_gb300.problems import qap
+    D, W = wl.qap_instance(30, 0)
+    st = qap.initialize_state(D, W, 30)
+    n, m = st.C.shape[0], st.b.shape[0]
+    trace_ub = 2.0 * float(30 + 1) * st.SCALE_X
+    out = {"workload": "qap l=30 (n=901)", "m": int(m), "nnz_C": int(st.C.nnz),
+           "settings": {"k_curr": 2, "k_past": 0, "rho": 0.005, "trace_factor": 2.0,
+                        "sketch_dim": 30, "subprob_eps": 1e-7, "lanczos_max_restarts": 10}}
+    inst = solver.DeviceInstance(st, device)
+    for prec in (32, 64):
+        def run(k):
+            return solver.usbs(st, n, m, trace_ub, 2.0, 0.005, 0.25, 2, 0, k, np.inf, -1.0, -1.0,
+                               -1.0, 32, 10, 1e-7, 100, precision=prec, instance=inst,
+                               return_trace=True)
+        run(2)
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        _, recs, info = run(iters)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t
+        out[f"fp{prec}"] = {"outer_iterations_per_s": iters / dt, "status": info["status"],
+                            "obj_gap": recs[-1]["obj_gap"], "infeas_gap": recs[-1]["infeas_gap"]}
+    return out
+
+
 def blas_threads():
     """Threads the oracle's NumPy/SciPy linear algebra runs on (its dense
     kernels are multithreaded BLAS; the rest of the port is one thread)."""
@@ -413,7 +445,8 @@ def main():
     ap.add_argument("--iters-per-step", type=int, default=10)
     ap.add_argument("--cpu-iters", type=int, default=24)
     ap.add_argument("--no-spmv", action="store_true")
-    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--no-serving", action="store_true",
+                    help="skip the serving and QAP legs (the main line is unchanged)")
     ap.add_argument("--profile-case", choices=["usbs", "spmv", "eigsh-rgg"], default=None,
                     help="run one piece of the workload once, untimed (for ncu captures): "
                          "'usbs' = --iters-per-step outer iterations on the torus instance, "
@@ -569,6 +602,13 @@ def main():
         except Exception as exc:  # the main line is still reported
             spmv = {"error": str(exc)[:200]}
 
+    qapl = None
+    if rank == 0 and not args.no_serving:
+        try:
+            qapl = qap_leg(device)
+        except Exception as exc:  # the main line is still reported
+            qapl = {"error": str(exc)[:200]}
+
     serving = None
     if rank == 0 and not args.no_serving:
         try:
@@ -605,6 +645,7 @@ def main():
                                  "reach DRAM; it is bound by the latency of its step chain"
                          if lz_kernel.startswith("lanczos_cluster") else None},
             "lanczos_spmv_rgg1m": spmv,
+            "qap_l30": qapl,
             "serving": serving,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
