@@ -161,6 +161,42 @@ int usbs_eigsh_smallest_noalloc(int n, long long nnz, const int* rowptr, const i
                                 int precision, void* Q, int ldq, double* eigenvalues, int* info,
                                 void* stream);
 
+/* One problem of usbs_eigsh_smallest_batched: the arguments of
+ * usbs_eigsh_smallest that differ between problems (device pointers; the
+ * workspace is usbs_eigsh_workspace_bytes(n, nnz, inner_iterations,
+ * precision) bytes, one per problem). */
+typedef struct usbs_eigsh_problem {
+  int n;
+  long long nnz;
+  const int* rowptr;
+  const int* col;
+  const double* c_val;
+  double c_scale;
+  const int* slot_ptr;
+  const int* slot_tid;
+  const int* t_con;
+  const double* t_a;
+  const double* adjoint_left_vec;
+  const void* q0;
+  int num_desired;
+  void* Q;
+  int ldq;
+  double* eigenvalues;
+  int* info;
+  void* workspace;
+  size_t workspace_bytes;
+} usbs_eigsh_problem;
+
+/* eigsh_smallest for `count` independent problems with shared settings, in
+ * as few launches as the kernels allow: up to 48 problems per launch, one
+ * thread-block cluster each when every problem fits one (cluster size of
+ * the largest), otherwise one cooperative team each.  Results and info words
+ * as usbs_eigsh_smallest's, per problem (host array of `count` problems).
+ * No counterpart in the reference, which solves one instance per call. */
+int usbs_eigsh_smallest_batched(int count, const usbs_eigsh_problem* problems,
+                                int inner_iterations, int max_restarts, double tolerance,
+                                int precision, void* stream);
+
 /* ------------------------------------------------------------------ usbs()
  * One SDP instance, resident in device memory.  Field meanings follow the
  * reference's SDPState (utils/common.py:11-26) after scale_sdp_state. */

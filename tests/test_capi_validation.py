@@ -94,3 +94,25 @@ def test_qap_round_rejects_bad_sizes(lib):
     rc = lib.usbs_qap_round(10, 10, FAKE, FAKE, 101, FAKE, FAKE, 1e-6, FAKE, None, None, FAKE,
                             ws - 8, None)
     assert rc == -2 and "workspace" in _err(lib)
+
+
+def test_eigsh_batched_rejects_bad_problems(lib):
+    from usbs_gb300.api import EigshProblem
+    lib.usbs_eigsh_smallest_batched.argtypes = [ctypes.c_int, ctypes.POINTER(EigshProblem),
+                                                ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                                ctypes.c_int, P]
+    arr = (EigshProblem * 2)()
+    for p in arr:
+        p.n, p.nnz, p.num_desired, p.ldq = 100, 300, 4, 128
+        p.workspace, p.workspace_bytes = 256, 1 << 30
+    assert lib.usbs_eigsh_smallest_batched(0, arr, 32, 10, 1e-7, 64, None) == 0   # nothing to do
+    assert lib.usbs_eigsh_smallest_batched(2, arr, 33, 10, 1e-7, 64, None) == -2
+    assert "inner_iterations" in _err(lib)
+    arr[1].ldq = 99
+    assert lib.usbs_eigsh_smallest_batched(2, arr, 32, 10, 1e-7, 64, None) == -2
+    assert "problem 1" in _err(lib) and "bad sizes" in _err(lib)
+    arr[1].ldq = 128
+    arr[0].workspace_bytes = 16
+    assert lib.usbs_eigsh_smallest_batched(2, arr, 32, 10, 1e-7, 64, None) == -2
+    assert "problem 0" in _err(lib) and "workspace" in _err(lib)
+    assert lib.usbs_eigsh_smallest_batched(2, arr, 32, 10, 1e-7, 16, None) == -2

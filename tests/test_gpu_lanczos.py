@@ -256,3 +256,56 @@ def test_eigsh_team_kernel_matches_oracle(cuda, side, precision):
     Op = ((-st.C) + sp.diags(y)).tocsr()
     r = np.linalg.norm(Op @ gV - gV * gv[None, :], axis=0)
     assert r.max() < (1e-6 if precision == 64 else 1e-2) * scale
+
+
+def _maxcut_case(cuda, Wg, seed):
+    from usbs_gb300.problem import DeviceProblem, layout
+    st = omaxcut.initialize_state(Wg, 4)
+    n = st.C.shape[0]
+    prob = DeviceProblem(layout(st.C, st.A_data, st.A_indices, m=n), cuda)
+    y = np.random.default_rng(seed).standard_normal(n) * 0.5
+    return st, prob, y, orng.default_q0(n)
+
+
+# Many independent instances in one launch: six small graphs run as clusters
+# of one launch; with a 22,500-node graph in the batch every problem runs on
+# the cooperative team kernel, one team per problem
+@pytest.mark.parametrize("with_large", [False, True])
+def test_eigsh_batched_matches_oracle(cuda, with_large):
+    from usbs_gb300 import api
+    graphs = [wl.er_graph(300 + 100 * i, 2000 + 900 * i, 10 + i) for i in range(6)]
+    if with_large:
+        graphs.insert(2, wl.er_graph(22500, 90000, 150))
+    cases = [_maxcut_case(cuda, g, 20 + i) for i, g in enumerate(graphs)]
+    nd, restarts, tol = 4, 200, 1e-9
+    out = api.eigsh_smallest_batched([(p, y, q0) for _, p, y, q0 in cases], nd, 32, restarts, tol,
+                                     c_scale=-1.0, precision=64, return_info=True)
+    assert len(out) == len(cases)
+    for (st, p, y, q0), (gv, gV, info) in zip(cases, out):
+        n = p.n
+        ov, oV, ost = olz.eigsh_smallest(n, (-st.C).tocsr(), st.A_data, st.A_indices, y, q0, nd,
+                                         32, restarts, tol)
+        gv, gV = _np(gv), _np(gV)
+        assert info.status == 0 and ost["nconv"] >= nd
+        scale = np.abs(ov).max()
+        np.testing.assert_allclose(gv, ov, rtol=1e-9, atol=1e-9 * scale)
+        for j in range(nd):
+            assert abs(gV[:, j] @ oV[:, j]) > 1 - 1e-10, (n, j)
+
+
+def test_eigsh_batched_many_matches_single_calls(cuda):
+    """More problems than one launch takes (48): the batch splits; every result
+    equals that of a separate eigsh_smallest call to round-off."""
+    from usbs_gb300 import api
+    cases = [_maxcut_case(cuda, wl.er_graph(200 + 7 * i, 1200 + 40 * i, 100 + i), 300 + i)
+             for i in range(53)]
+    nd, restarts, tol = 3, 100, 1e-9
+    out = api.eigsh_smallest_batched([(p, y, q0) for _, p, y, q0 in cases], nd, 32, restarts, tol,
+                                     c_scale=-1.0, precision=64)
+    for (st, p, y, q0), (gv, gV) in zip(cases, out):
+        sv, sV = api.eigsh_smallest(p.n, p, None, None, y, q0, nd, 32, restarts, tol,
+                                    c_scale=-1.0, precision=64)
+        sv, gv = _np(sv), _np(gv)
+        np.testing.assert_allclose(gv, sv, rtol=1e-10, atol=1e-10 * np.abs(sv).max())
+        G = _np(gV).T @ _np(sV)
+        assert np.abs(np.abs(np.diag(G)) - 1).max() < 1e-9

@@ -31,6 +31,8 @@ SIGNATURES = {
     "usbs_eigsh_workspace_bytes": (c_size_t, [c_int, c_ll, c_int, c_int]),
     "usbs_eigsh_smallest": (c_int, [c_int, c_ll, P, P, P, c_double, P, P, P, P, P, P, c_int, c_int, c_int,
                                     c_double, c_int, P, c_int, P, P, P, c_size_t, P]),
+    # struct-array entry point; usbs_gb300.api installs the exact ctypes types
+    "usbs_eigsh_smallest_batched": (c_int, [c_int, P, c_int, c_int, c_double, c_int, P]),
     "usbs_eigsh_smallest_noalloc": (c_int, [c_int, c_ll, P, P, P, c_double, P, P, P, P, P, P, c_int,
                                             c_int, c_int, c_double, c_int, P, c_int, P, P, P]),
     # struct-typed entry points; usbs_gb300.solver installs the exact ctypes types

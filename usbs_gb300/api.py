@@ -182,3 +182,66 @@ def eigsh_smallest(n, C, A_data, A_indices, adjoint_left_vec, q0, num_desired, i
             raise RuntimeError("eigsh_smallest: a team barrier timed out on the device")
         return evals, vecs, inf
     return evals, vecs
+
+
+class EigshProblem(ctypes.Structure):
+    """usbs_eigsh_problem (include/usbs_gb300.h)."""
+    _fields_ = [("n", ctypes.c_int), ("nnz", ctypes.c_longlong)] + \
+        [(f, ctypes.c_void_p) for f in ("rowptr", "col", "c_val")] + [("c_scale", ctypes.c_double)] + \
+        [(f, ctypes.c_void_p) for f in ("slot_ptr", "slot_tid", "t_con", "t_a",
+                                         "adjoint_left_vec", "q0")] + \
+        [("num_desired", ctypes.c_int), ("Q", ctypes.c_void_p), ("ldq", ctypes.c_int),
+         ("eigenvalues", ctypes.c_void_p), ("info", ctypes.c_void_p),
+         ("workspace", ctypes.c_void_p), ("workspace_bytes", ctypes.c_size_t)]
+
+
+def eigsh_smallest_batched(problems, num_desired, inner_iterations, max_restarts, tolerance, *,
+                           c_scale=1.0, precision=64, return_info=False):
+    """eigsh_smallest for many independent problems in as few launches as the
+    kernels allow (up to 48 per launch): ``problems`` is a list of
+    ``(DeviceProblem, adjoint_left_vec, q0)`` on one device.  Returns a list of
+    ``(eigenvalues, eigenvectors)`` (with an EigshInfo each if return_info)."""
+    torch = _torch()
+    lib = _lib.load()
+    fn = lib.usbs_eigsh_smallest_batched
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_int, ctypes.POINTER(EigshProblem), ctypes.c_int, ctypes.c_int,
+                   ctypes.c_double, ctypes.c_int, ctypes.c_void_p]
+    vt = _vt(precision)
+    keep, out = [], []
+    arr = (EigshProblem * max(len(problems), 1))()
+    for i, (prob, w, q0) in enumerate(problems):
+        dev = prob.device
+        n = prob.n
+        wt = _dev(w, torch.float64, dev)
+        q0t = _dev(q0, vt, dev)
+        ld = (n + 31) // 32 * 32
+        Q = torch.empty((inner_iterations + 1, ld), dtype=vt, device=dev)
+        evals = torch.empty(num_desired, dtype=torch.float64, device=dev)
+        info = torch.zeros(16, dtype=torch.int32, device=dev)
+        need = int(lib.usbs_eigsh_workspace_bytes(n, prob.nnz, inner_iterations, precision))
+        ws = torch.empty(need, dtype=torch.uint8, device=dev)
+        keep += [wt, q0t, Q, ws]
+        a = arr[i]
+        a.n, a.nnz = n, prob.nnz
+        a.rowptr, a.col, a.c_val = prob.rowptr.data_ptr(), prob.col.data_ptr(), prob.c_val.data_ptr()
+        a.c_scale = float(c_scale)
+        a.slot_ptr, a.slot_tid = prob.slot_ptr.data_ptr(), prob.slot_tid.data_ptr()
+        a.t_con, a.t_a = prob.t_con.data_ptr(), prob.t_a0.data_ptr()
+        a.adjoint_left_vec, a.q0 = wt.data_ptr(), q0t.data_ptr()
+        a.num_desired, a.Q, a.ldq = num_desired, Q.data_ptr(), ld
+        a.eigenvalues, a.info = evals.data_ptr(), info.data_ptr()
+        a.workspace, a.workspace_bytes = ws.data_ptr(), need
+        out.append((evals, Q[:num_desired, :n].t(), info))
+    rc = fn(len(problems), arr, inner_iterations, max_restarts, float(tolerance), precision,
+            _stream())
+    _lib.check(rc, "usbs_eigsh_smallest_batched")
+    if not return_info:
+        return [(e, v) for e, v, _ in out]
+    res = []
+    for e, v, info in out:
+        inf = EigshInfo(info.cpu().tolist())
+        if inf.status & 1:
+            raise RuntimeError("eigsh_smallest_batched: a team barrier timed out on the device")
+        res.append((e, v, inf))
+    return res

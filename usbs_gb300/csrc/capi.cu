@@ -229,6 +229,75 @@ int usbs_eigsh_smallest(int n, long long nnz, const int* rowptr, const int* col,
   return 0;
 }
 
+int usbs_eigsh_smallest_batched(int count, const usbs_eigsh_problem* problems,
+                                int inner_iterations, int max_restarts, double tolerance,
+                                int precision, void* stream) {
+  if (precision != 32 && precision != 64) { set_error("precision must be 32 or 64"); return -2; }
+  if (count < 0 || (count > 0 && !problems) || inner_iterations < 1 ||
+      inner_iterations > MAXM || max_restarts < 0) {
+    set_error("eigsh_batched: bad arguments count=%d inner_iterations=%d (<= %d) max_restarts=%d",
+              count, inner_iterations, MAXM, max_restarts);
+    return -2;
+  }
+  for (int i = 0; i < count; ++i) {
+    const usbs_eigsh_problem& q = problems[i];
+    if (q.n < 1 || q.ldq < q.n || q.num_desired < 1 || q.num_desired > inner_iterations ||
+        q.nnz < 0 || q.nnz > 0x7fffffffLL) {
+      set_error("eigsh_batched: problem %d: bad sizes n=%d ldq=%d num_desired=%d nnz=%lld", i,
+                q.n, q.ldq, q.num_desired, q.nnz);
+      return -2;
+    }
+    const size_t need = usbs_eigsh_workspace_bytes(q.n, q.nnz, inner_iterations, precision);
+    if (!q.workspace || q.workspace_bytes < need) {
+      set_error("eigsh_batched: problem %d: workspace of %zu bytes given, %zu needed", i,
+                q.workspace_bytes, need);
+      return -2;
+    }
+  }
+  if (count == 0) return 0;
+  DeviceInfo di;
+  int rc = get_device_info(&di);
+  if (rc) return rc;
+  cudaStream_t st = (cudaStream_t)stream;
+  const int vt = (precision == 64) ? 8 : 4;
+  constexpr int CHUNK = 48;                 // problems per launch (the kernels' batch limit)
+  LanczosProblem lp[CHUNK];
+  for (int c0 = 0; c0 < count; c0 += CHUNK) {
+    const int cnt = (count - c0) < CHUNK ? (count - c0) : CHUNK;
+    for (int j = 0; j < cnt; ++j) {
+      const usbs_eigsh_problem& q = problems[c0 + j];
+      char* w = (char*)q.workspace;
+      void* op_val = w; w += a256((size_t)(q.nnz > 0 ? q.nnz : 1) * vt);
+      double* alpha = (double*)w;
+      w += a256(2 * MAXM * sizeof(double));
+      rc = assemble_operator((int)q.nnz, q.c_val, q.c_scale, q.slot_ptr, q.slot_tid, q.t_con,
+                             q.t_a, q.adjoint_left_vec, op_val, precision, st);
+      if (rc) return rc;
+      if (cudaMemcpyAsync(q.Q, q.q0, (size_t)q.n * vt, cudaMemcpyDeviceToDevice, st) != cudaSuccess ||
+          cudaMemsetAsync(alpha, 0, 2 * MAXM * sizeof(double), st) != cudaSuccess) {
+        set_error("eigsh_batched: staging copy failed");
+        return -5;
+      }
+      LanczosProblem& p = lp[j];
+      p.n = q.n; p.ld = q.ldq; p.m = inner_iterations; p.num_desired = q.num_desired;
+      p.max_restarts = max_restarts; p.nnz = q.nnz; p.tol = tolerance;
+      p.rowptr = q.rowptr; p.col = q.col; p.val = op_val; p.Q = q.Q;
+      p.alpha = alpha; p.beta = alpha + MAXM; p.ctl = q.info; p.status = q.info + 5; p.work = w;
+    }
+    rc = lanczos_run(di, lp, cnt, precision, st);
+    if (rc) return rc;
+    for (int j = 0; j < cnt; ++j) {
+      if (cudaMemcpyAsync(problems[c0 + j].eigenvalues, lp[j].alpha,
+                          (size_t)lp[j].num_desired * sizeof(double), cudaMemcpyDeviceToDevice,
+                          st) != cudaSuccess) {
+        set_error("eigsh_batched: result copy failed");
+        return -5;
+      }
+    }
+  }
+  return 0;
+}
+
 int usbs_eigsh_smallest_noalloc(int n, long long nnz, const int* rowptr, const int* col,
                                 const double* c_val, double c_scale, const int* slot_ptr,
                                 const int* slot_tid, const int* t_con, const double* t_a,
