@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define USBS_GB300_ABI_VERSION 2
+#define USBS_GB300_ABI_VERSION 3
 
 /* ABI version of the loaded library (USBS_GB300_ABI_VERSION). */
 int usbs_abi_version(void);
@@ -277,6 +277,11 @@ typedef struct usbs_state {
    * bar_primal_obj, tr_X_bar, b.y; usbs_cgal_solve: its first 8 trace fields);
    * the scaled problem's values, as the reference's cond_func sees them */
   double cond[20];
+  /* outer iterations that ran as one launch of the captured CUDA graph of the
+   * iteration (usbs_solve: problems without inequality constraints whose
+   * Lanczos runs as one cluster; the others run eagerly); negative: the
+   * capture failed with that CUDA error and every iteration ran eagerly */
+  long long graph_iterations;
 } usbs_state;
 
 /* Called on the host at every condition check (after the device has caught

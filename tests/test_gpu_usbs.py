@@ -259,3 +259,47 @@ def test_usbs_renumbered_matches_plain(cuda):
     np.testing.assert_allclose(b.P.cpu().numpy(), a.P.cpu().numpy(), rtol=1e-6,
                                atol=1e-6 * np.abs(a.P.cpu().numpy()).max())
     np.testing.assert_allclose(b.y.cpu().numpy(), a.y.cpu().numpy(), rtol=1e-6, atol=1e-8)
+
+
+@pytest.mark.parametrize("precision,cond_base", [(64, 1.0), (32, 1.5)])
+def test_usbs_graph_replay_equals_eager(cuda, monkeypatch, precision, cond_base):
+    """The captured CUDA graph of the outer iteration runs the same kernels on
+    the same data as the eager iteration: traces and final iterates are
+    bit-identical, with condition checks every iteration (base 1) and in
+    geometric blocks (base 1.5, several graph launches between host waits)."""
+    from usbs_gb300 import solver
+    W = wl.torus_graph(30, 1)
+    st = omaxcut.initialize_state(W, 10)
+    n = st.C.shape[0]
+    q0 = orng.default_q0(n)
+    args = (st, n, n, 2.0 * n, 2.0, S["rho"], S["beta"], 10, 1, 12, np.inf, -1.0, -1.0, -1.0, 32,
+            10, 1e-7, S["subprob_max_iters"], cond_base)
+    kw = dict(q0=q0, precision=precision, return_trace=True, return_info=True)
+    monkeypatch.setenv("USBS_GRAPH", "0")
+    a, atr, ainfo = solver.usbs(*args, **kw)
+    monkeypatch.setenv("USBS_GRAPH", "1")
+    b, btr, binfo = solver.usbs(*args, **kw)
+    assert ainfo["graph_iterations"] == 0
+    assert binfo["graph_iterations"] == binfo["iterations"] == 12
+    assert ainfo["kernel_launches"] == binfo["kernel_launches"]
+    assert len(atr) == len(btr) == 12
+    for x, y in zip(atr, btr):
+        assert np.array_equal(np.array(list(x.values())), np.array(list(y.values())),
+                              equal_nan=True), (x, y)
+    for f in ("y", "z", "P"):
+        assert np.array_equal(getattr(a, f).cpu().numpy(), getattr(b, f).cpu().numpy()), f
+    assert a.primal_obj == b.primal_obj and a.tr_X == b.tr_X
+    assert binfo["lanczos_launches"] >= 1 and binfo["lanczos_ms"] > 0
+
+
+def test_usbs_graph_not_used_with_inequalities(cuda):
+    """The QAP relaxation decides its upsilon loop on the host: it runs eagerly."""
+    from usbs_gb300 import solver
+    from oracle import qap as oqap
+    D, Wf = wl.qap_instance(6, 0, grid=5)
+    st = oqap.initialize_state(D, Wf, 6)
+    n, m = st.C.shape[0], st.b.shape[0]
+    _, info = solver.usbs(st, n, m, 14.0 * st.SCALE_X, 2.0, 0.005, 0.25, 2, 0, 2, np.inf, -1.0,
+                          -1.0, -1.0, min(n, 32), 10, 1e-7, 100, q0=orng.default_q0(n),
+                          precision=64, return_info=True)
+    assert info["status"] == 0 and info["graph_iterations"] == 0

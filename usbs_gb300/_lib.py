@@ -70,7 +70,7 @@ def load(build_if_missing=True):
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.usbs_abi_version() != 2:
+    if lib.usbs_abi_version() != 3:
         raise LibraryError("libusbs_gb300 ABI version mismatch")
     _lib = lib
     return lib

@@ -1809,7 +1809,9 @@ static int run_cluster(const LanczosProblem* probs, int count, cudaStream_t stre
   cfg.attrs = attr;
   cfg.numAttrs = 1;
   int nclusters = 0;
-  if (cudaOccupancyMaxActiveClusters(&nclusters, (const void*)lanczos_cluster_kernel<VT>, &cfg) !=
+  cudaLaunchConfig_t qcfg = cfg;     // the query needs no stream (this one may be capturing)
+  qcfg.stream = nullptr;
+  if (cudaOccupancyMaxActiveClusters(&nclusters, (const void*)lanczos_cluster_kernel<VT>, &qcfg) !=
           cudaSuccess || nclusters < 1) {
     cudaGetLastError();
     return 1;

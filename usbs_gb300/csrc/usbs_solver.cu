@@ -9,6 +9,7 @@
 // (solver/usbs.py:543-688); the notes at each step name the lines.
 #include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 #include "../../include/usbs_gb300.h"
 #include "common.cuh"
@@ -565,7 +566,8 @@ struct PostArgs {
   int refined;               // use the FP64 Rayleigh quotients in smalls[o_GR] instead
   double trace_ub, trace_factor, beta, scale_c, scale_x, bnorm;
   double* trace;             // TR_NUM doubles per iteration (optional)
-  int t;
+  int trace_capacity;
+  int t;                     // < 0: the iteration counter in smalls (a replayed graph)
   const int* skip;
 };
 
@@ -575,6 +577,7 @@ __global__ void post_kernel(PostArgs a) {
   if (a.skip && *a.skip) return;
   if (threadIdx.x != 0) return;
   double* sc = a.smalls + a.o_sc;
+  const int t = a.t >= 0 ? a.t : (int)sc[SC_T];
   double lam0 = -a.alpha[0];
   if (a.refined) lam0 = -a.smalls[a.o_GR];
   const double eta = sc[SC_ETA];
@@ -611,10 +614,10 @@ __global__ void post_kernel(PostArgs a) {
   sc[SC_INFGAP] = infgap;
   sc[SC_MAXINF] = maxinf;
   sc[SC_DESCENT] = descent ? 1.0 : 0.0;
-  sc[SC_T] = a.t + 1;
-  if (a.trace) {
-    double* r = a.trace + (size_t)a.t * TR_NUM;
-    r[TR_T] = a.t; r[TR_PRIMAL] = primal_n; r[TR_OBJUB] = ub; r[TR_OBJGAP] = gap;
+  sc[SC_T] = t + 1;
+  if (a.trace && t < a.trace_capacity) {
+    double* r = a.trace + (size_t)t * TR_NUM;
+    r[TR_T] = t; r[TR_PRIMAL] = primal_n; r[TR_OBJUB] = ub; r[TR_OBJGAP] = gap;
     r[TR_INFGAP] = infgap; r[TR_MAXINF] = maxinf; r[TR_PEN] = pen_n; r[TR_CANDPEN] = cand_pen;
     r[TR_LB] = lb; r[TR_LAM0] = lam0; r[TR_DESCENT] = descent ? 1.0 : 0.0; r[TR_ETA] = eta;
     r[TR_TRS] = sc[SC_TRS]; r[TR_TRX] = trX_n; r[TR_QITERS] = sc[SC_QITERS];
@@ -740,6 +743,16 @@ struct Solver {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_l0 = nullptr, ev_l1 = nullptr;
   bool lz_pending = false;
   long long launches = 0;
+  // CUDA graph of one outer iteration (captured at the first one, replayed)
+  bool use_graph = false, capturing = false;
+  cudaStream_t gst = nullptr;        // capture origin (the caller's stream may be the legacy one)
+  cudaGraphExec_t gexec = nullptr;
+  long long graph_body_launches = 0;
+  // event record on the main stream; while capturing, a graph node of its own
+  void record(cudaEvent_t e) {
+    if (capturing) cudaEventRecordWithFlags(e, st, cudaEventRecordExternal);
+    else cudaEventRecord(e, st);
+  }
   // algorithmic bytes of one Lanczos launch from its counters (ctl[2], [4], [13], [14])
   double lanczos_bytes(const int* c) const {
     const double b = (double)L.vt, n = L.n, nnz = (double)P->nnz;
@@ -836,9 +849,9 @@ struct Solver {
     if (cudaMemcpyAsync(L.Q, L.q0L, (size_t)L.n * L.vt, cudaMemcpyDeviceToDevice, st) != cudaSuccess)
       return kerr("q0 copy");
     if (timed) {
-      cudaEventRecord(ev_l0, st);
+      record(ev_l0);
       const int rc = lanczos_launch(num_desired);
-      cudaEventRecord(ev_l1, st);
+      record(ev_l1);
       lz_pending = true;
       return rc;
     }
@@ -1033,7 +1046,8 @@ static int body(Solver& X, int t) {
     pa.smalls = L.smalls; pa.o_sc = L.o_sc; pa.o_GR = L.o_GR; pa.kc = L.kc; pa.alpha = L.alpha;
     pa.refined = refined; pa.trace_ub = Pa->trace_ub; pa.trace_factor = Pa->trace_factor;
     pa.beta = Pa->beta; pa.scale_c = P->scale_c; pa.scale_x = P->scale_x; pa.bnorm = P->b_norm;
-    pa.trace = (S->trace && t < S->trace_capacity) ? S->trace : nullptr;
+    pa.trace = S->trace;
+    pa.trace_capacity = S->trace ? S->trace_capacity : 0;
     pa.t = t; pa.skip = nullptr;
     ++X.launches;
     post_kernel<<<1, 32, 0, st>>>(pa);
@@ -1057,6 +1071,59 @@ static int body(Solver& X, int t) {
   if (cudaMemcpyAsync(V, L.Vn, (size_t)L.ld * L.k * sizeof(double), cudaMemcpyDeviceToDevice, st) != cudaSuccess)
     return kerr("V copy");
   return 0;
+}
+
+// One outer iteration.  Problems without inequality constraints (no host
+// decision inside the body) whose Lanczos runs as one cluster replay a CUDA
+// graph of the body: captured at the first iteration on a stream of the
+// solver's own (capture is not possible on the legacy default stream), with
+// the iteration number read on the device (post_kernel); each iteration is
+// then one cudaGraphLaunch into the caller's stream and the host does not
+// wait between iterations of a condition-check block.  If the capture fails
+// the solve continues eagerly and graph_iterations holds -(the CUDA error).
+static bool graph_wanted(const Solver& X) {
+  const char* e = getenv("USBS_GRAPH");           // 0 runs every iteration eagerly
+  if (e && atoi(e) == 0) return false;
+  return !X.P->has_ineq && !X.S->debug &&
+         lanczos_kernel_kind(X.L.n, X.Pa->lanczos_inner_iterations, X.Pa->precision) == 1;
+}
+
+static int step(Solver& X, int t) {
+  if (!X.use_graph) return body(X, t);
+  if (!X.gexec) {
+    cudaGraph_t g = nullptr;
+    const long long l0 = X.launches;
+    cudaError_t e = cudaStreamCreateWithFlags(&X.gst, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamBeginCapture(X.gst, cudaStreamCaptureModeRelaxed);
+    int rc = -5;
+    if (e == cudaSuccess) {
+      const cudaStream_t user = X.st;
+      X.st = X.gst;
+      X.capturing = true;
+      rc = body(X, -1);
+      X.capturing = false;
+      X.st = user;
+      e = cudaStreamEndCapture(X.gst, &g);
+      if (rc != 0 && e == cudaSuccess) e = cudaErrorUnknown;
+    }
+    if (e == cudaSuccess && g) e = cudaGraphInstantiate(&X.gexec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    X.graph_body_launches = X.launches - l0;
+    X.launches = l0;
+    if (e != cudaSuccess || !X.gexec) {
+      cudaGetLastError();                           // nothing was launched: run eagerly
+      if (X.gexec) cudaGraphExecDestroy(X.gexec);
+      X.gexec = nullptr;
+      X.use_graph = false;
+      X.lz_pending = false;
+      X.S->graph_iterations = -(long long)(e != cudaSuccess ? e : cudaErrorUnknown);
+      return body(X, t);
+    }
+  }
+  X.launches += X.graph_body_launches;
+  X.lz_pending = true;
+  ++X.S->graph_iterations;
+  return cudaGraphLaunch(X.gexec, X.st) == cudaSuccess ? 0 : kerr("graph launch");
 }
 
 // geometric schedule of condition checks (utils/loop.py:84-98)
@@ -1331,8 +1398,12 @@ int usbs_solve(const usbs_problem* P, const usbs_params* Pa, usbs_state* S, void
       if (x->ev_join) cudaEventDestroy(x->ev_join);
       if (x->ev_l0) cudaEventDestroy(x->ev_l0);
       if (x->ev_l1) cudaEventDestroy(x->ev_l1);
+      if (x->gexec) cudaGraphExecDestroy(x->gexec);
+      if (x->gst) cudaStreamDestroy(x->gst);
     }
   } cleanup{&X};
+  S->graph_iterations = 0;
+  X.use_graph = graph_wanted(X);
   cudaMemsetAsync(L.counters, 0, 64 * sizeof(unsigned int), st);
   cudaMemsetAsync(L.status, 0, 32 * sizeof(int), st);
   cudaMemsetAsync(L.smalls, 0, (size_t)L.n_smalls * sizeof(double), st);
@@ -1421,11 +1492,11 @@ int usbs_solve(const usbs_problem* P, const usbs_params* Pa, usbs_state* S, void
   CK(cond(0, &go));
   for (size_t b = 0; b < sched.size() && go; ++b) {
     for (long long j = 0; j < sched[b]; ++j) {
-      if (j > 0) {   // within a block: sync only to collect the previous Lanczos timing
+      if (j > 0 && !X.use_graph) {   // eager: sync to collect the previous Lanczos timing
         if (cudaStreamSynchronize(st) != cudaSuccess) return kerr("iteration");
         CK(X.collect_lanczos());
       }
-      CK(body(X, t));
+      CK(step(X, t));
       ++t;
     }
     if (cudaStreamSynchronize(st) != cudaSuccess) return kerr("iteration");

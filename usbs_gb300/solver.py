@@ -60,7 +60,8 @@ class UsbsState(ctypes.Structure):
          ("pen_dual_obj", ctypes.c_double), ("elapsed", ctypes.c_double),
          ("status", ctypes.c_int), ("lanczos_launches", ctypes.c_int),
          ("lanczos_ms", ctypes.c_double), ("lanczos_bytes", ctypes.c_double),
-         ("kernel_launches", ctypes.c_longlong), ("cond", ctypes.c_double * 20)]
+         ("kernel_launches", ctypes.c_longlong), ("cond", ctypes.c_double * 20),
+         ("graph_iterations", ctypes.c_longlong)]
 
 
 class CgalParams(ctypes.Structure):
@@ -325,7 +326,7 @@ def usbs(sdp_state, n, m, trace_ub, trace_factor, rho, beta, k_curr, k_past, max
                 elapsed=pst.elapsed, status=pst.status, callback_vals=cb_val,
                 V=V[:, :n].t(), lanczos_launches=pst.lanczos_launches,
                 lanczos_ms=pst.lanczos_ms, lanczos_bytes=pst.lanczos_bytes,
-                kernel_launches=pst.kernel_launches)
+                kernel_launches=pst.kernel_launches, graph_iterations=pst.graph_iterations)
     out, info = ren.restore(out, info)
     if return_trace:
         tr = trace[:pst.iterations].cpu().numpy()
