@@ -362,9 +362,13 @@ def eigsh_batched_leg(device, count=48, seed=9, reps=3):
         ts, rs = timed(lambda: [api.eigsh_smallest(p.n, p, None, None, y, q0, 10, 32, 10, 1e-7,
                                                    c_scale=-1.0, precision=prec)
                                 for p, y, q0 in probs])
+        # the smallest eigenvalue converges; the trailing returned values need
+        # not (10 restarts), and which ones the restart keeps depends on rounding
+        dev0 = max(float(abs(a[0][0] - b[0][0]) / abs(b[0][0])) for a, b in zip(rb, rs))
         dev = max(float((a[0] - b[0]).abs().max() / b[0].abs().max()) for a, b in zip(rb, rs))
         out[f"fp{prec}"] = {"batched_solves_per_s": count / tb, "serial_solves_per_s": count / ts,
-                            "speedup": ts / tb, "max_rel_eigenvalue_diff": dev}
+                            "speedup": ts / tb, "max_rel_diff_smallest_eigenvalue": dev0,
+                            "max_rel_diff_all_returned": dev}
     return out
 
 
@@ -388,7 +392,9 @@ def serving_leg(device, count=16, iters=30, slots=8, seed=4):
     """Requests of `serving_stream` solved (a fixed `iters` outer iterations
     each, reference settings) through SolverService in mixed precision, released
     at their arrival times, against the same requests run one after another on
-    the plain FP64 single-instance path.  Returns throughput and latencies."""
+    the plain FP64 single-instance path.  Returns throughput and latencies, with
+    the service's cluster Lanczos at the library's single-solve spread (0) and
+    packed at 640 rows per CTA."""
     import torch
     from usbs_gb300 import solver
     from usbs_gb300.serving import SolveRequest, SolverService
@@ -410,8 +416,9 @@ def serving_leg(device, count=16, iters=30, slots=8, seed=4):
         solver.usbs(st, precision=64, device=device, **kw(n))
     torch.cuda.synchronize()
     serial = time.perf_counter() - t0
-    def served(nslots, paced):
-        with SolverService(device=device, max_slots=nslots, reserve_bytes=4 << 30) as svc:
+    def served(nslots, paced, rows):
+        with SolverService(device=device, max_slots=nslots, reserve_bytes=4 << 30,
+                           lanczos_rows_per_cta=rows) as svc:
             t0 = time.perf_counter()
             handles = []
             for arr, n, st in stream:
@@ -423,18 +430,24 @@ def serving_leg(device, count=16, iters=30, slots=8, seed=4):
             wall = time.perf_counter() - t0
         return wall, np.array([h.latency for h in handles])
 
-    wall, lat = served(slots, True)
     # capacity: every request queued at once (the service admits them as slots free up)
-    sat = {q: served(q, False)[0] for q in (slots, 2 * slots)}
+    sat = {(q, r): served(q, False, r)[0] for q in (slots, 2 * slots) for r in (0, 640)}
     best = min(sat, key=sat.get)
+    paced = {r: served(slots, True, r) for r in (0, 640)}
+    rows = min(paced, key=lambda r: paced[r][0])
+    wall, lat = paced[rows]
     return {"requests": count, "outer_iterations_each": iters, "slots": slots,
-            "n_range": [200, 2000], "arrivals": "Poisson 20/s",
+            "n_range": [200, 2000], "arrivals": "Poisson 20/s", "lanczos_rows_per_cta": rows,
             "served_requests_per_s": count / wall, "p50_latency_s": float(np.percentile(lat, 50)),
             "p99_latency_s": float(np.percentile(lat, 99)),
+            "paced_requests_per_s_by_rows_per_cta": {str(r): count / w for r, (w, _) in
+                                                     paced.items()},
             "serial_fp64_requests_per_s": count / serial,
             "throughput_ratio_vs_serial_fp64": (count / wall) / (count / serial),
-            "saturated": {"slots": best, "requests_per_s": count / sat[best],
-                          "by_slots": {str(q): count / w for q, w in sat.items()},
+            "saturated": {"slots": best[0], "lanczos_rows_per_cta": best[1],
+                          "requests_per_s": count / sat[best],
+                          "by_slots_and_rows_per_cta": {f"{q}/{r}": count / w
+                                                        for (q, r), w in sat.items()},
                           "ratio_vs_serial_fp64": serial / sat[best]}}
 
 

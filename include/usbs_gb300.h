@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define USBS_GB300_ABI_VERSION 3
+#define USBS_GB300_ABI_VERSION 4
 
 /* ABI version of the loaded library (USBS_GB300_ABI_VERSION). */
 int usbs_abi_version(void);
@@ -197,6 +197,28 @@ int usbs_eigsh_smallest_batched(int count, const usbs_eigsh_problem* problems,
                                 int inner_iterations, int max_restarts, double tolerance,
                                 int precision, void* stream);
 
+/* Cluster-size autotuner for the Lanczos launches (no counterpart in the
+ * reference).  A cluster-path launch spreads its problems over
+ * ceil(n_max / rows_per_cta) CTAs per cluster (at most 16): one problem
+ * alone runs fastest spread thin, a batch or concurrent solves fastest packed.
+ * usbs_lanczos_autotune runs the batch (as usbs_eigsh_smallest_batched, at
+ * most 48 problems) once per candidate rows per CTA (64, 128, 256, 640, 1280;
+ * candidates giving the same cluster size are skipped, their time -1), times
+ * each with CUDA events on `stream` after a warm-up run, records the fastest
+ * for the batch's class -- (precision, floor(log2(count)), floor(log2(max n)))
+ * -- in a process-wide table that later launches of that class use, and
+ * returns with the batch's outputs from the chosen candidate.  Host call that
+ * waits for the device. */
+int usbs_lanczos_autotune(int count, const usbs_eigsh_problem* problems, int inner_iterations,
+                          int max_restarts, double tolerance, int precision, void* stream,
+                          int* best_rows_per_cta, float* candidate_ms /* [5] or NULL */);
+/* The table: entries as keys (precision << 32 | log2 count << 16 | log2 max n)
+ * and rows per CTA; returns the number of entries (writes at most capacity). */
+int usbs_lanczos_tuning_get(long long* keys, int* rows_per_cta, int capacity);
+/* Sets (rows_per_cta >= 16) or erases (0) the entry of a class. */
+int usbs_lanczos_tuning_put(int precision, int count, int max_n, int rows_per_cta);
+void usbs_lanczos_tuning_clear(void);
+
 /* ------------------------------------------------------------------ usbs()
  * One SDP instance, resident in device memory.  Field meanings follow the
  * reference's SDPState (utils/common.py:11-26) after scale_sdp_state. */
@@ -243,6 +265,8 @@ typedef struct usbs_params {
   int precision;            /* 64: FP64 everywhere; 32: FP32 Lanczos + FP64 rest */
   int sketch_mode;          /* 0: Nystrom sketch P = X Omega, 1: dense X, 2: diag(X) only */
   int sketch_dim;           /* columns of Omega (mode 0) */
+  int lanczos_rows_per_cta; /* cluster Lanczos: rows per CTA (>= 16); 0: the class's tuned
+                               choice (usbs_lanczos_autotune), else 64 */
 } usbs_params;
 
 /* Iterate state (device arrays, column-major with leading dimension ld) and

@@ -116,3 +116,27 @@ def test_eigsh_batched_rejects_bad_problems(lib):
     assert lib.usbs_eigsh_smallest_batched(2, arr, 32, 10, 1e-7, 64, None) == -2
     assert "problem 0" in _err(lib) and "workspace" in _err(lib)
     assert lib.usbs_eigsh_smallest_batched(2, arr, 32, 10, 1e-7, 16, None) == -2
+
+
+def test_lanczos_tuning_table_and_autotune_arguments(lib):
+    from usbs_gb300 import api
+    api.set_lanczos_tuning([], clear=True)
+    assert lib.usbs_lanczos_tuning_put(16, 1, 100, 640) == -2           # precision
+    assert lib.usbs_lanczos_tuning_put(32, 1, 100, 8) == -2             # rows per CTA < 16
+    assert lib.usbs_lanczos_tuning_put(32, 0, 100, 640) == -2           # count
+    api.set_lanczos_tuning([{"precision": 32, "log2_count": 5, "log2_max_n": 12,
+                             "rows_per_cta": 640},
+                            {"precision": 64, "log2_count": 0, "log2_max_n": 9,
+                             "rows_per_cta": 128}])
+    got = sorted((e["precision"], e["log2_count"], e["log2_max_n"], e["rows_per_cta"])
+                 for e in api.lanczos_tuning())
+    assert got == [(32, 5, 12, 640), (64, 0, 9, 128)]
+    assert lib.usbs_lanczos_tuning_put(32, 33, 5000, 0) == 0            # erase that class
+    assert [e["precision"] for e in api.lanczos_tuning()] == [64]
+    api.set_lanczos_tuning([], clear=True)
+    assert api.lanczos_tuning() == []
+    best = ctypes.c_int(0)
+    assert lib.usbs_lanczos_autotune(0, FAKE, 32, 10, 1e-7, 32, None, ctypes.byref(best),
+                                     None) == -2
+    assert lib.usbs_lanczos_autotune(49, FAKE, 32, 10, 1e-7, 32, None, ctypes.byref(best),
+                                     None) == -2

@@ -309,3 +309,38 @@ def test_eigsh_batched_many_matches_single_calls(cuda):
         np.testing.assert_allclose(gv, sv, rtol=1e-10, atol=1e-10 * np.abs(sv).max())
         G = _np(gV).T @ _np(sV)
         assert np.abs(np.abs(np.diag(G)) - 1).max() < 1e-9
+
+
+def test_lanczos_autotune_records_a_choice_and_keeps_parity(cuda):
+    """The tuner times the cluster sizes on a batch, records the fastest for
+    the class, and the class's later launches (which use it) still match the
+    oracle; an explicit rows-per-CTA request in a solve overrides the table."""
+    from usbs_gb300 import api, solver
+    api.set_lanczos_tuning([], clear=True)
+    cases = [_maxcut_case(cuda, wl.er_graph(1500 + 200 * i, 12000, 40 + i), 50 + i)
+             for i in range(4)]
+    probs = [(p, y, q0) for _, p, y, q0 in cases]
+    nd, restarts, tol = 4, 200, 1e-9
+    r = api.lanczos_autotune(probs, nd, 32, restarts, tol, c_scale=-1.0, precision=64)
+    assert r["rows_per_cta"] in api.TUNE_CANDIDATES
+    timed = [m for m in r["ms"].values() if m is not None]
+    assert len(timed) >= 2 and min(timed) == r["ms"][r["rows_per_cta"]]
+    tab = api.lanczos_tuning()
+    assert tab == [{"precision": 64, "log2_count": 2, "log2_max_n": 11,
+                    "rows_per_cta": r["rows_per_cta"]}]
+    out = api.eigsh_smallest_batched(probs, nd, 32, restarts, tol, c_scale=-1.0, precision=64)
+    for (st, p, y, q0), (gv, _) in zip(cases, out):
+        ov, _, _ = olz.eigsh_smallest(p.n, (-st.C).tocsr(), st.A_data, st.A_indices, y, q0, nd,
+                                      32, restarts, tol)
+        np.testing.assert_allclose(_np(gv), ov, rtol=1e-9, atol=1e-9 * np.abs(ov).max())
+    api.set_lanczos_tuning([], clear=True)
+    # a solve's own packing: same iterates as the default spread to round-off
+    st = omaxcut.initialize_state(wl.er_graph(2000, 12000, 3), 10)
+    n = st.C.shape[0]
+    args = (st, n, n, 2.0 * n, 2.0, 0.01, 0.25, 4, 1, 2, np.inf, -1.0, -1.0, -1.0, 32, 200, 1e-9,
+            100)
+    a, atr, _ = solver.usbs(*args, q0=orng.default_q0(n), precision=64, return_trace=True)
+    b, btr, _ = solver.usbs(*args, q0=orng.default_q0(n), precision=64, return_trace=True,
+                            lanczos_rows_per_cta=640)
+    for key in ("primal_obj", "obj_ub", "pen_dual_obj", "tr_X"):
+        assert abs(atr[0][key] - btr[0][key]) <= 1e-9 * max(1.0, abs(atr[0][key])), key

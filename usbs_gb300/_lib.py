@@ -33,6 +33,10 @@ SIGNATURES = {
                                     c_double, c_int, P, c_int, P, P, P, c_size_t, P]),
     # struct-array entry point; usbs_gb300.api installs the exact ctypes types
     "usbs_eigsh_smallest_batched": (c_int, [c_int, P, c_int, c_int, c_double, c_int, P]),
+    "usbs_lanczos_autotune": (c_int, [c_int, P, c_int, c_int, c_double, c_int, P, P, P]),
+    "usbs_lanczos_tuning_get": (c_int, [P, P, c_int]),
+    "usbs_lanczos_tuning_put": (c_int, [c_int, c_int, c_int, c_int]),
+    "usbs_lanczos_tuning_clear": (None, []),
     "usbs_eigsh_smallest_noalloc": (c_int, [c_int, c_ll, P, P, P, c_double, P, P, P, P, P, P, c_int,
                                             c_int, c_int, c_double, c_int, P, c_int, P, P, P]),
     # struct-typed entry points; usbs_gb300.solver installs the exact ctypes types
@@ -70,7 +74,7 @@ def load(build_if_missing=True):
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.usbs_abi_version() != 3:
+    if lib.usbs_abi_version() != 4:
         raise LibraryError("libusbs_gb300 ABI version mismatch")
     _lib = lib
     return lib

@@ -195,18 +195,11 @@ class EigshProblem(ctypes.Structure):
          ("workspace", ctypes.c_void_p), ("workspace_bytes", ctypes.c_size_t)]
 
 
-def eigsh_smallest_batched(problems, num_desired, inner_iterations, max_restarts, tolerance, *,
-                           c_scale=1.0, precision=64, return_info=False):
-    """eigsh_smallest for many independent problems in as few launches as the
-    kernels allow (up to 48 per launch): ``problems`` is a list of
-    ``(DeviceProblem, adjoint_left_vec, q0)`` on one device.  Returns a list of
-    ``(eigenvalues, eigenvectors)`` (with an EigshInfo each if return_info)."""
+def _eigsh_batch(problems, num_desired, inner_iterations, precision, c_scale):
+    """The usbs_eigsh_problem array of a batch with its output tensors (kept
+    alive in the returned list)."""
     torch = _torch()
     lib = _lib.load()
-    fn = lib.usbs_eigsh_smallest_batched
-    fn.restype = ctypes.c_int
-    fn.argtypes = [ctypes.c_int, ctypes.POINTER(EigshProblem), ctypes.c_int, ctypes.c_int,
-                   ctypes.c_double, ctypes.c_int, ctypes.c_void_p]
     vt = _vt(precision)
     keep, out = [], []
     arr = (EigshProblem * max(len(problems), 1))()
@@ -233,15 +226,87 @@ def eigsh_smallest_batched(problems, num_desired, inner_iterations, max_restarts
         a.eigenvalues, a.info = evals.data_ptr(), info.data_ptr()
         a.workspace, a.workspace_bytes = ws.data_ptr(), need
         out.append((evals, Q[:num_desired, :n].t(), info))
-    rc = fn(len(problems), arr, inner_iterations, max_restarts, float(tolerance), precision,
-            _stream())
-    _lib.check(rc, "usbs_eigsh_smallest_batched")
+    return arr, keep, out
+
+
+def _batch_results(out, return_info, what):
     if not return_info:
         return [(e, v) for e, v, _ in out]
     res = []
     for e, v, info in out:
         inf = EigshInfo(info.cpu().tolist())
         if inf.status & 1:
-            raise RuntimeError("eigsh_smallest_batched: a team barrier timed out on the device")
+            raise RuntimeError(f"{what}: a team barrier timed out on the device")
         res.append((e, v, inf))
     return res
+
+
+def eigsh_smallest_batched(problems, num_desired, inner_iterations, max_restarts, tolerance, *,
+                           c_scale=1.0, precision=64, return_info=False):
+    """eigsh_smallest for many independent problems in as few launches as the
+    kernels allow (up to 48 per launch): ``problems`` is a list of
+    ``(DeviceProblem, adjoint_left_vec, q0)`` on one device.  Returns a list of
+    ``(eigenvalues, eigenvectors)`` (with an EigshInfo each if return_info)."""
+    lib = _lib.load()
+    fn = lib.usbs_eigsh_smallest_batched
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_int, ctypes.POINTER(EigshProblem), ctypes.c_int, ctypes.c_int,
+                   ctypes.c_double, ctypes.c_int, ctypes.c_void_p]
+    arr, keep, out = _eigsh_batch(problems, num_desired, inner_iterations, precision, c_scale)
+    rc = fn(len(problems), arr, inner_iterations, max_restarts, float(tolerance), precision,
+            _stream())
+    _lib.check(rc, "usbs_eigsh_smallest_batched")
+    del keep
+    return _batch_results(out, return_info, "eigsh_smallest_batched")
+
+
+TUNE_CANDIDATES = (64, 128, 256, 640, 1280)
+
+
+def lanczos_autotune(problems, num_desired, inner_iterations, max_restarts, tolerance, *,
+                     c_scale=1.0, precision=32):
+    """Times the cluster-size candidates (rows per CTA) on a batch of at most
+    48 ``(DeviceProblem, adjoint_left_vec, q0)`` and records the fastest for the
+    batch's class (precision, log2 of the count, log2 of the largest n); later
+    Lanczos launches of that class use it.  Returns ``{"rows_per_cta": best,
+    "ms": {candidate: ms or None (same cluster size as the one before)}}``."""
+    lib = _lib.load()
+    fn = lib.usbs_lanczos_autotune
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_int, ctypes.POINTER(EigshProblem), ctypes.c_int, ctypes.c_int,
+                   ctypes.c_double, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_int),
+                   ctypes.POINTER(ctypes.c_float)]
+    arr, keep, _ = _eigsh_batch(problems, num_desired, inner_iterations, precision, c_scale)
+    best = ctypes.c_int(0)
+    ms = (ctypes.c_float * len(TUNE_CANDIDATES))()
+    rc = fn(len(problems), arr, inner_iterations, max_restarts, float(tolerance), precision,
+            _stream(), ctypes.byref(best), ms)
+    _lib.check(rc, "usbs_lanczos_autotune")
+    del keep
+    return {"rows_per_cta": best.value,
+            "ms": {c: (float(m) if m >= 0 else None) for c, m in zip(TUNE_CANDIDATES, ms)}}
+
+
+def lanczos_tuning():
+    """The process's tuned classes: a list of ``{"precision", "log2_count",
+    "log2_max_n", "rows_per_cta"}`` (JSON-serialisable, for set_lanczos_tuning)."""
+    lib = _lib.load()
+    k = lib.usbs_lanczos_tuning_get(None, None, 0)
+    keys = (ctypes.c_longlong * max(k, 1))()
+    rows = (ctypes.c_int * max(k, 1))()
+    k = lib.usbs_lanczos_tuning_get(ctypes.cast(keys, ctypes.c_void_p),
+                                    ctypes.cast(rows, ctypes.c_void_p), k)
+    return [{"precision": int(keys[i] >> 32), "log2_count": int((keys[i] >> 16) & 0xffff),
+             "log2_max_n": int(keys[i] & 0xffff), "rows_per_cta": int(rows[i])}
+            for i in range(k)]
+
+
+def set_lanczos_tuning(entries, clear=False):
+    """Loads entries of lanczos_tuning() (e.g. saved from another process)."""
+    lib = _lib.load()
+    if clear:
+        lib.usbs_lanczos_tuning_clear()
+    for e in entries:
+        rc = lib.usbs_lanczos_tuning_put(int(e["precision"]), 1 << int(e["log2_count"]),
+                                         1 << int(e["log2_max_n"]), int(e["rows_per_cta"]))
+        _lib.check(rc, "usbs_lanczos_tuning_put")

@@ -298,6 +298,79 @@ int usbs_eigsh_smallest_batched(int count, const usbs_eigsh_problem* problems,
   return 0;
 }
 
+int usbs_lanczos_autotune(int count, const usbs_eigsh_problem* problems, int inner_iterations,
+                          int max_restarts, double tolerance, int precision, void* stream,
+                          int* best_rows_per_cta, float* candidate_ms) {
+  if (count < 1 || count > 48 || !problems || !best_rows_per_cta) {
+    set_error("lanczos_autotune: count=%d must be in [1, 48] with problems and an output", count);
+    return -2;
+  }
+  int nmax = 1;
+  for (int i = 0; i < count; ++i) nmax = problems[i].n > nmax ? problems[i].n : nmax;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (cudaEventCreate(&e0) != cudaSuccess || cudaEventCreate(&e1) != cudaSuccess) {
+    if (e0) cudaEventDestroy(e0);
+    set_error("lanczos_autotune: event create failed");
+    return -5;
+  }
+  int best = 0, prev_csize = -1, rc = 0;
+  float best_ms = 0.f;
+  for (int i = 0; lanczos_tune_candidates(i) > 0; ++i) {
+    const int target = lanczos_tune_candidates(i);
+    if (candidate_ms) candidate_ms[i] = -1.f;
+    const int cs = lanczos_cluster_size(nmax, target);
+    if (cs == prev_csize) continue;               // the same launch as the previous candidate
+    prev_csize = cs;
+    lanczos_force_target(target);
+    rc = usbs_eigsh_smallest_batched(count, problems, inner_iterations, max_restarts, tolerance,
+                                     precision, stream);           // warm-up
+    if (!rc && cudaEventRecord(e0, st) != cudaSuccess) rc = -5;
+    if (!rc) rc = usbs_eigsh_smallest_batched(count, problems, inner_iterations, max_restarts,
+                                              tolerance, precision, stream);
+    if (!rc && (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess))
+      rc = -5;
+    lanczos_force_target(0);
+    float ms = 0.f;
+    if (!rc && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) rc = -5;
+    if (rc) break;
+    if (candidate_ms) candidate_ms[i] = ms;
+    if (!best || ms < best_ms) { best = target; best_ms = ms; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (rc) {
+    if (rc == -5) set_error("lanczos_autotune: timing failed");
+    return rc;
+  }
+  lanczos_tune_record(precision, count, nmax, best);
+  *best_rows_per_cta = best;
+  // leave the outputs of the chosen configuration
+  return usbs_eigsh_smallest_batched(count, problems, inner_iterations, max_restarts, tolerance,
+                                     precision, stream);
+}
+
+int usbs_lanczos_tuning_get(long long* keys, int* rows_per_cta, int capacity) {
+  if (capacity < 0 || (capacity > 0 && (!keys || !rows_per_cta))) {
+    set_error("lanczos_tuning_get: bad capacity %d or null arrays", capacity);
+    return -2;
+  }
+  return lanczos_tune_entries(keys, rows_per_cta, capacity);
+}
+
+int usbs_lanczos_tuning_put(int precision, int count, int max_n, int rows_per_cta) {
+  if ((precision != 32 && precision != 64) || count < 1 || max_n < 1 ||
+      (rows_per_cta != 0 && rows_per_cta < 16)) {
+    set_error("lanczos_tuning_put: precision=%d count=%d max_n=%d rows_per_cta=%d", precision,
+              count, max_n, rows_per_cta);
+    return -2;
+  }
+  lanczos_tune_record(precision, count, max_n, rows_per_cta);
+  return 0;
+}
+
+void usbs_lanczos_tuning_clear(void) { lanczos_tune_clear(); }
+
 int usbs_eigsh_smallest_noalloc(int n, long long nnz, const int* rowptr, const int* col,
                                 const double* c_val, double c_scale, const int* slot_ptr,
                                 const int* slot_tid, const int* t_con, const double* t_a,

@@ -34,6 +34,7 @@ struct LanczosProblem {
   int* ctl;             // 16 ints: k_next, nconv, restarts, breakdowns, steps, -, cycle counters
   int* status;
   void* work;           // workspace of lanczos_workspace_bytes()
+  int rows_per_cta = 0; // cluster path: rows per CTA (0: measured class choice or default)
 };
 size_t lanczos_workspace_bytes(int n, int ld, int m, int prec, int nctas);
 int lanczos_team_size(const DeviceInfo& di, int n, int prec);
@@ -46,6 +47,14 @@ int lanczos_kernel_kind(int n, int m, int prec);
 // fit, else one cooperative team each.
 int lanczos_run(const DeviceInfo& di, const LanczosProblem* probs, int count, int prec,
                 cudaStream_t stream);
+// cluster-size policy (rows per CTA by precision, batch and size class) and
+// the autotuner's hooks
+int lanczos_tune_candidates(int i);          // i-th candidate rows per CTA, 0 past the end
+void lanczos_force_target(int target);       // this thread's launches use it (0: policy)
+int lanczos_cluster_size(int nmax, int target);
+void lanczos_tune_record(int prec, int count, int nmax, int target);   // target 0 erases
+int lanczos_tune_entries(long long* keys, int* targets, int cap);
+void lanczos_tune_clear();
 
 // ---------------------------------------------------------------- operators
 // op_val[p] = alpha_c * c_val[p] + sum_{t in slot p} a[t] * w[con[t]]

@@ -20,6 +20,8 @@
 // eigensolver; after a barrier every CTA rotates its rows of Q by the saved
 // Ritz vectors.
 #include <stdlib.h>
+#include <map>
+#include <mutex>
 #include "common.cuh"
 #include "dense.cuh"
 #include "internal.h"
@@ -1722,14 +1724,54 @@ static int run_typed(const DeviceInfo& di, const LanczosProblem* probs, int coun
 // shared memory left for the cluster kernel's dynamic layout
 template <typename VT>
 constexpr size_t cl_budget() { return 227 * 1024 - sizeof(LzShared<VT>) - 1024; }
-// cluster size for n rows: FP64 arithmetic is slow on this part, so FP64
-// problems are spread thinner (128 rows per CTA against 640 for FP32); past
-// 16 CTAs the rows per CTA grow until the shared memory is full
-template <typename VT>
-inline int cl_csize(int n) {
-  const int target = (sizeof(VT) == 8) ? 128 : 640;
+// ---- cluster-size policy and its autotuner ----
+// A launch's cluster size is ceil(n_max / target) CTAs (at most 16), for a
+// target number of rows per CTA.  Each step's phases scale with the rows per
+// CTA and its cluster reductions with the CTAs, and clusters of one launch
+// (or of concurrent solves) compete for the SMs: on GB300 a lone problem runs
+// fastest spread over 16 CTAs (FP32 n = 5000: 4.8 ms at 16 CTAs, 8.7 ms at 8),
+// while 48 problems in one launch run fastest packed at 640 rows per CTA
+// (17 ms against 27 ms spread).  A caller that knows its launch shares the
+// GPU (a solve service) passes its own rows per CTA in the problem; otherwise
+// the class's measured choice is used (usbs_lanczos_autotune times the
+// candidates on a caller's batch and records the fastest for its precision,
+// batch and size class), else 64 rows per CTA for one problem and 640 for a
+// batch.
+constexpr int TUNE_NCAND = 5;
+constexpr int TUNE_CAND[TUNE_NCAND] = {64, 128, 256, 640, 1280};
+static std::mutex g_tune_mu;
+static std::map<long long, int> g_tune;            // class key -> rows per CTA
+static thread_local int t_forced_target = 0;       // set by the tuner while it measures
+
+static int log2_bucket(long long v) {
+  int b = 0;
+  while (v > 1) { v >>= 1; ++b; }
+  return b;
+}
+// class key: precision << 32 | floor(log2(problems)) << 16 | floor(log2(largest n))
+static long long tune_key(int prec, int count, int nmax) {
+  return ((long long)prec << 32) | ((long long)log2_bucket(count < 1 ? 1 : count) << 16) |
+         log2_bucket(nmax);
+}
+static int cl_target(int prec, int count, int nmax, int requested) {
+  if (t_forced_target) return t_forced_target;
+  if (requested > 0) return requested;
+  if (const char* e = getenv(prec == 64 ? "USBS_CL_TARGET64" : "USBS_CL_TARGET32"))
+    if (atoi(e) >= 32) return atoi(e);
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune.find(tune_key(prec, count, nmax));
+    if (it != g_tune.end()) return it->second;
+  }
+  return count <= 1 ? 64 : 640;
+}
+static int cl_csize_for(int n, int target) {
   const int c = (n + target - 1) / target;
   return c < 1 ? 1 : (c > CL_MAX_CTAS ? CL_MAX_CTAS : c);
+}
+template <typename VT>
+inline int cl_csize(int n) {
+  return cl_csize_for(n, cl_target(sizeof(VT) == 8 ? 64 : 32, 1, n, 0));
 }
 template <typename VT>
 static bool cl_fits(int n, int m) {
@@ -1759,11 +1801,12 @@ static int run_cluster(const LanczosProblem* probs, int count, cudaStream_t stre
   }();
   if (!enabled || count < 1 || count > MAX_TEAMS) return 1;
   constexpr size_t BUDGET = cl_budget<VT>();
-  int csize = 1;
+  int nmax = 1, req = 0;
   for (int i = 0; i < count; ++i) {
-    const int c = cl_csize<VT>(probs[i].n);
-    csize = c > csize ? c : csize;
+    nmax = probs[i].n > nmax ? probs[i].n : nmax;
+    req = probs[i].rows_per_cta > req ? probs[i].rows_per_cta : req;
   }
+  const int csize = cl_csize_for(nmax, cl_target(sizeof(VT) == 8 ? 64 : 32, count, nmax, req));
   if (csize > CL_MAX_CTAS) return 1;
   ClusterBatch<VT> batch;
   batch.count = count;
@@ -1845,6 +1888,34 @@ int lanczos_run(const DeviceInfo& di, const LanczosProblem* probs, int count, in
   }
   set_error("lanczos: precision must be 32 or 64");
   return -2;
+}
+
+int lanczos_tune_candidates(int i) { return (i >= 0 && i < TUNE_NCAND) ? TUNE_CAND[i] : 0; }
+
+void lanczos_force_target(int target) { t_forced_target = target; }
+
+// cluster size a launch of `count` problems of at most nmax rows gets with `target`
+int lanczos_cluster_size(int nmax, int target) { return cl_csize_for(nmax, target); }
+
+void lanczos_tune_record(int prec, int count, int nmax, int target) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  if (target > 0) g_tune[tune_key(prec, count, nmax)] = target;
+  else g_tune.erase(tune_key(prec, count, nmax));
+}
+
+int lanczos_tune_entries(long long* keys, int* targets, int cap) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  int i = 0;
+  for (const auto& kv : g_tune) {
+    if (i < cap) { keys[i] = kv.first; targets[i] = kv.second; }
+    ++i;
+  }
+  return i;
+}
+
+void lanczos_tune_clear() {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  g_tune.clear();
 }
 
 int lanczos_occupancy(int prec) {

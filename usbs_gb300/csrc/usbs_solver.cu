@@ -864,6 +864,7 @@ struct Solver {
     lp.rowptr = P->rowptr; lp.col = P->col; lp.val = L.opL; lp.Q = L.Q;
     lp.alpha = L.alpha; lp.beta = L.beta; lp.ctl = L.ctl; lp.status = L.status;
     lp.work = L.lz_work;
+    lp.rows_per_cta = Pa->lanczos_rows_per_cta;
     ++launches;
     return lanczos_run(di, &lp, 1, Pa->precision, st);
   }
@@ -1359,6 +1360,10 @@ int usbs_solve(const usbs_problem* P, const usbs_params* Pa, usbs_state* S, void
     return -2;
   }
   if (Pa->precision != 64 && Pa->precision != 32) { set_error("precision must be 32 or 64"); return -2; }
+  if (Pa->lanczos_rows_per_cta != 0 && Pa->lanczos_rows_per_cta < 16) {
+    set_error("usbs_solve: lanczos_rows_per_cta must be 0 or >= 16");
+    return -2;
+  }
   if (Pa->sketch_mode == 0 && (Pa->sketch_dim < 1 || Pa->sketch_dim > 64 || !S->Omega || !S->P)) {
     set_error("usbs_solve: sketch mode needs 1 <= sketch_dim <= 64, P and Omega");
     return -2;

@@ -119,12 +119,16 @@ def footprint_bytes(host_layout, k, sketch_dim, params_struct, lib):
 
 
 class SolverService:
-    """``submit()`` requests; ``max_slots`` solves run at once."""
+    """``submit()`` requests; ``max_slots`` solves run at once.
+    ``lanczos_rows_per_cta``: the cluster Lanczos packing of requests that do
+    not set their own (0: the library's single-solve choice)."""
 
-    def __init__(self, device="cuda", max_slots=8, reserve_bytes=2 << 30, mem_info=None):
+    def __init__(self, device="cuda", max_slots=8, reserve_bytes=2 << 30, mem_info=None,
+                 lanczos_rows_per_cta=0):
         import torch
         self.device = torch.device(device)
         self.max_slots = int(max_slots)
+        self.rows_per_cta = int(lanczos_rows_per_cta)
         self.reserve = int(reserve_bytes)
         mem_info = mem_info or (lambda: torch.cuda.mem_get_info(self.device))
         free, _total = mem_info()
@@ -206,9 +210,12 @@ class SolverService:
                 with torch.cuda.stream(stream):
                     inst = solver.DeviceInstance(req.sdp_state, self.device,
                                                  host_layout=req._host_layout)
+                    kw = dict(req.kwargs)
+                    if self.rows_per_cta:
+                        kw.setdefault("lanczos_rows_per_cta", self.rows_per_cta)
                     out, info = solver.usbs(req.sdp_state, precision=req.precision,
                                             device=self.device, return_info=True,
-                                            instance=inst, stream=stream, **req.kwargs)
+                                            instance=inst, stream=stream, **kw)
                     stream.synchronize()
                     del inst
                 req.result, req.info = out, info
