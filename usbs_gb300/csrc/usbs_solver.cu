@@ -101,6 +101,84 @@ __global__ void __launch_bounds__(RED_BLOCK) gram_kernel(GramArgs a) {
   if (tid == 0) *a.counter = 0u;
 }
 
+// Symmetric case G = X^T X of a wide X (create_Q_base): the same per-block
+// tiles and accumulation order as gram_kernel, for the upper triangle only
+// (x_p x_q and x_q x_p round alike, so the lower triangle is its mirror), and
+// the partials are summed by gram_sym_reduce_kernel, one thread per entry,
+// instead of by one block reading every partial: the same products summed
+// in the same order as gram_kernel's.
+__device__ __forceinline__ void tri_coords(int t, int k, int& p, int& q) {
+  p = 0;
+  while (t >= k - p) { t -= k - p; ++p; }
+  q = p + t;
+}
+
+template <int EPT>
+__global__ void __launch_bounds__(RED_BLOCK) gram_sym_kernel(GramArgs a) {
+  if (a.skip && *a.skip) return;
+  __shared__ double xs[GR_ROWS][GR_MAXC + 1];
+  const int k = a.kx, ET = k * (k + 1) / 2, tid = threadIdx.x;
+  double acc[EPT];
+  int pj[EPT], qj[EPT];
+#pragma unroll
+  for (int j = 0; j < EPT; ++j) {
+    acc[j] = 0.0;
+    const int t = tid + j * RED_BLOCK;
+    pj[j] = qj[j] = 0;
+    if (t < ET) tri_coords(t, k, pj[j], qj[j]);
+  }
+  const int ntiles = (a.n + GR_ROWS - 1) / GR_ROWS;
+  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int r0 = tile * GR_ROWS;
+    for (int e = tid; e < GR_ROWS * k; e += RED_BLOCK) {
+      const int c = e / GR_ROWS, r = e - c * GR_ROWS;
+      xs[r][c] = (r0 + r < a.n) ? a.X[(size_t)c * a.ldx + r0 + r] : 0.0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int j = 0; j < EPT; ++j) {
+      if (tid + j * RED_BLOCK < ET) {
+        const int p = pj[j], q = qj[j];
+        double s = acc[j];
+#pragma unroll
+        for (int r = 0; r < GR_ROWS; ++r) s += xs[r][p] * xs[r][q];
+        acc[j] = s;
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int j = 0; j < EPT; ++j) {
+    const int t = tid + j * RED_BLOCK;
+    if (t < ET) a.partial[(size_t)blockIdx.x * ET + t] = acc[j];
+  }
+}
+
+// Sums nb blocks' partials of the k(k+1)/2 upper-triangle entries in
+// gram_kernel's order (four interleaved chains over the blocks) and writes
+// both triangles of the k x k result.
+__global__ void gram_sym_reduce_kernel(const double* __restrict__ partial, int nb, int k,
+                                       double* __restrict__ out, const int* skip) {
+  if (skip && *skip) return;
+  const int ET = k * (k + 1) / 2;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ET) return;
+  double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  int b = 0;
+  for (; b + 3 < nb; b += 4) {
+    s0 += partial[(size_t)b * ET + t];
+    s1 += partial[(size_t)(b + 1) * ET + t];
+    s2 += partial[(size_t)(b + 2) * ET + t];
+    s3 += partial[(size_t)(b + 3) * ET + t];
+  }
+  for (; b < nb; ++b) s0 += partial[(size_t)b * ET + t];
+  const double v = (s0 + s1) + (s2 + s3);
+  int p, q;
+  tri_coords(t, k, p, q);
+  out[p * k + q] = v;
+  out[q * k + p] = v;
+}
+
 // ---------------------------------------------------------------- SpMM
 
 // Y[:, q] = M X[:, q] for q < k, CSR M with double values, L lanes per row.
@@ -779,6 +857,14 @@ struct Solver {
     if (blocks > tiles) blocks = tiles;
     if (blocks > L.grid_gram) blocks = L.grid_gram;
     if (blocks < 1) blocks = 1;
+    if (X == Y && kx == ky && ldx == ldy && kx * ky > 4 * RED_BLOCK) {
+      constexpr int EPT_T = (IPM_MAXS * (IPM_MAXS + 1) / 2 + RED_BLOCK - 1) / RED_BLOCK;
+      gram_sym_kernel<EPT_T><<<blocks, RED_BLOCK, 0, st>>>(a);
+      ++launches;
+      const int et = kx * (kx + 1) / 2;
+      gram_sym_reduce_kernel<<<(et + 127) / 128, 128, 0, st>>>(a.partial, blocks, kx, out, nullptr);
+      return kerr("gram");
+    }
     if (kx * ky <= RED_BLOCK) gram_kernel<1><<<blocks, RED_BLOCK, 0, st>>>(a);
     else if (kx * ky <= 4 * RED_BLOCK) gram_kernel<4><<<blocks, RED_BLOCK, 0, st>>>(a);
     else gram_kernel<(IPM_MAXS * IPM_MAXS + RED_BLOCK - 1) / RED_BLOCK><<<blocks, RED_BLOCK, 0, st>>>(a);
