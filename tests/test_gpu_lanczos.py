@@ -270,27 +270,35 @@ def _maxcut_case(cuda, Wg, seed):
 # Many independent instances in one launch: six small graphs run as clusters
 # of one launch; with a 22,500-node graph in the batch every problem runs on
 # the cooperative team kernel, one team per problem
-@pytest.mark.parametrize("with_large", [False, True])
-def test_eigsh_batched_matches_oracle(cuda, with_large):
+@pytest.mark.parametrize("with_large,precision", [(False, 64), (True, 64), (False, 32),
+                                                   (True, 32)])
+def test_eigsh_batched_matches_oracle(cuda, with_large, precision):
     from usbs_gb300 import api
     graphs = [wl.er_graph(300 + 100 * i, 2000 + 900 * i, 10 + i) for i in range(6)]
     if with_large:
         graphs.insert(2, wl.er_graph(22500, 90000, 150))
     cases = [_maxcut_case(cuda, g, 20 + i) for i, g in enumerate(graphs)]
-    nd, restarts, tol = 4, 200, 1e-9
+    nd, restarts = 4, 200
+    tol = 1e-9 if precision == 64 else 1e-5
     out = api.eigsh_smallest_batched([(p, y, q0) for _, p, y, q0 in cases], nd, 32, restarts, tol,
-                                     c_scale=-1.0, precision=64, return_info=True)
+                                     c_scale=-1.0, precision=precision, return_info=True)
     assert len(out) == len(cases)
     for (st, p, y, q0), (gv, gV, info) in zip(cases, out):
         n = p.n
         ov, oV, ost = olz.eigsh_smallest(n, (-st.C).tocsr(), st.A_data, st.A_indices, y, q0, nd,
                                          32, restarts, tol)
-        gv, gV = _np(gv), _np(gV)
+        gv, gV = _np(gv), _np(gV).astype(np.float64)
         assert info.status == 0 and ost["nconv"] >= nd
         scale = np.abs(ov).max()
-        np.testing.assert_allclose(gv, ov, rtol=1e-9, atol=1e-9 * scale)
-        for j in range(nd):
-            assert abs(gV[:, j] @ oV[:, j]) > 1 - 1e-10, (n, j)
+        if precision == 64:
+            np.testing.assert_allclose(gv, ov, rtol=1e-9, atol=1e-9 * scale)
+            for j in range(nd):
+                assert abs(gV[:, j] @ oV[:, j]) > 1 - 1e-10, (n, j)
+        else:
+            assert np.abs(gv - ov).max() < 1e-4 * scale, n
+            Op = ((-st.C) + sp.diags(y)).tocsr()
+            r = np.linalg.norm(Op @ gV - gV * gv[None, :], axis=0)
+            assert r.max() < 1e-2 * scale, n
 
 
 def test_eigsh_batched_many_matches_single_calls(cuda):
