@@ -84,19 +84,21 @@ __device__ __forceinline__ double symkron_sum(const double* T, const double* X, 
 // without pivoting: PD iff every pivot is positive (equivalent to Cholesky
 // succeeding, i.e. to the smallest eigenvalue being > 0, up to round-off at the
 // boundary).  One reciprocal per column, no square roots.
+// L holds the unit lower factor l_ip and U the unscaled l_ip d_p (packed lower
+// triangles), so each update term l_ip (l_jp d_p) is one FMA.
 __device__ __forceinline__ bool pd_test(const double* A, const double* dA, double s, int k) {
-  double L[IPM_MAXS];   // packed lower triangle, unit diagonal implied; L[jj] holds d_j
+  double L[IPM_MAXS], U[IPM_MAXS];
   for (int j = 0; j < k; ++j) {
     const int rj = j * (j + 1) / 2;
     double d = A[j * k + j] + s * dA[j * k + j];
-    for (int p = 0; p < j; ++p) d -= L[rj + p] * L[rj + p] * L[p * (p + 1) / 2 + p];
+    for (int p = 0; p < j; ++p) d -= L[rj + p] * U[rj + p];
     if (!(d > 0.0)) return false;
-    L[rj + j] = d;
     const double inv = 1.0 / d;
     for (int i = j + 1; i < k; ++i) {
       const int ri = i * (i + 1) / 2;
       double v = A[i * k + j] + s * dA[i * k + j];
-      for (int p = 0; p < j; ++p) v -= L[ri + p] * L[rj + p] * L[p * (p + 1) / 2 + p];
+      for (int p = 0; p < j; ++p) v -= L[ri + p] * U[rj + p];
+      U[ri + j] = v;
       L[ri + j] = v * inv;
     }
   }
