@@ -186,3 +186,26 @@ def test_compute_max_cut_known_answers():
     Om = np.random.default_rng(1).standard_normal((n, 6))
     assert omaxcut.compute_max_cut(np.outer(v, v @ Om), Om, None, C) == W.nnz / 2
     assert omaxcut.compute_max_cut(np.zeros((n, 6)), Om, None, C) == 0.0
+
+
+def test_usbs_invariants_along_the_trace():
+    """Invariants of the iteration (the reference's definitions): tr X stays
+    within trace_ub, the best dual bound only decreases and stays above the
+    primal value of the nearly feasible X, and diag X moves to 1 (max_infeas
+    falls) as the gap closes.  At these settings 200 iterations reach a gap of
+    about 5e-2."""
+    from usbs_gb300 import workloads as wl
+    n = 40
+    st = omaxcut.initialize_state(wl.er_graph(n, 300, 3), 4)
+    tr = []
+    out, fin = ousbs.usbs(st, n, n, 2.0 * n, 2.0, 0.01, 0.25, 4, 1, 200, np.inf, 1e-5, 1e-5,
+                          1e-5, 32, 50, 1e-9, 100, trace=tr)
+    assert len(tr) > 2
+    for r in tr:
+        assert r["tr_X"] <= 2.0 * n * (1 + 1e-9)
+    ubs = [r["obj_ub"] for r in tr]
+    assert all(b <= a + 1e-12 * abs(a) for a, b in zip(ubs, ubs[1:]))     # best bound so far
+    last = tr[-1]
+    assert last["max_infeas"] < 0.05 and last["max_infeas"] < tr[0]["max_infeas"] / 10
+    assert last["obj_ub"] >= last["primal_obj"]
+    assert last["obj_gap"] < 0.1 < tr[0]["obj_gap"]
