@@ -596,6 +596,9 @@ def main():
                          Omega=torch.as_tensor(st.Omega, device=device))
     q0_dev = torch.as_tensor(q0, device=device)
     it_step = args.iters_per_step
+    # L2 flush before every timed step: a 256 MB write (the L2 holds 129 MB),
+    # on the solver's stream, inside the timed region (about 40 us a step)
+    l2_flush = torch.empty(256 * 2 ** 20, dtype=torch.uint8, device=device)
     for _ in range(args.warmup):
         run_usbs(st_dev, n, it_step, inst, device, q0=q0_dev)
     torch.cuda.synchronize()
@@ -607,6 +610,7 @@ def main():
         e0.record()
         t0 = time.perf_counter()
         for _ in range(args.steps):
+            l2_flush.zero_()
             out, info = run_usbs(st_dev, n, it_step, inst, device, q0=q0_dev)
             infos.append(info)
         e1.record()
@@ -650,6 +654,7 @@ def main():
     e2.record()
     e2e_iters = 0
     for _ in range(args.steps):
+        l2_flush.zero_()
         inst_e = solver.DeviceInstance.__new__(solver.DeviceInstance)
         inst_e.__dict__.update(inst.__dict__)
         prob = DeviceProblem.__new__(DeviceProblem)
@@ -715,7 +720,8 @@ def main():
             "config": {"workload": "maxcut torus 100x100 +-1 (n=10000, nnz=50000), "
                                    "mixed precision, reference settings",
                        "iters_per_step": it_step, "settings": S, "parallelism": "replicas",
-                       "l2": "working set ~3 MB stays in the 129 MB L2 (no flush)"},
+                       "l2": "flushed before every timed step (256 MB write); the ~3 MB "
+                             "working set is reloaded within the step"},
             "roofline": {"kernel": lz_kernel, "bound": "hbm",
                          "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "peak_kind": peak_kind,
