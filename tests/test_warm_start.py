@@ -161,3 +161,4 @@ def test_qap_explicit_warm_start_sketch_matches_oracle(cuda):
     old, D, W = _qap_solved(4, 6, 6)
     _same_qap(pqap.explicit_warm_start(old, D, W, 6),
               oqap.get_explicit_warm_start_state(old, D, W, 6), rtol=1e-8)
+
