@@ -209,3 +209,46 @@ def test_usbs_invariants_along_the_trace():
     assert last["max_infeas"] < 0.05 and last["max_infeas"] < tr[0]["max_infeas"] / 10
     assert last["obj_ub"] >= last["primal_obj"]
     assert last["obj_gap"] < 0.1 < tr[0]["obj_gap"]
+
+
+def _golden():
+    import json
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "known_answers.json")
+    with open(path) as f:
+        return json.load(f)
+
+
+def test_golden_laplacian_spectra():
+    """tests/golden/known_answers.json (closed forms): the oracle's eigsh on the
+    path and cycle Laplacians.  A single-vector Krylov method sees a double
+    eigenvalue once in exact arithmetic, so for the cycle the third returned
+    value is either the second copy of lambda_1 or lambda_3."""
+    g = _golden()
+    A_idx = np.zeros((0, 3), dtype=np.int64)
+    n = g["path_laplacian"]["n"]
+    want = np.array(g["path_laplacian"]["smallest"])
+    vals, _, _ = lanczos.eigsh_smallest(n, _path_laplacian(n), np.zeros(0), A_idx, np.zeros(1),
+                                        rng.default_q0(n), len(want), 32, 300, 1e-11)
+    np.testing.assert_allclose(vals, want, atol=1e-8)
+    n = g["cycle_laplacian"]["n"]
+    lam = g["cycle_laplacian"]["smallest"]
+    W = sp.diags([np.ones(n - 1), np.ones(n - 1)], [-1, 1]).tolil()
+    W[0, n - 1] = W[n - 1, 0] = 1.0
+    W = W.tocsr()
+    L = (sp.diags(np.asarray(W.sum(1)).ravel()) - W).tocsr()
+    vals, _, _ = lanczos.eigsh_smallest(n, L, np.zeros(0), A_idx, np.zeros(1), rng.default_q0(n),
+                                        3, 32, 300, 1e-11)
+    assert abs(vals[0] - lam[0]) < 1e-8 and abs(vals[1] - lam[1]) < 1e-8
+    assert min(abs(vals[2] - lam[2]), abs(vals[2] - lam[3])) < 1e-8
+
+
+def test_golden_maxcut_sdp_even_torus():
+    """The MaxCut SDP value of the bipartite 6 x 6 torus is |E| = 72."""
+    from usbs_gb300 import workloads as wl
+    g = _golden()["maxcut_sdp_even_torus"]
+    n = g["n"]
+    st = omaxcut.initialize_state(wl.torus_graph(g["side"], 0, weights="unit"), 4)
+    out, fin = ousbs.usbs(st, n, n, 2.0 * n, 2.0, 0.01, 0.25, 3, 1, 300, np.inf, 1e-6, 1e-6,
+                          1e-6, min(n, 32), 10, 1e-7, 100)
+    assert abs(out.primal_obj - g["value"]) / g["value"] < 2e-3
