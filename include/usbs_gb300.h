@@ -95,10 +95,15 @@ int usbs_apply_A_adjoint(int n, int k, const int* row_ptr, const int* r_con, con
                          const double* r_a, const double* z, const double* U, int ldu,
                          double* out, int ldo, void* stream);
 
-/* Which Lanczos kernel usbs_eigsh_smallest launches for n rows (host call):
- * 1 = one thread-block cluster with the basis in shared memory, 0 = a
- * cooperative team streaming the basis through L2/HBM; negative on error.
- * No counterpart in the reference. */
+/* Which Lanczos path usbs_eigsh_smallest takes for n rows (host call):
+ *   1 = one thread-block cluster with the basis in shared memory;
+ *   0 = one cooperative launch (a team of CTAs, x staged in shared memory,
+ *       n * sizeof(value) <= 160 KB); it needs the whole GPU co-resident;
+ *   2 = the stream path (larger n): every Lanczos phase is an ordinary
+ *       full-GPU launch, and the loop state is read back once per restart,
+ *       so such a call synchronises `stream` at each restart and cannot be
+ *       captured into a CUDA graph;
+ * negative on error.  No counterpart in the reference. */
 int usbs_lanczos_kernel(int n, int inner_iterations, int precision);
 
 /* Workspace bytes needed by usbs_eigsh_smallest (host call, no GPU work). */
@@ -115,15 +120,18 @@ size_t usbs_eigsh_workspace_bytes(int n, long long nnz, int inner_iterations, in
  *   eigenvalues: num_desired doubles (ascending);
  *   info: 16 ints: [0] saved vectors of the last restart, [1] converged count,
  *         [2] restarts run, [3] breakdown restarts, [4] operator applications,
- *         [5] status bits (1 barrier timeout, 8 projected eigensolver failure),
+ *         [5] status bits (1 barrier timeout, 2 non-finite projected matrix:
+ *             the call ends at that restart, 8 projected eigensolver failure),
  *         [6] kilo-cycles in the restarts, [7] kilo-cycles in total,
  *         [8..12] kilo-cycles of CTA 0 in barrier waits, team reductions and
  *         the three step phases, [13] sum over steps of the active basis
  *         columns, [14] sum over restarts of the saved vectors (for byte counts),
  *         [15] kilo-cycles of CTA 0 in the projected eigensolver.
- * Runs as one kernel launch: one thread-block cluster when the problem's rows
- * fit in the cluster's shared memory, else a cooperative team of CTAs.  The
- * call is asynchronous. */
+ * Runs as one kernel launch when the problem's rows fit in a thread-block
+ * cluster's shared memory or its x in one CTA's (usbs_lanczos_kernel 1 or 0);
+ * the call is then asynchronous.  Larger problems take the stream path
+ * (usbs_lanczos_kernel 2): a sequence of launches, with `stream`
+ * synchronised once per restart.  Kilo-cycle counters [7..12] stay 0 there. */
 int usbs_eigsh_smallest(int n, long long nnz, const int* rowptr, const int* col,
                         const double* c_val, double c_scale, const int* slot_ptr, const int* slot_tid,
                         const int* t_con, const double* t_a, const double* adjoint_left_vec,
@@ -145,8 +153,9 @@ int usbs_eigsh_smallest(int n, long long nnz, const int* rowptr, const int* col,
  *    that first call before any stream capture on the device.
  *  - Problems whose usbs_eigsh_workspace_bytes() exceeds
  *    USBS_EIGSH_STATIC_SCRATCH_BYTES are rejected (-2, usbs_last_error()).
- *    With the usual 32 inner iterations that is about nnz + 2*n above
- *    2.0e6 (FP64) or 4.0e6 (FP32).
+ *    The scratch holds the assembled operator (nnz values), three n-vectors
+ *    and at most 0.5 MB of partial sums, so with 32 inner iterations problems
+ *    up to about nnz + 3n = 2.0e6 (FP64) or 4.0e6 (FP32) fit.
  *  - The scratch need not start at zero: each call clears its barrier
  *    counters, info words and Lanczos coefficients on `stream` before use.
  *  - One scratch per device: calls whose work may overlap in time on the
@@ -400,6 +409,19 @@ size_t usbs_qap_round_workspace_bytes(int l, int s);
 int usbs_qap_round(int l, int s, const double* Omega, const double* P, int ld, const double* W,
                    const double* D, double approx_eps, double* value, double* candidate_values,
                    int* candidate_perms, void* workspace, size_t workspace_bytes, void* stream);
+
+/* Self-test of the bounded device waits (no counterpart in the reference,
+ * which has no device code).  Every spin-wait of the library's kernels gives
+ * up after a time limit, ORs ST_BARRIER_TIMEOUT (1) into the caller's status
+ * word and returns.  This call runs one such wait on a condition nothing
+ * satisfies, for `limit_ns` (1 us .. 2 s):
+ *   which 0: the cooperative team barrier, `nctas` (1..8) CTAs launched and
+ *            nctas + 1 expected; `counters` = 2 device uints (cleared here);
+ *   which 1: an mbarrier wait that no thread or copy completes (counters
+ *            unused).
+ * *status (device int) gains bit 1 once the launch ends.  Stream-ordered. */
+int usbs_selftest_wait_limits(int which, int nctas, long long limit_ns, unsigned int* counters,
+                              int* status, void* stream);
 
 #ifdef __cplusplus
 }

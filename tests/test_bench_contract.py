@@ -11,7 +11,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 def test_reference_arm_prints_one_contract_line():
     r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--steps", "1",
-                        "--warmup", "0", "--cpu-iters", "4"], cwd=ROOT, capture_output=True,
+                        "--warmup", "0", "--iters-per-step", "2"], cwd=ROOT, capture_output=True,
                        text=True, timeout=600)
     assert r.returncode == 0, r.stderr[-2000:]
     lines = [ln for ln in r.stdout.splitlines() if ln.strip()]
@@ -28,3 +28,10 @@ def test_reference_arm_prints_one_contract_line():
     e2e = d["e2e"]
     assert e2e["value"] == d["value"] and e2e["unit"] == d["unit"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
+    # the same workload description as the device arm's line
+    sys.path.insert(0, ROOT)
+    import bench
+    assert d["config"] == json.loads(json.dumps(bench.main_config(2)))
+    # the oracle's solve rates on the recorded solves' instances
+    for name, r in d["solves"]["oracle"].items():
+        assert r["solves_per_s"] > 0 and r["iterations_to_eps"] > 0, name

@@ -224,17 +224,17 @@ def test_sell_apply_matches_csr(cuda, shape, precision):
     assert np.all(np.abs(y.double().cpu().numpy() - ref) <= tol * scale)
 
 
-# The cooperative team kernel (problems too large for one cluster): unstaged
-# (x in shared memory, n = 15,625 in FP64) and staged (Q tiles streamed by bulk
-# copies, n > 20,480 in FP64 / 40,960 in FP32)
-@pytest.mark.parametrize("side,precision", [(125, 64), (150, 64), (210, 32)])
-def test_eigsh_team_kernel_matches_oracle(cuda, side, precision):
+# Problems too large for one cluster: the cooperative team kernel while x fits
+# in shared memory (n = 15,625 in FP64), the stream path past that (a
+# sequence of full-GPU launches; n > 20,480 in FP64, 40,960 in FP32)
+@pytest.mark.parametrize("side,precision,kind", [(125, 64, 0), (150, 64, 2), (210, 32, 2)])
+def test_eigsh_team_and_stream_paths_match_oracle(cuda, side, precision, kind):
     from usbs_gb300 import _lib, api
     from usbs_gb300.problem import DeviceProblem, layout
     Wg = wl.er_graph(side * side, 4 * side * side, side)
     st = omaxcut.initialize_state(Wg, 4)
     n = st.C.shape[0]
-    assert _lib.load().usbs_lanczos_kernel(n, 32, precision) == 0     # team kernel
+    assert _lib.load().usbs_lanczos_kernel(n, 32, precision) == kind
     prob = DeviceProblem(layout(st.C, st.A_data, st.A_indices, m=n), cuda)
     y = np.random.default_rng(3).standard_normal(n) * 0.5
     q0 = orng.default_q0(n)
@@ -248,6 +248,7 @@ def test_eigsh_team_kernel_matches_oracle(cuda, side, precision):
     scale = np.abs(ov).max()
     if precision == 64:
         assert ost["nconv"] >= nd
+        assert info.restarts == ost["restart"] and info.num_converged == ost["nconv"]
         np.testing.assert_allclose(gv, ov, rtol=1e-9, atol=1e-9 * scale)
         for j in range(nd):
             assert abs(gV[:, j] @ oV[:, j]) > 1 - 1e-10, j
@@ -352,3 +353,29 @@ def test_lanczos_autotune_records_a_choice_and_keeps_parity(cuda):
                             lanczos_rows_per_cta=640)
     for key in ("primal_obj", "obj_ub", "pen_dual_obj", "tr_X"):
         assert abs(atr[0][key] - btr[0][key]) <= 1e-9 * max(1.0, abs(atr[0][key])), key
+
+
+# The stream path's breakdown branch: on the zero operator every Lanczos step
+# breaks down (y = 0), and each step's vector is replaced by a Gaussian vector
+# keyed by the step, orthogonalised twice against the basis
+# (solver/lanczos.py:107-117).  The oracle draws the same vectors.
+@pytest.mark.parametrize("precision", [64, 32])
+def test_stream_path_breakdown_on_zero_operator(cuda, precision):
+    from usbs_gb300 import _lib, api
+    from usbs_gb300.problem import DeviceProblem, layout
+    n = 50000
+    C = sp.csr_matrix((n, n))
+    A_idx = np.stack([np.arange(n)] * 3, 1)
+    assert _lib.load().usbs_lanczos_kernel(n, 32, precision) == 2
+    prob = DeviceProblem(layout(C, np.ones(n), A_idx, m=n), cuda)
+    y = np.zeros(n)
+    q0 = orng.default_q0(n)
+    ov, oV, ost = olz.eigsh_smallest(n, C, np.ones(n), A_idx, y, q0, 4, 32, 3, 1e-7)
+    gv, gV, info = api.eigsh_smallest(n, prob, None, None, y, q0, 4, 32, 3, 1e-7, c_scale=-1.0,
+                                      precision=precision, return_info=True)
+    gv, gV = _np(gv), _np(gV).astype(np.float64)
+    assert info.status == 0 and info.breakdowns > 0
+    assert info.restarts == ost["restart"] and info.num_converged == ost["nconv"]
+    assert np.abs(gv).max() < 1e-12 and np.abs(ov).max() < 1e-12
+    G = gV.T @ gV
+    assert np.abs(G - np.eye(4)).max() < (1e-12 if precision == 64 else 1e-5)

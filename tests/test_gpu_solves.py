@@ -1,0 +1,70 @@
+"""Whole solves on the device against full FP64 oracle solves.
+
+Each instance of tests/golden/oracle_solves.json is solved from the cold
+start until the reference's stop test fires (obj_gap, infeas_gap and
+max_infeas all <= eps; solver/usbs.py:533-540), in FP64 and in mixed
+precision (FP32 Lanczos, FP64 subproblems).  The trajectories of two
+implementations part at round-off level and the bundle iteration amplifies
+that, so the iterates are not compared step by step here; the solutions
+are: both stop, and their primal and dual objectives agree with the oracle's
+final values within the stop tolerance.  The 6 x 6 unit torus also has a
+closed-form SDP value, |E| = 72."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from usbs_gb300 import workloads as wl
+
+pytestmark = pytest.mark.gpu
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "oracle_solves.json")
+with open(GOLDEN) as _f:
+    G = json.load(_f)
+
+
+def _solve(rec, precision):
+    from usbs_gb300 import solver
+    from usbs_gb300.problems import maxcut
+    S = G["settings"]
+    st = maxcut.initialize_state(wl.graph_from_spec(rec["graph"]), S["sketch_dim"])
+    n = st.C.shape[0]
+    eps = rec["eps"]
+    out, tr, info = solver.usbs(st, n, n, S["trace_factor"] * n, S["trace_factor"], S["rho"],
+                                S["beta"], S["k_curr"], S["k_past"], rec["max_iters"], np.inf, eps,
+                                eps, eps, min(n, 32), S["lanczos_max_restarts"], S["subprob_eps"],
+                                S["subprob_max_iters"], precision=precision, return_trace=True)
+    dual = float(np.asarray(st.b) @ out.y.cpu().numpy())
+    return out, tr[-1], info, dual
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+@pytest.mark.parametrize("name", ["er60_1e-4", "torus6_1e-4"])
+def test_solve_to_1e4_matches_oracle_solution(cuda, name, precision):
+    rec = G["solves"][name]
+    eps = rec["eps"]
+    out, last, info, dual = _solve(rec, precision)
+    assert info["status"] == 0
+    # the stop test fired, within the iteration budget
+    assert info["iterations"] < rec["max_iters"]
+    assert last["obj_gap"] <= eps and last["infeas_gap"] <= eps and last["max_infeas"] <= eps
+    # the solution: objectives within the stop tolerance of the FP64 oracle's
+    # (each is within eps of the optimum, so they are within 2 eps of each other)
+    assert abs(out.primal_obj - rec["primal_obj"]) <= 2 * eps * abs(rec["primal_obj"])
+    assert abs(dual - rec["dual_obj"]) <= 2 * eps * abs(rec["dual_obj"])
+    # and the iteration count is that of the same algorithm
+    assert abs(info["iterations"] - rec["iterations"]) <= 0.25 * rec["iterations"]
+    if name.startswith("torus6"):
+        assert abs(out.primal_obj - 72.0) <= 2 * eps * 72.0
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+def test_er800_to_1e2_matches_oracle_solution(cuda, precision):
+    rec = G["solves"]["er800_1e-2"]
+    eps = rec["eps"]
+    out, last, info, dual = _solve(rec, precision)
+    assert info["status"] == 0 and info["iterations"] < rec["max_iters"]
+    assert last["obj_gap"] <= eps and last["infeas_gap"] <= eps and last["max_infeas"] <= eps
+    assert abs(out.primal_obj - rec["primal_obj"]) <= 2 * eps * abs(rec["primal_obj"])
+    assert abs(info["iterations"] - rec["iterations"]) <= 0.25 * rec["iterations"]

@@ -32,3 +32,8 @@ def test_exclusive_request_waits_for_drain_and_holds_the_line():
     assert adm.pick([(5, False)]) is None      # nothing runs beside an exclusive solve
     adm.finish(100, True)
     assert adm.pick([(5, False)]) == 0
+
+
+def test_request_larger_than_the_budget_never_fits():
+    adm = Admission(budget_bytes=100, max_slots=2)
+    assert adm.ever_fits(100) and not adm.ever_fits(101)

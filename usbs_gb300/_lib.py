@@ -52,6 +52,7 @@ SIGNATURES = {
     "usbs_qap_round_workspace_bytes": (c_size_t, [c_int, c_int]),
     "usbs_qap_round": (c_int, [c_int, c_int, P, P, c_int, P, P, c_double, P, P, P, P, c_size_t,
                                P]),
+    "usbs_selftest_wait_limits": (c_int, [c_int, c_int, c_ll, P, P, P]),
 }
 
 

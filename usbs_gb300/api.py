@@ -8,9 +8,10 @@ Each function keeps the name, argument order and meaning of the reference
 * ``eigsh_smallest``                  solver/lanczos.py:239-284
 * ``usbs`` / ``cgal``                 solver/usbs.py:436, solver/cgal.py:21 (see solver.py)
 
-Inputs may be NumPy / SciPy (copied to the device) or CUDA torch tensors; the
-outputs are CUDA torch tensors.  There is no CPU path: without a CUDA device or
-without the built library every call raises.
+Inputs may be NumPy / SciPy (copied to the device), CUDA torch tensors, or any
+DLPack producer such as a JAX device array (used in place, no copy, when its
+dtype matches); the outputs are CUDA torch tensors.  There is no CPU path:
+without a CUDA device or without the built library every call raises.
 """
 import ctypes
 
@@ -18,6 +19,7 @@ import numpy as np
 import scipy.sparse as sp
 
 from . import _lib
+from .arrays import as_torch, to_device
 from .problem import DeviceProblem, layout
 
 
@@ -38,10 +40,8 @@ def _stream():
 
 
 def _dev(x, dtype, device):
-    torch = _torch()
-    if isinstance(x, torch.Tensor):
-        return x.to(device=device, dtype=dtype).contiguous()
-    return torch.as_tensor(np.ascontiguousarray(x), dtype=dtype, device=device)
+    _torch()
+    return to_device(x, dtype, device)
 
 
 def _vt(precision):
@@ -155,8 +155,9 @@ def eigsh_smallest(n, C, A_data, A_indices, adjoint_left_vec, q0, num_desired, i
     ``(eigenvalues[num_desired] float64, eigenvectors[n, num_desired])``."""
     torch = _torch()
     lib = _lib.load()
-    w = np.asarray(adjoint_left_vec) if not isinstance(adjoint_left_vec, torch.Tensor) \
-        else adjoint_left_vec
+    w = as_torch(adjoint_left_vec)
+    if w is None:
+        w = np.asarray(adjoint_left_vec)
     prob = _problem_for(C, A_data, A_indices, int(w.shape[0]), device)
     dev = prob.device
     vt = _vt(precision)

@@ -38,6 +38,8 @@ int get_device_info(DeviceInfo* out) {
     di.sm_count = sms;
     di.lanczos_occ64 = lanczos_occupancy(64);
     di.lanczos_occ32 = lanczos_occupancy(32);
+    di.stream_occ64 = lanczos_stream_occupancy(64);
+    di.stream_occ32 = lanczos_stream_occupancy(32);
     di.device = dev;
   }
   *out = di;
@@ -167,6 +169,7 @@ size_t usbs_eigsh_workspace_bytes(int n, long long nnz, int inner_iterations, in
     // no device: size for the largest GB300 team (152 SMs x 4 CTAs)
     di.sm_count = 152;
     di.lanczos_occ64 = di.lanczos_occ32 = 4;
+    di.stream_occ64 = di.stream_occ32 = 8;
   }
   const int vt = (precision == 64) ? 8 : 4;
   const int ld = (n + 31) & ~31;

@@ -12,6 +12,8 @@ struct DeviceInfo {
   int sm_count = 0;
   int lanczos_occ64 = 0;   // co-resident Lanczos CTAs per SM (FP64)
   int lanczos_occ32 = 0;   // co-resident Lanczos CTAs per SM (FP32)
+  int stream_occ64 = 0;    // co-resident CTAs per SM of the stream-path kernels (FP64)
+  int stream_occ32 = 0;    // ... (FP32)
 };
 int get_device_info(DeviceInfo* out);
 
@@ -40,6 +42,7 @@ size_t lanczos_workspace_bytes(int n, int ld, int m, int prec, int nctas);
 int lanczos_team_size(const DeviceInfo& di, int n, int prec);
 int lanczos_lanes(int n, long long nnz);
 int lanczos_occupancy(int prec);
+int lanczos_stream_occupancy(int prec);
 // 1 if a problem of n rows and m inner vectors runs as a thread-block cluster
 // (shared-memory resident), 0 if it runs as a cooperative team.
 int lanczos_kernel_kind(int n, int m, int prec);
@@ -47,6 +50,8 @@ int lanczos_kernel_kind(int n, int m, int prec);
 // fit, else one cooperative team each.
 int lanczos_run(const DeviceInfo& di, const LanczosProblem* probs, int count, int prec,
                 cudaStream_t stream);
+// kernels the calling thread's last lanczos_run launched
+int lanczos_last_launches();
 // cluster-size policy (rows per CTA by precision, batch and size class) and
 // the autotuner's hooks
 int lanczos_tune_candidates(int i);          // i-th candidate rows per CTA, 0 past the end

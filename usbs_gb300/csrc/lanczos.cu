@@ -38,19 +38,14 @@ constexpr int LZ_XS_BYTES = 160 * 1024;   // dynamic shared memory for a staged 
 template <typename VT>
 struct TeamDesc {
   int n, ld, m, num_desired, max_restarts, lanes, first_cta, nctas, xsmem;
-  int stages;            // non-zero: phases stream Q tiles through shared memory (bulk copies)
-  int stage_csr;         // the stages also carry each tile's CSR slice (phase A)
-  int stg_budget;        // bytes of the stage area (a multiple of 128)
-  int stg_cap;           // CSR slice capacity (entries, a multiple of 64)
   long long nnz;
   double tol;
   const int* rowptr;
   const int* col;
   const VT* val;
   VT* Q;                 // the caller's basis, ld x (m+1) column-major
-  // working basis: element (c, row) at Qw[qix(c, row)].  Staged teams keep it
-  // tile-major in the workspace (each 256-row tile's m+1 columns contiguous,
-  // so one bulk copy moves a tile's active columns); otherwise it is Q.
+  // working basis: element (c, row) at Qw[qix(c, row)] (here always Q:
+  // tile stride LZ_BLOCK, column stride ld)
   VT* Qw;
   long long qts, qcs;    // tile and column strides (elements)
   VT* vbuf;              // 3 flat vectors: two work vectors, then Q[:, k] of the cycle
@@ -108,8 +103,8 @@ struct LzShared {
 // [column][cta] partial layout, so the team reduction reads each column in one
 // coalesced load).  Columns 0..31 are reduced across each warp by one
 // butterfly reduce-scatter (lane c ends with column c), column 32 by a warp sum.
-template <typename VT, typename AT>
-__device__ __forceinline__ void block_reduce_cols(AT* acc, int nv, LzShared<VT>& sh, double* out,
+template <typename SH, typename AT>
+__device__ __forceinline__ void block_reduce_cols(AT* acc, int nv, SH& sh, double* out,
                                                   int R) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   if (nv == 1) {
@@ -167,8 +162,8 @@ __device__ __forceinline__ void reduce_part(const double* part_pass, int R, int 
 // Groups of up to 4 passes issue their rowptr loads, then their first col/val
 // loads, before any result is used: two dependent L2 round trips per group
 // instead of two per pass.
-template <typename VT, int L>
-__device__ __forceinline__ void spmv_tile(const TeamDesc<VT>& P, LzShared<VT>& sh, int base,
+template <typename VT, int L, typename SH>
+__device__ __forceinline__ void spmv_tile(const TeamDesc<VT>& P, SH& sh, int base,
                                           const VT* xsrc, const VT* xs, bool use_xs) {
   typedef typename Acc<VT>::type AT;
   constexpr int GPP = LZ_BLOCK / L;
@@ -269,395 +264,9 @@ __device__ void phase_spmv(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0, int 
   block_reduce_cols(acc, i + 1, sh, part_out, P.nctas);
 }
 
-// ---------------------------------------------------------------- staged tiles
-// Large problems (x not staged in shared memory): each phase streams its
-// tiles' rows of the needed Q columns and of one work vector into shared
-// memory with bulk async copies issued by thread 0, `stages` tiles ahead, so
-// a CTA reads its rows of the basis at streaming rate instead of one DRAM
-// round trip per tile.  The stage layout is planned per phase: the staged Q
-// columns, then the work vector, then (phase A, FP32) the tile's CSR slice,
-// so a phase that streams few columns keeps more tiles in flight.
-constexpr int STG_MAXS = 8;     // mbarriers, i.e. the deepest pipeline
-constexpr int STG_CAP = 4096;   // largest CSR slice (entries) a stage can carry
-struct StgHdr {
-  int rcnt;       // staged rowptr entries (from the tile's first row)
-  int p0;         // first entry of the tile
-  int ca0, ca1;   // staged col range [ca0, ca1)
-  int va0, va1;   // staged val range [va0, va1)
-  int pad[2];
-};
-// bytes of a stage's CSR slice part (rowptr, col, val, header) for `cap` entries
-template <typename VT>
-__host__ __device__ constexpr unsigned stg_csr_bytes(int cap) {
-  return (unsigned)(((LZ_BLOCK + 4) * 4 + (cap + 8) * 4 + (cap + 8) * (int)sizeof(VT) +
-                     (int)sizeof(StgHdr) + 127) / 128 * 128);
-}
-// bytes of the Q part of a stage: `cols` columns of LZ_BLOCK values
-template <typename VT>
-__host__ __device__ constexpr unsigned stg_q_bytes(int cols) {
-  return (unsigned)cols * LZ_BLOCK * (unsigned)sizeof(VT);
-}
-
-template <typename VT>
-struct Stager {
-  unsigned char* base;   // the stage area, `budget` bytes
-  uint64_t* bar;         // STG_MAXS mbarriers
-  unsigned budget;
-  int cap;               // CSR slice capacity (entries) of a phase-A stage
-  int csr;               // phase A stages carry the tile's CSR slice
-  // plan of the running phase (identical in every thread)
-  unsigned bytes;        // bytes per stage
-  int S;                 // stages (tiles in flight)
-  int vcol;              // stage column of the work vector (= staged Q columns)
-  unsigned rp, col, val, hdr;   // CSR slice offsets inside a stage
-  int nx_p0, nx_p1;      // thread 0: entry range of the next tile to issue (prefetched)
-  unsigned ph;           // parity of each mbarrier's next phase (identical in every thread)
-  __device__ VT* stage(int s) const { return (VT*)(base + (size_t)s * bytes); }
-  __device__ unsigned char* raw(int s) const { return base + (size_t)s * bytes; }
-};
-
-// stage layout and depth of a phase streaming `ncols` Q columns (+ the work
-// vector, + the CSR slice); the host sizes `budget` for two of the largest
-template <typename VT>
-__device__ __forceinline__ void stg_plan(Stager<VT>& G, int ncols, bool vec, bool csr) {
-  G.vcol = ncols;
-  const unsigned qb = stg_q_bytes<VT>(ncols + (vec ? 1 : 0));
-  G.rp = qb;
-  G.col = G.rp + (LZ_BLOCK + 4) * 4;
-  G.val = G.col + (unsigned)(G.cap + 8) * 4;
-  G.hdr = G.val + (unsigned)(G.cap + 8) * (unsigned)sizeof(VT);
-  G.bytes = csr ? qb + stg_csr_bytes<VT>(G.cap) : qb;
-  int S = (int)(G.budget / G.bytes);
-  G.S = S > STG_MAXS ? STG_MAXS : (S < 1 ? 1 : S);
-}
-
-// warp 0: rows of tile `tile` of Q[:, 0:ncols] and, if vec, of vec into stage
-// s; lane 0 arms the stage's mbarrier with the byte count, then the lanes
-// issue the copies in parallel (copy j by lane j mod 32)
-template <typename VT>
-__device__ void stg_issue(const TeamDesc<VT>& P, Stager<VT>& G, int s, int tile, int ncols,
-                          const VT* vec, bool csr = false) {
-  constexpr int E16 = 16 / (int)sizeof(VT);
-  const int lane = threadIdx.x & 31;
-  const int r0 = tile * LZ_BLOCK;
-  const int rows = min(LZ_BLOCK, P.n - r0);
-  // ld is a multiple of 32 >= n, so the padded rows stay inside each column
-  const unsigned bytes = (unsigned)(((rows + E16 - 1) / E16) * E16 * (int)sizeof(VT));
-  VT* st = G.stage(s);
-  unsigned tx = stg_q_bytes<VT>(ncols) + (vec ? bytes : 0u);
-  // CSR slice of the tile (phase A of FP32 stages): rowptr[r0 ..], col and val
-  // over [p0, p1), each widened to 16-byte boundaries inside its array; the
-  // few elements past an array's last full 16-byte block, and every entry of
-  // a tile larger than STG_CAP, are read from global memory by the consumers
-  unsigned rb = 0, cb = 0, vb = 0;
-  StgHdr h;
-  if (csr) {
-    const int p0 = __shfl_sync(0xffffffffu, G.nx_p0, 0);
-    const int p1 = __shfl_sync(0xffffffffu, G.nx_p1, 0);
-    int rcnt = (rows + 1 + 3) & ~3;
-    const int rmax = ((P.n + 1) & ~3) - r0;
-    if (rcnt > rmax) rcnt = rmax > 0 ? rmax : 0;
-    const long long nnz = P.nnz;
-    const bool fits = (p1 - p0) <= G.cap;
-    int ca0 = p0 & ~3, ca1 = (p1 + 3) & ~3;
-    const int cfull = (int)(nnz & ~3LL);
-    if (ca1 > cfull) ca1 = cfull;
-    if (!fits || ca1 < ca0) ca1 = ca0;
-    int va0 = p0 & ~(E16 - 1), va1 = (p1 + E16 - 1) & ~(E16 - 1);
-    const int vfull = (int)(nnz & ~(long long)(E16 - 1));
-    if (va1 > vfull) va1 = vfull;
-    if (!fits || va1 < va0) va1 = va0;
-    h.rcnt = rcnt; h.p0 = p0; h.ca0 = ca0; h.ca1 = ca1; h.va0 = va0; h.va1 = va1;
-    if (lane == 0) *(StgHdr*)(G.raw(s) + G.hdr) = h;
-    rb = (unsigned)rcnt * 4u;
-    cb = (unsigned)(ca1 - ca0) * 4u;
-    vb = (unsigned)(va1 - va0) * (unsigned)sizeof(VT);
-    tx += rb + cb + vb;
-  }
-  // the stage's earlier generic accesses (header, products written over the
-  // values) before the async copies into it; the global data the copies read
-  // was fenced by its writers before the team barrier that precedes the phase
-  fence_proxy_async_smem();
-  if (lane == 0) mbar_arrive_expect_tx(&G.bar[s], tx);
-  __syncwarp();
-  // streamed once per phase: evict_first, so the copies do not push the SpMV's
-  // x (gathered with evict_last) out of L2
-  const uint64_t pol = l2_evict_first_policy();
-  // the tile's first ncols columns are contiguous in the tile-major basis
-  // (full 256-row columns; the last tile is padded): one copy
-  const int nq = ncols > 0 ? 1 : 0;
-  const int ncopies = nq + (vec ? 1 : 0) + (csr ? 3 : 0);
-  if (lane < ncopies) {
-    const int j = lane;
-    if (j < nq) {
-      bulk_g2s_hint(st, P.Qw + (size_t)tile * (size_t)P.qts, stg_q_bytes<VT>(ncols), &G.bar[s],
-                    pol);
-    } else if (vec && j == nq) {
-      bulk_g2s_hint(st + (size_t)G.vcol * LZ_BLOCK, vec + r0, bytes, &G.bar[s], pol);
-    } else {
-      const int k = j - nq - (vec ? 1 : 0);   // 0 rowptr, 1 col, 2 val
-      if (k == 0 && rb) bulk_g2s_hint(G.raw(s) + G.rp, P.rowptr + r0, rb, &G.bar[s], pol);
-      if (k == 1 && cb) bulk_g2s_hint(G.raw(s) + G.col, P.col + h.ca0, cb, &G.bar[s], pol);
-      if (k == 2 && vb) bulk_g2s_hint(G.raw(s) + G.val, P.val + h.va0, vb, &G.bar[s], pol);
-    }
-  }
-}
-
-// thread 0: entry range of tile `tile` (loads left in flight until the next issue)
-template <typename VT>
-__device__ __forceinline__ void stg_prefetch_range(const TeamDesc<VT>& P, Stager<VT>& G, int tile) {
-  const int r0 = tile * LZ_BLOCK;
-  G.nx_p0 = P.rowptr[r0];
-  G.nx_p1 = P.rowptr[min(r0 + LZ_BLOCK, P.n)];
-}
-
-// body(tile, stage) for tiles [t0, t1), copies pipelined `stages` deep.  On a
-// wait that runs past its limit: records ST_BARRIER_TIMEOUT, waits (bounded)
-// for the copies still in flight and returns false; the CTA then leaves at
-// its next team barrier.
-template <typename VT, typename F>
-__device__ bool stg_loop(const TeamDesc<VT>& P, Stager<VT>& G, int t0, int t1, int ncols,
-                         const VT* vec, F&& body, bool csr = false) {
-  const uint64_t LIMIT = 1000000000ull;
-  stg_plan(G, ncols, vec != nullptr, csr);
-  const int S = G.S;
-  if (threadIdx.x < 32) {
-    for (int j = 0; j < S && t0 + j < t1; ++j) {
-      if (csr && threadIdx.x == 0) stg_prefetch_range(P, G, t0 + j);
-      stg_issue(P, G, j, t0 + j, ncols, vec, csr);
-    }
-    if (csr && threadIdx.x == 0 && t0 + S < t1) stg_prefetch_range(P, G, t0 + S);
-  }
-  for (int t = t0; t < t1; ++t) {
-    const int s = (t - t0) % S;
-    const unsigned par = (G.ph >> s) & 1u;
-    const bool ok = mbar_wait(&G.bar[s], par, LIMIT);
-    if (__syncthreads_or(!ok)) {
-      // drain: this tile's copies and those of the later tiles already issued
-      mbar_wait(&G.bar[s], par, LIMIT);
-      G.ph ^= (1u << s);
-      for (int tt = t + 1; tt < t1 && tt < t + S; ++tt) {
-        const int s2 = (tt - t0) % S;
-        mbar_wait(&G.bar[s2], (G.ph >> s2) & 1u, LIMIT);
-        G.ph ^= (1u << s2);
-      }
-      if (threadIdx.x == 0) atomicOr(P.status, ST_BARRIER_TIMEOUT);
-      __syncthreads();
-      return false;
-    }
-    G.ph ^= (1u << s);
-    body(t, s);
-    __syncthreads();
-    if (threadIdx.x < 32 && t + S < t1) {
-      stg_issue(P, G, s, t + S, ncols, vec, csr);
-      if (csr && threadIdx.x == 0 && t + S + 1 < t1) stg_prefetch_range(P, G, t + S + 1);
-    }
-  }
-  return true;
-}
-
-// SpMV of one 256-row tile from its staged CSR slice (rowptr, col, val in
-// shared memory; x gathered from global memory), L lanes per row, groups of up
-// to 4 passes as in spmv_tile
-template <typename VT, int L>
-__device__ __forceinline__ void spmv_tile_stg(const TeamDesc<VT>& P, LzShared<VT>& sh,
-                                              const Stager<VT>& G, int base,
-                                              const unsigned char* stg, const VT* xsrc) {
-  typedef typename Acc<VT>::type AT;
-  constexpr int GPP = LZ_BLOCK / L;
-  constexpr int CH = L < 4 ? L : 4;
-  const StgHdr h = *(const StgHdr*)(stg + G.hdr);
-  const int* rp = (const int*)(stg + G.rp);
-  const int* cs = (const int*)(stg + G.col);
-  VT* vs = (VT*)(stg + G.val);
-  const int tid = threadIdx.x, g = tid / L, lig = tid - (tid / L) * L;
-  const int rows = min(LZ_BLOCK, P.n - base);
-  // fully staged tile: every product v x[c] of the tile at once (about nnz /
-  // 256 independent gathers per thread), written over its own value in the
-  // stage, then one thread per row sums its row's products
-  if (rows + 1 <= h.rcnt) {
-    const int p0 = rp[0], p1 = rp[rows];
-    if (p1 <= h.ca1 && p1 <= h.va1) {
-      const uint64_t keep = l2_evict_last_policy();
-      constexpr int U = 16;   // one round of gathers for slices up to STG_CAP entries
-      for (int pb = p0 + tid; pb < p1; pb += U * LZ_BLOCK) {
-        int c[U];
-        VT xv[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int p = pb + u * LZ_BLOCK;
-          c[u] = (p < p1) ? cs[p - h.ca0] : 0;
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) xv[u] = ldcg_pol(xsrc + c[u], keep);
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int p = pb + u * LZ_BLOCK;
-          if (p < p1) vs[p - h.va0] = vs[p - h.va0] * xv[u];
-        }
-      }
-      fence_proxy_async_smem();   // the stage is refilled by bulk copies later
-      __syncthreads();
-      if (tid < rows) {
-        AT sacc = (AT)0;
-        const int e = rp[tid + 1];
-        for (int p = rp[tid]; p < e; ++p) sacc += (AT)vs[p - h.va0];
-        sh.u.st.ys[tid] = (double)sacc;
-      }
-      return;
-    }
-  }
-  auto colv = [&](int p, int& c, VT& v) {
-    c = (p < h.ca1) ? cs[p - h.ca0] : P.col[p];
-    v = (p < h.va1) ? vs[p - h.va0] : P.val[p];
-  };
-#pragma unroll 1
-  for (int q0 = 0; q0 < L; q0 += CH) {
-    int pb[CH], pe[CH];
-#pragma unroll
-    for (int q = 0; q < CH; ++q) {
-      const int lr = (q0 + q) * GPP + g;
-      const int row = base + lr;
-      pb[q] = 0; pe[q] = 0;
-      if (row < P.n) {
-        pb[q] = ((lr < h.rcnt) ? rp[lr] : P.rowptr[row]) + lig;
-        pe[q] = (lr + 1 < h.rcnt) ? rp[lr + 1] : P.rowptr[row + 1];
-      }
-    }
-#pragma unroll
-    for (int q = 0; q < CH; ++q) {
-      AT s = (AT)0;
-      for (int p = pb[q]; p < pe[q]; p += L) {
-        int c;
-        VT v;
-        colv(p, c, v);
-        s += (AT)v * (AT)__ldcg(xsrc + c);
-      }
-#pragma unroll
-      for (int o = L >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-      if (lig == 0) sh.u.st.ys[(q0 + q) * GPP + g] = (double)s;
-    }
-  }
-}
-
-// staged phase A: as phase_spmv, with Q[:, c] (and xsrc's own rows) from the stage
-template <typename VT>
-__device__ void stg_phase_spmv(const TeamDesc<VT>& P, LzShared<VT>& sh, Stager<VT>& G, int t0,
-                               int t1, int i, const VT* xsrc, VT xscale, bool wq, VT* vout,
-                               double* part_out) {
-  typedef typename Acc<VT>::type AT;
-  AT acc[MP1];
-#pragma unroll
-  for (int c = 0; c < MP1; ++c) acc[c] = (AT)0;
-  const int tid = threadIdx.x, L = P.lanes;
-  const size_t ld = (size_t)P.ld;
-  const int ncols = wq ? i : i + 1;
-  const bool csr = G.csr != 0;
-  stg_loop(P, G, t0, t1, ncols, wq ? xsrc : nullptr, [&](int tile, int sidx) {
-    const VT* stq = G.stage(sidx);
-    const int base = tile * LZ_BLOCK;
-    if (csr) {
-      const unsigned char* stg = G.raw(sidx);
-      switch (L) {
-        case 1: spmv_tile_stg<VT, 1>(P, sh, G, base, stg, xsrc); break;
-        case 2: spmv_tile_stg<VT, 2>(P, sh, G, base, stg, xsrc); break;
-        case 4: spmv_tile_stg<VT, 4>(P, sh, G, base, stg, xsrc); break;
-        case 8: spmv_tile_stg<VT, 8>(P, sh, G, base, stg, xsrc); break;
-        case 16: spmv_tile_stg<VT, 16>(P, sh, G, base, stg, xsrc); break;
-        default: spmv_tile_stg<VT, 32>(P, sh, G, base, stg, xsrc); break;
-      }
-    } else {
-      switch (L) {
-        case 1: spmv_tile<VT, 1>(P, sh, base, xsrc, nullptr, false); break;
-        case 2: spmv_tile<VT, 2>(P, sh, base, xsrc, nullptr, false); break;
-        case 4: spmv_tile<VT, 4>(P, sh, base, xsrc, nullptr, false); break;
-        case 8: spmv_tile<VT, 8>(P, sh, base, xsrc, nullptr, false); break;
-        case 16: spmv_tile<VT, 16>(P, sh, base, xsrc, nullptr, false); break;
-        default: spmv_tile<VT, 32>(P, sh, base, xsrc, nullptr, false); break;
-      }
-    }
-    __syncthreads();
-    const int row = base + tid;
-    if (row < P.n) {
-      const VT y = (VT)sh.u.st.ys[tid] * xscale;
-      vout[row] = y;
-      VT xn = (VT)0;
-      if (wq) {
-        xn = stq[(size_t)G.vcol * LZ_BLOCK + tid] * xscale;
-        P.Qw[qix(P, i, row)] = xn;
-      }
-#pragma unroll
-      for (int c = 0; c < MP1; ++c) {
-        if (c <= i) {
-          const VT qc = (wq && c == i) ? xn : stq[(size_t)c * LZ_BLOCK + tid];
-          acc[c] += (AT)qc * (AT)y;
-        }
-      }
-    }
-  }, csr);
-  block_reduce_cols(acc, i + 1, sh, part_out, P.nctas);
-}
-
-// staged phase B: buf -= Q h (c < nv); acc[c] = Q[:, c] . buf
-template <typename VT>
-__device__ void stg_phase_update_dot(const TeamDesc<VT>& P, LzShared<VT>& sh, Stager<VT>& G,
-                                     int t0, int t1, int nv, VT* buf, double* part_out) {
-  typedef typename Acc<VT>::type AT;
-  AT acc[MP1];
-#pragma unroll
-  for (int c = 0; c < MP1; ++c) acc[c] = (AT)0;
-  const int tid = threadIdx.x;
-  stg_loop(P, G, t0, t1, nv, buf, [&](int tile, int sidx) {
-    const VT* stq = G.stage(sidx);
-    const int row = tile * LZ_BLOCK + tid;
-    if (row < P.n) {
-      VT qr[MP1];
-      VT s = (VT)0;
-#pragma unroll
-      for (int c = 0; c < MP1; ++c) {
-        if (c < nv) {
-          qr[c] = stq[(size_t)c * LZ_BLOCK + tid];
-          s += qr[c] * sh.hv[c];
-        }
-      }
-      const VT q1 = stq[(size_t)G.vcol * LZ_BLOCK + tid] - s;
-      buf[row] = q1;
-#pragma unroll
-      for (int c = 0; c < MP1; ++c)
-        if (c < nv) acc[c] += (AT)qr[c] * (AT)q1;
-    }
-  });
-  block_reduce_cols(acc, nv, sh, part_out, P.nctas);
-}
-
-// staged phase C: buf -= Q h (c < nv); part_out[0] = sum buf^2 over own rows
-template <typename VT>
-__device__ void stg_phase_update_norm(const TeamDesc<VT>& P, LzShared<VT>& sh, Stager<VT>& G,
-                                      int t0, int t1, int nv, VT* buf, double* part_out) {
-  typedef typename Acc<VT>::type AT;
-  AT nrm = (AT)0;
-  const int tid = threadIdx.x;
-  stg_loop(P, G, t0, t1, nv, buf, [&](int tile, int sidx) {
-    const VT* stq = G.stage(sidx);
-    const int row = tile * LZ_BLOCK + tid;
-    if (row < P.n) {
-      VT s = (VT)0;
-#pragma unroll
-      for (int c = 0; c < MP1; ++c)
-        if (c < nv) s += stq[(size_t)c * LZ_BLOCK + tid] * sh.hv[c];
-      const VT q2 = stq[(size_t)G.vcol * LZ_BLOCK + tid] - s;
-      buf[row] = q2;
-      nrm += (AT)q2 * (AT)q2;
-    }
-  });
-  AT one[MP1];
-  one[0] = nrm;
-  block_reduce_cols(one, 1, sh, part_out, P.nctas);
-}
-
 // Breakdown pass a: buf = hash_normal(key) for own rows, acc[c] = Q[:, c] . buf (c < nv)
-template <typename VT>
-__device__ void phase_random(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0, int t1, int nv,
+template <typename VT, typename SH>
+__device__ void phase_random(const TeamDesc<VT>& P, SH& sh, int t0, int t1, int nv,
                              uint64_t key, VT* buf, double* part_out) {
   typedef typename Acc<VT>::type AT;
   AT acc[MP1];
@@ -678,8 +287,8 @@ __device__ void phase_random(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0, in
 }
 
 // Phase B: buf -= Q h (c < nv); acc[c] = Q[:, c] . buf
-template <typename VT>
-__device__ void phase_update_dot(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0, int t1, int nv,
+template <typename VT, typename SH>
+__device__ void phase_update_dot(const TeamDesc<VT>& P, SH& sh, int t0, int t1, int nv,
                                  VT* buf, double* part_out) {
   typedef typename Acc<VT>::type AT;
   AT acc[MP1];
@@ -709,8 +318,8 @@ __device__ void phase_update_dot(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0
 }
 
 // Phase C: buf -= Q h (c < nv); part_out[0] = sum buf^2 over own rows
-template <typename VT>
-__device__ void phase_update_norm(const TeamDesc<VT>& P, LzShared<VT>& sh, int t0, int t1, int nv,
+template <typename VT, typename SH>
+__device__ void phase_update_norm(const TeamDesc<VT>& P, SH& sh, int t0, int t1, int nv,
                                   VT* buf, double* part_out) {
   typedef typename Acc<VT>::type AT;
   AT nrm = (AT)0;
@@ -801,6 +410,11 @@ __device__ void restart_select(const D& P, LzShared<VT>& sh, int k, bool write_o
   }
   const double* Z = X;
   if (tid == 0) {
+    // a NaN / Inf in the projected matrix (e.g. from a non-finite operator)
+    // ends the call after this restart with ST_NONFINITE
+    bool fin = true;
+    for (int c = 0; c < m; ++c) fin = fin && isfinite(sh.alpha[c]) && isfinite(sh.beta[c]);
+    if (!fin) atomicOr(P.status, ST_NONFINITE);
     const double bl = sh.beta[m - 1];
     int nconv = m;
     for (int c = 0; c < m; ++c) {
@@ -873,13 +487,7 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
   const int rank = (int)blockIdx.x - P.first_cta, R = P.nctas;
   const int tid = threadIdx.x;
   TeamBarrier bar{P.bar, R, P.status};
-  // staged phases read Q and the work vectors with bulk copies (async proxy):
-  // every thread fences its generic global stores before each team barrier
-  const bool staged = P.stages != 0;
-  auto team_sync = [&]() -> bool {
-    if (staged) fence_proxy_async_global();
-    return bar.sync();
-  };
+  auto team_sync = [&]() -> bool { return bar.sync(); };
   const int n = P.n, m = P.m;
   const size_t ld = (size_t)P.ld;
   const int ntiles = (n + LZ_BLOCK - 1) / LZ_BLOCK;
@@ -905,35 +513,11 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
   } while (0)
   if (rank == 0 && tid < MAXM) { sh.alpha[tid] = 0.0; sh.beta[tid] = 0.0; }
   if (tid == 0) sh.eig_cycles = 0;
-  // staged tiles (large problems): the stage area (laid out per phase), then
-  // STG_MAXS mbarriers, in the dynamic shared memory
-  extern __shared__ __align__(16) unsigned char lz_dyn[];
-  Stager<VT> G;
-  G.budget = (unsigned)P.stg_budget;
-  G.cap = P.stg_cap;
-  G.csr = P.stage_csr;
-  G.S = 0;
-  G.bytes = 0;
-  G.vcol = 0;
-  G.ph = 0u;
-  G.nx_p0 = G.nx_p1 = 0;
-  G.base = lz_dyn;
-  G.bar = (uint64_t*)(lz_dyn + (size_t)G.budget);
-  if (P.stages && tid == 0) {
-    for (int j = 0; j < STG_MAXS; ++j) mbar_init(&G.bar[j], 1);
-    mbar_init_fence();
-  }
-  // the start vector Q[:, 0]: flat copy for the first cycle's gathers and, for
-  // a tile-major working basis, its column 0 (own rows)
+  // the start vector Q[:, 0]: flat copy for the first cycle's gathers
   VT* xk = P.vbuf + 2 * ld;
-  const bool tiled = P.Qw != P.Q;
   for (int tile = t0; tile < t1; ++tile) {
     const int row = tile * LZ_BLOCK + tid;
-    if (row < n) {
-      const VT v = P.Q[row];
-      xk[row] = v;
-      if (tiled) P.Qw[qix(P, 0, row)] = v;
-    }
+    if (row < n) xk[row] = P.Q[row];
   }
   __syncthreads();
   if (!team_sync()) return;
@@ -975,24 +559,21 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
       }
       VT* vout = P.vbuf + (size_t)cur * ld;
       LZ_MARK(1);
-      if (P.stages) stg_phase_spmv(P, sh, G, t0, t1, i, xsrc, invb, wq, vout, part0 + rank);
-      else phase_spmv(P, sh, t0, t1, i, xsrc, invb, wq, vout, part0 + rank);
+      phase_spmv(P, sh, t0, t1, i, xsrc, invb, wq, vout, part0 + rank);
       LZ_MARK(2);
       if (!team_sync()) return;
       LZ_MARK(0);
       reduce_part(part0, R, i + 1, sh);
       LZ_MARK(1);
       const double h1i = sh.h[i];
-      if (P.stages) stg_phase_update_dot(P, sh, G, t0, t1, i + 1, vout, part1 + rank);
-      else phase_update_dot(P, sh, t0, t1, i + 1, vout, part1 + rank);
+      phase_update_dot(P, sh, t0, t1, i + 1, vout, part1 + rank);
       LZ_MARK(3);
       if (!team_sync()) return;
       LZ_MARK(0);
       reduce_part(part1, R, i + 1, sh);
       LZ_MARK(1);
       if (rank == 0 && tid == 0) sh.alpha[i] = h1i + sh.h[i];
-      if (P.stages) stg_phase_update_norm(P, sh, G, t0, t1, i + 1, vout, part2 + rank);
-      else phase_update_norm(P, sh, t0, t1, i + 1, vout, part2 + rank);
+      phase_update_norm(P, sh, t0, t1, i + 1, vout, part2 + rank);
       LZ_MARK(4);
       if (!team_sync()) return;
       LZ_MARK(0);
@@ -1031,6 +612,7 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
       clk_restart += clock64() - c0;
     }
     if (!team_sync()) return;
+    if (__ldcg(P.status) & ST_NONFINITE) { ++restart; break; }
     const int kn = __ldcg(P.ctl + 0);
     nconv = __ldcg(P.ctl + 1);
     for (int e = tid; e < m * MAXM; e += LZ_BLOCK) {
@@ -1065,14 +647,6 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
     if (!team_sync()) return;
     if (timing) tmark = clock64();   // restart time is reported separately (ctl[6])
   }
-  // a tile-major working basis back to the caller's column-major Q (own rows)
-  if (tiled && restart > 0) {
-    for (int c = 0; c <= m; ++c)
-      for (int tile = t0; tile < t1; ++tile) {
-        const int row = tile * LZ_BLOCK + tid;
-        if (row < n) P.Q[(size_t)c * ld + row] = P.Qw[qix(P, c, row)];
-      }
-  }
   if (rank == 0 && tid == 0) {
     P.ctl[2] = restart;
     P.ctl[3] = breakdowns;
@@ -1084,6 +658,305 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
     P.ctl[14] = sum_kn;
     P.ctl[15] = (int)(sh.eig_cycles >> 10);
     if (restart == 0) P.ctl[0] = 0;
+  }
+}
+
+// ---------------------------------------------------------------- stream path
+// Problems whose x does not fit in shared memory (n * sizeof(VT) > 160 KB) run
+// as a sequence of ordinary full-GPU launches instead of one cooperative
+// launch: every Lanczos step is
+//   A1  y = Op x for one 256-row tile per CTA (L lanes per row), x = v * 1/beta
+//       folded in; also stores Q[:, i] = x          (no partial sums)
+//   A2  h1 = Q[:, :i+1]^T y                          (partials, last-CTA sum)
+//   B   q1 = y - Q h1,  h2 = Q^T q1                  (partials, last-CTA sum)
+//   C   q2 = q1 - Q h2, ||q2||^2                     (partials, last-CTA sum)
+// and a restart is one CTA's projected eigensolve and selection followed by a
+// full-GPU rotation of the basis.  A kernel boundary is the grid-wide
+// barrier, so no CTA ever waits on another and the kernels may share the GPU
+// with other work.  Each CTA writes its partial sums to [column][cta]; the
+// last CTA to finish (an atomic ticket after a fence) sums them in CTA order,
+// so the result does not depend on which CTA is last.  The loop state lives
+// in a device control block (StreamCtl) that only those last CTAs and the
+// restart kernel write: every kernel of a step reads the same state at its
+// start and derives the same mode (step, breakdown replacement, or nothing
+// to do), so the host enqueues a cycle's launches without reading anything
+// back, and reads the block once per restart.
+struct StreamCtl {
+  int i, k, bd, cur;           // step, saved vectors, breakdown pending, work vector in use
+  int stop, rot, stepped;      // loop ended; rotation pending; the finished cycle had steps
+  int restarts, breakdowns, steps, sum_nv, sum_kn, nconv;
+  unsigned ticket[4];          // last-CTA tickets of A2, B, C and the rotation
+  double invb;                 // 1 / beta of the latest unnormalised vector
+  double h1[MP1], h2[MP1];
+  double alpha[MAXM], beta[MAXM];
+};
+
+template <typename VT>
+struct StShared {
+  union {
+    struct {
+      double ys[LZ_BLOCK];
+      double wred[LZ_NW][MP1];
+    } st;
+    VT Ys[MAXM * MAXM];
+  } u;
+  double h[MP1];
+  VT hv[MP1];
+  int last;
+};
+
+enum { SM_SKIP = 0, SM_STEP = 1, SM_BREAKDOWN = 2 };
+
+// the step's mode from the control block (the same in every kernel of a step)
+__device__ __forceinline__ int st_mode(const StreamCtl* c, int m, int* i, int* nv, int* buf) {
+  const int stop = __ldcg(&c->stop), bd = __ldcg(&c->bd), ii = __ldcg(&c->i),
+            cur = __ldcg(&c->cur);
+  *i = ii;
+  if (stop || __ldcg(&c->rot)) return SM_SKIP;
+  if (bd) { *nv = ii; *buf = cur ^ 1; return SM_BREAKDOWN; }
+  if (ii < m) { *nv = ii + 1; *buf = cur; return SM_STEP; }
+  return SM_SKIP;
+}
+
+// ticket of the last CTA: true in every thread of the CTA that finished last
+// (its partial sums, fenced by their writers, are then visible to it)
+template <typename SH>
+__device__ __forceinline__ bool st_last_cta(unsigned* ticket, SH& sh) {
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) sh.last = (atomicAdd(ticket, 1u) == gridDim.x - 1) ? 1 : 0;
+  __syncthreads();
+  if (sh.last) __threadfence();
+  return sh.last != 0;
+}
+
+// h[c] = sum over the R CTAs of part[c][r], c < nv: warp w takes columns
+// w, w + 8, ...; lane l sums CTAs l, l + 32, ... in order, then a butterfly
+template <typename VT, typename SH>
+__device__ __forceinline__ void st_reduce(const double* part, int R, int nv, SH& sh) {
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int c = w; c < nv; c += LZ_NW) {
+    const double* p = part + (size_t)c * R;
+    double a0 = 0.0, a1 = 0.0;
+    int r = lane;
+    for (; r + 32 < R; r += 64) { a0 += __ldcg(p + r); a1 += __ldcg(p + r + 32); }
+    if (r < R) a0 += __ldcg(p + r);
+    const double a = warp_sum(a0 + a1);
+    if (lane == 0) { sh.h[c] = a; sh.hv[c] = (VT)a; }
+  }
+  __syncthreads();
+}
+
+// A1: one tile per CTA.  Step: vbuf[cur] = Op x, x = (i == k ? Q[:, k] :
+// vbuf[cur ^ 1] / beta), and Q[:, i] = x when i > k.  Breakdown: vbuf[cur ^ 1]
+// = a Gaussian vector keyed by i (the replacement of solver/lanczos.py:107-117).
+template <typename VT>
+__global__ void __launch_bounds__(LZ_BLOCK) st_spmv_kernel(const __grid_constant__ TeamDesc<VT> P,
+                                                            StreamCtl* ctl) {
+  __shared__ StShared<VT> sh;
+  int i, nv, buf;
+  const int mode = st_mode(ctl, P.m, &i, &nv, &buf);
+  if (mode == SM_SKIP) return;
+  const size_t ld = (size_t)P.ld;
+  const int base = blockIdx.x * LZ_BLOCK, row = base + threadIdx.x;
+  if (mode == SM_BREAKDOWN) {
+    if (row < P.n) P.vbuf[(size_t)buf * ld + row] = (VT)hash_normal((uint64_t)i, (uint64_t)row);
+    return;
+  }
+  const int k = __ldcg(&ctl->k);
+  const bool wq = i > k;
+  const VT xscale = wq ? (VT)__ldcg(&ctl->invb) : (VT)1;
+  const VT* xsrc = wq ? P.vbuf + (size_t)(buf ^ 1) * ld : P.Q + (size_t)k * ld;
+  switch (P.lanes) {
+    case 1: spmv_tile<VT, 1>(P, sh, base, xsrc, xsrc, false); break;
+    case 2: spmv_tile<VT, 2>(P, sh, base, xsrc, xsrc, false); break;
+    case 4: spmv_tile<VT, 4>(P, sh, base, xsrc, xsrc, false); break;
+    case 8: spmv_tile<VT, 8>(P, sh, base, xsrc, xsrc, false); break;
+    case 16: spmv_tile<VT, 16>(P, sh, base, xsrc, xsrc, false); break;
+    default: spmv_tile<VT, 32>(P, sh, base, xsrc, xsrc, false); break;
+  }
+  __syncthreads();
+  if (row < P.n) {
+    P.vbuf[(size_t)buf * ld + row] = (VT)sh.u.st.ys[threadIdx.x] * xscale;
+    if (wq) P.Q[(size_t)i * ld + row] = __ldcg(xsrc + row) * xscale;
+  }
+}
+
+// A2: h1[c] = Q[:, c] . v for c < nv (v = the step's y, or the breakdown vector)
+template <typename VT>
+__global__ void __launch_bounds__(LZ_BLOCK) st_dot_kernel(const __grid_constant__ TeamDesc<VT> P,
+                                                           StreamCtl* ctl) {
+  typedef typename Acc<VT>::type AT;
+  __shared__ StShared<VT> sh;
+  int i, nv, buf;
+  if (st_mode(ctl, P.m, &i, &nv, &buf) == SM_SKIP) return;
+  const int R = gridDim.x, ntiles = (P.n + LZ_BLOCK - 1) / LZ_BLOCK;
+  const int t0 = (int)((long long)ntiles * blockIdx.x / R);
+  const int t1 = (int)((long long)ntiles * (blockIdx.x + 1) / R);
+  const VT* v = P.vbuf + (size_t)buf * P.ld;
+  AT acc[MP1];
+#pragma unroll
+  for (int c = 0; c < MP1; ++c) acc[c] = (AT)0;
+  for (int tile = t0; tile < t1; ++tile) {
+    const int row = tile * LZ_BLOCK + threadIdx.x;
+    if (row < P.n) {
+      const VT y = v[row];
+#pragma unroll
+      for (int c = 0; c < MP1; ++c)
+        if (c < nv) acc[c] += (AT)P.Q[(size_t)c * P.ld + row] * (AT)y;
+    }
+  }
+  block_reduce_cols(acc, nv, sh, P.part + blockIdx.x, R);
+  if (!st_last_cta(&ctl->ticket[0], sh)) return;
+  st_reduce<VT>(P.part, R, nv, sh);
+  for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) ctl->h1[c] = sh.h[c];
+  if (threadIdx.x == 0) ctl->ticket[0] = 0u;
+}
+
+// B: v -= Q h1 (c < nv), h2 = Q^T v; on a step, alpha[i] = h1[i] + h2[i]
+template <typename VT>
+__global__ void __launch_bounds__(LZ_BLOCK) st_update_dot_kernel(
+    const __grid_constant__ TeamDesc<VT> P, StreamCtl* ctl) {
+  __shared__ StShared<VT> sh;
+  int i, nv, buf;
+  const int mode = st_mode(ctl, P.m, &i, &nv, &buf);
+  if (mode == SM_SKIP) return;
+  const int R = gridDim.x, ntiles = (P.n + LZ_BLOCK - 1) / LZ_BLOCK;
+  const int t0 = (int)((long long)ntiles * blockIdx.x / R);
+  const int t1 = (int)((long long)ntiles * (blockIdx.x + 1) / R);
+  for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) sh.hv[c] = (VT)__ldcg(&ctl->h1[c]);
+  __syncthreads();
+  double* part = P.part + (size_t)MP1 * R;
+  phase_update_dot(P, sh, t0, t1, nv, P.vbuf + (size_t)buf * P.ld, part + blockIdx.x);
+  if (!st_last_cta(&ctl->ticket[1], sh)) return;
+  st_reduce<VT>(part, R, nv, sh);
+  for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) ctl->h2[c] = sh.h[c];
+  if (threadIdx.x == 0) {
+    if (mode == SM_STEP) ctl->alpha[i] = __ldcg(&ctl->h1[i]) + sh.h[i];
+    ctl->ticket[1] = 0u;
+  }
+}
+
+// C: v -= Q h2 (c < nv), ||v||^2; the last CTA advances the loop state
+template <typename VT>
+__global__ void __launch_bounds__(LZ_BLOCK) st_update_norm_kernel(
+    const __grid_constant__ TeamDesc<VT> P, StreamCtl* ctl) {
+  __shared__ StShared<VT> sh;
+  int i, nv, buf;
+  const int mode = st_mode(ctl, P.m, &i, &nv, &buf);
+  if (mode == SM_SKIP) return;
+  const int R = gridDim.x, ntiles = (P.n + LZ_BLOCK - 1) / LZ_BLOCK;
+  const int t0 = (int)((long long)ntiles * blockIdx.x / R);
+  const int t1 = (int)((long long)ntiles * (blockIdx.x + 1) / R);
+  for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) sh.hv[c] = (VT)__ldcg(&ctl->h2[c]);
+  __syncthreads();
+  double* part = P.part + (size_t)2 * MP1 * R;
+  phase_update_norm(P, sh, t0, t1, nv, P.vbuf + (size_t)buf * P.ld, part + blockIdx.x);
+  if (!st_last_cta(&ctl->ticket[2], sh)) return;
+  st_reduce<VT>(part, R, 1, sh);
+  if (threadIdx.x == 0) {
+    const double nrm2 = sh.h[0];
+    if (mode == SM_STEP) {
+      // solver/lanczos.py:95-105 and the breakdown test of :107
+      const double b = sqrt(nrm2);
+      ctl->beta[i] = b;
+      ctl->steps += 1;
+      ctl->sum_nv += i + 1;
+      ctl->cur = buf ^ 1;
+      ctl->i = i + 1;
+      if (b < 1e-15) {
+        ctl->bd = 1;
+        ctl->breakdowns += 1;
+      } else {
+        ctl->invb = 1.0 / b;
+      }
+    } else {
+      ctl->invb = 1.0 / sqrt(nrm2);
+      ctl->bd = 0;
+    }
+    ctl->ticket[2] = 0u;
+  }
+}
+
+// restart, one CTA: the projected eigenproblem and the thick-restart choice
+// (solver/lanczos.py:128-168, 202-221) once the cycle's m steps are done
+template <typename VT>
+__global__ void __launch_bounds__(LZ_BLOCK, 1) st_restart_kernel(
+    const __grid_constant__ TeamDesc<VT> P, StreamCtl* ctl) {
+  __shared__ LzShared<VT> sh;
+  const int m = P.m, tid = threadIdx.x;
+  if (ctl->stop || ctl->rot || ctl->bd || ctl->i < m) return;
+  if (tid == 0) sh.eig_cycles = 0;
+  if (tid < m) { sh.alpha[tid] = ctl->alpha[tid]; sh.beta[tid] = ctl->beta[tid]; }
+  __syncthreads();
+  const int k = ctl->k;
+  const long long c0 = clock64();
+  restart_select<false>(P, sh, k);
+  if (tid < m) { ctl->alpha[tid] = sh.alpha[tid]; ctl->beta[tid] = sh.beta[tid]; }
+  if (tid == 0) {
+    const int kn = sh.k_next;
+    ctl->stepped = (k < m) ? 1 : 0;
+    ctl->k = kn;
+    ctl->nconv = sh.nconv;
+    ctl->restarts += 1;
+    ctl->sum_kn += kn;
+    ctl->rot = 1;
+    const bool bad = (*(volatile int*)P.status & ST_NONFINITE) != 0;
+    if (bad || sh.nconv >= P.num_desired || ctl->restarts >= P.max_restarts) ctl->stop = 1;
+    P.ctl[2] = ctl->restarts;
+    P.ctl[3] = ctl->breakdowns;
+    P.ctl[4] = ctl->steps;
+    P.ctl[6] += (int)((clock64() - c0) >> 10);
+    P.ctl[13] = ctl->sum_nv;
+    P.ctl[14] = ctl->sum_kn;
+    P.ctl[15] += (int)(sh.eig_cycles >> 10);
+  }
+}
+
+// restart rotation, full grid: Q[:, :kn] = Q[:, :m] Y, then Q[:, kn] (and
+// Q[:, m]) = the last normalised vector (solver/lanczos.py:217-221)
+template <typename VT>
+__global__ void __launch_bounds__(LZ_BLOCK) st_rotate_kernel(const __grid_constant__ TeamDesc<VT> P,
+                                                              StreamCtl* ctl) {
+  __shared__ StShared<VT> sh;
+  if (!__ldcg(&ctl->rot)) return;
+  const int m = P.m, kn = __ldcg(&ctl->k);
+  const bool stepped = __ldcg(&ctl->stepped) != 0;
+  const VT invb = (VT)__ldcg(&ctl->invb);
+  const size_t ld = (size_t)P.ld;
+  const VT* lastv = P.vbuf + (size_t)(__ldcg(&ctl->cur) ^ 1) * ld;
+  for (int e = threadIdx.x; e < m * MAXM; e += LZ_BLOCK) {
+    const int j = e / MAXM, c = e - j * MAXM;
+    sh.u.Ys[e] = (c < kn) ? (VT)__ldcg(P.Ybuf + j * m + c) : (VT)0;
+  }
+  __syncthreads();
+  const int R = gridDim.x, ntiles = (P.n + LZ_BLOCK - 1) / LZ_BLOCK;
+  const int t0 = (int)((long long)ntiles * blockIdx.x / R);
+  const int t1 = (int)((long long)ntiles * (blockIdx.x + 1) / R);
+  for (int tile = t0; tile < t1; ++tile) {
+    const int row = tile * LZ_BLOCK + threadIdx.x;
+    if (row < P.n) {
+      VT qr[MAXM];
+#pragma unroll
+      for (int j = 0; j < MAXM; ++j) qr[j] = (j < m) ? P.Q[(size_t)j * ld + row] : (VT)0;
+      const VT xl = stepped ? lastv[row] * invb : P.Q[(size_t)m * ld + row];
+      for (int c = 0; c < kn; ++c) {
+        if (c >= m) break;
+        VT s = (VT)0;
+#pragma unroll
+        for (int j = 0; j < MAXM; ++j)
+          if (j < m) s += qr[j] * sh.u.Ys[j * MAXM + c];
+        P.Q[(size_t)c * ld + row] = s;
+      }
+      P.Q[(size_t)kn * ld + row] = xl;
+      if (kn != m) P.Q[(size_t)m * ld + row] = xl;
+    }
+  }
+  if (!st_last_cta(&ctl->ticket[3], sh)) return;
+  if (threadIdx.x == 0) {
+    ctl->i = kn;     // the next cycle starts from Q[:, kn]
+    ctl->rot = 0;
+    ctl->ticket[3] = 0u;
   }
 }
 
@@ -1494,6 +1367,9 @@ lanczos_cluster_kernel(const __grid_constant__ ClusterBatch<VT> batch) {
     const long long c0 = clock64();
     restart_select<true>(P, sh, k, /*write_out=*/rank == 0);
     if (timing) clk_restart += clock64() - c0;
+    // every CTA of the cluster found the same projected matrix, so all of
+    // them see their own ST_NONFINITE here and leave together
+    if (*(volatile int*)P.status & ST_NONFINITE) { ++restart; break; }
     const int kn = sh.k_next;
     nconv = sh.nconv;
     const VT* last = stepped ? (X.vb + (size_t)prev * rc) : (X.Qs + (size_t)m * rc);
@@ -1546,22 +1422,26 @@ lanczos_cluster_kernel(const __grid_constant__ ClusterBatch<VT> batch) {
 
 static size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 
-// tile-major working basis of a staged team (x too large for shared memory)
-static size_t team_basis_bytes(int n, int m, size_t vt) {
-  if ((size_t)n * vt <= (size_t)LZ_XS_BYTES) return 0;
-  const size_t tiles = ((size_t)n + LZ_BLOCK - 1) / LZ_BLOCK;
-  return align256(tiles * (size_t)(m + 1) * LZ_BLOCK * vt);
-}
+static thread_local int t_launches = 0;   // kernels the last lanczos_run launched (this thread)
 
+// x of a team-kernel problem is staged in shared memory; larger problems take
+// the stream path
+static bool x_fits_smem(int n, size_t vt) { return (size_t)n * vt <= (size_t)LZ_XS_BYTES; }
+
+// team path: 3 work vectors, [pass][column][cta] partials, the Ritz vectors
+// and the barrier counters.  Stream path (nctas = its grid): 2 work vectors
+// and the control block in the third vector's place, the same partials and
+// Ritz vectors.
 size_t lanczos_workspace_bytes(int n, int ld, int m, int prec, int nctas) {
+  (void)n; (void)m;
   const size_t vt = (prec == 64) ? 8 : 4;
   size_t b = align256(3 * (size_t)ld * vt);
   b += align256((size_t)3 * nctas * MP1 * sizeof(double));
   b += align256((size_t)MAXM * MAXM * sizeof(double));
   b += 256;  // barrier counters
-  b += team_basis_bytes(n, m, vt);
   return b;
 }
+static_assert(sizeof(StreamCtl) <= 32 * 4 * 32, "the control block takes one 32-row vector slot");
 
 int lanczos_lanes(int n, long long nnz) {
   const double avg = n > 0 ? (double)nnz / n : 1.0;
@@ -1571,6 +1451,13 @@ int lanczos_lanes(int n, long long nnz) {
 }
 
 int lanczos_team_size(const DeviceInfo& di, int n, int prec) {
+  if (!x_fits_smem(n, prec == 64 ? 8 : 4)) {
+    // stream path: the grid of its partial-sum kernels, one wave
+    const int tiles = (n + LZ_BLOCK - 1) / LZ_BLOCK;
+    const int occ = (prec == 64) ? di.stream_occ64 : di.stream_occ32;
+    const int g = di.sm_count * (occ > 0 ? occ : 1);
+    return tiles < g ? tiles : g;
+  }
   const int occ = (prec == 64) ? di.lanczos_occ64 : di.lanczos_occ32;
   // two SMs stay free for the single-CTA kernels that run beside the team
   const int maxc = (di.sm_count > 4 ? di.sm_count - 2 : di.sm_count) * (occ > 0 ? occ : 1);
@@ -1590,15 +1477,10 @@ int lanczos_team_size(const DeviceInfo& di, int n, int prec) {
   return want;
 }
 
-// team kernel: dynamic shared memory it may use (x staged, or the stage area
-// plus its mbarriers) and the stage area itself
+// team kernel: dynamic shared memory it may use (the staged x)
 template <typename VT>
 constexpr size_t tm_dyn_max() {
   return (227 * 1024 - sizeof(LzShared<VT>) - 1024) / 128 * 128;
-}
-template <typename VT>
-constexpr unsigned tm_budget() {
-  return (unsigned)((tm_dyn_max<VT>() - STG_MAXS * sizeof(uint64_t)) / 128 * 128);
 }
 static_assert(tm_dyn_max<double>() >= (size_t)LZ_XS_BYTES, "staged x must fit");
 
@@ -1647,34 +1529,6 @@ static int run_typed(const DeviceInfo& di, const LanczosProblem* probs, int coun
       t.lanes = lanczos_lanes(p.n, p.nnz);
       t.xsmem = ((size_t)p.n * sizeof(VT) <= (size_t)LZ_XS_BYTES) ? 1 : 0;
       if (t.xsmem && (size_t)p.n * sizeof(VT) > dyn) dyn = (size_t)p.n * sizeof(VT);
-      // staged tiles when x is not staged: bulk copies from the workspace (the
-      // work vectors and the tile-major basis) need it 16-byte aligned
-      t.stages = 0;
-      t.stage_csr = 0;
-      t.stg_budget = 0;
-      t.stg_cap = 0;
-      if (!t.xsmem && p.ld % 32 == 0 && ((uintptr_t)p.work & 15u) == 0) {
-        // the stage area takes the shared memory the kernel leaves; every
-        // phase keeps at least two of its largest stages in flight.  FP32
-        // stages also carry the tile's CSR slice, sized for 1.5x the mean
-        // tile (bulk copies of rowptr / col / val need 16-byte aligned arrays)
-        const unsigned budget = tm_budget<VT>();
-        const long long mean_tile = p.nnz * LZ_BLOCK / (p.n > 0 ? p.n : 1);
-        long long cap = (mean_tile * 3 / 2 + 63) / 64 * 64;
-        cap = cap < 512 ? 512 : (cap > STG_CAP ? STG_CAP : cap);
-        const unsigned qmax = stg_q_bytes<VT>(MP1 + 1);
-        const bool csr_ok = sizeof(VT) == 4 && ((((uintptr_t)p.rowptr) | ((uintptr_t)p.col) |
-                                                 ((uintptr_t)p.val)) & 15u) == 0 &&
-                            2 * (qmax + stg_csr_bytes<VT>((int)cap)) <= budget;
-        if (2 * qmax <= budget) {
-          t.stages = 1;
-          t.stage_csr = csr_ok ? 1 : 0;
-          t.stg_budget = (int)budget;
-          t.stg_cap = (int)cap;
-          const size_t need = (size_t)budget + STG_MAXS * sizeof(uint64_t);
-          if (need > dyn) dyn = need;
-        }
-      }
       t.first_cta = first;
       t.nctas = want[i];
       t.rowptr = p.rowptr; t.col = p.col; t.val = (const VT*)p.val;
@@ -1685,16 +1539,9 @@ static int run_typed(const DeviceInfo& di, const LanczosProblem* probs, int coun
       t.part = (double*)w; w += align256((size_t)3 * want[i] * MP1 * sizeof(double));
       t.Ybuf = (double*)w; w += align256((size_t)MAXM * MAXM * sizeof(double));
       t.bar = (unsigned int*)w; w += 256;
-      // staged teams work on a tile-major copy of the basis (workspace)
-      if (t.stages) {
-        t.Qw = (VT*)w;
-        t.qts = (long long)(p.m + 1) * LZ_BLOCK;
-        t.qcs = LZ_BLOCK;
-      } else {
-        t.Qw = t.Q;
-        t.qts = LZ_BLOCK;
-        t.qcs = p.ld;
-      }
+      t.Qw = t.Q;
+      t.qts = LZ_BLOCK;
+      t.qcs = p.ld;
       t.alpha = p.alpha; t.beta = p.beta; t.ctl = p.ctl; t.status = p.status;
       first += want[i];
       if (cudaMemsetAsync(t.bar, 0, 2 * sizeof(unsigned int), stream) != cudaSuccess ||
@@ -1712,10 +1559,114 @@ static int run_typed(const DeviceInfo& di, const LanczosProblem* probs, int coun
     }
     cudaError_t e = cudaLaunchCooperativeKernel((const void*)lanczos_team_kernel<VT>,
                                                 dim3(total), dim3(LZ_BLOCK), args, dyn, stream);
+    ++t_launches;
     if (e != cudaSuccess) {
       set_error("lanczos: cooperative launch of %d CTAs failed: %s", total,
                 cudaGetErrorString(e));
       return -5;
+    }
+  }
+  return 0;
+}
+
+// Stream path of one problem.  The host enqueues a cycle's steps (m - i of
+// them, one more after a breakdown), the restart and the rotation, then reads
+// the control block back once (a synchronisation of `stream`) to learn where
+// the next cycle starts and whether the loop has ended.  The loop state is
+// on the device, so a step that is not needed only returns.
+template <typename VT>
+static int run_stream(const DeviceInfo& di, const LanczosProblem& p, cudaStream_t stream) {
+  if (p.m > MAXM || p.m < 1 || p.n < 1 || p.ld < p.n) {
+    set_error("lanczos: unsupported sizes n=%d ld=%d m=%d (m must be in [1, %d])", p.n, p.ld,
+              p.m, MAXM);
+    return -2;
+  }
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(stream, &cs) != cudaSuccess || cs != cudaStreamCaptureStatusNone) {
+    set_error("lanczos: a problem of n=%d rows reads its loop state back once per restart and "
+              "cannot run inside a stream capture", p.n);
+    return -2;
+  }
+  const int ntiles = (p.n + LZ_BLOCK - 1) / LZ_BLOCK;
+  const int G = lanczos_team_size(di, p.n, sizeof(VT) == 8 ? 64 : 32);
+  TeamDesc<VT> t;
+  memset(&t, 0, sizeof(t));
+  t.n = p.n; t.ld = p.ld; t.m = p.m; t.num_desired = p.num_desired;
+  t.max_restarts = p.max_restarts; t.tol = p.tol;
+  t.lanes = lanczos_lanes(p.n, p.nnz);
+  t.first_cta = 0; t.nctas = G; t.xsmem = 0; t.nnz = p.nnz;
+  t.rowptr = p.rowptr; t.col = p.col; t.val = (const VT*)p.val;
+  t.Q = (VT*)p.Q; t.Qw = t.Q; t.qts = LZ_BLOCK; t.qcs = p.ld;
+  char* w = (char*)p.work;
+  t.vbuf = (VT*)w;
+  StreamCtl* ctl = (StreamCtl*)(t.vbuf + 2 * (size_t)p.ld);
+  w += align256(3 * (size_t)p.ld * sizeof(VT));
+  t.part = (double*)w; w += align256((size_t)3 * G * MP1 * sizeof(double));
+  t.Ybuf = (double*)w;
+  t.bar = nullptr;
+  t.alpha = p.alpha; t.beta = p.beta; t.ctl = p.ctl; t.status = p.status;
+  if (cudaMemsetAsync(ctl, 0, sizeof(StreamCtl), stream) != cudaSuccess ||
+      cudaMemsetAsync(p.ctl, 0, 16 * sizeof(int), stream) != cudaSuccess) {
+    set_error("lanczos: memset failed");
+    return -4;
+  }
+  if (p.max_restarts == 0 || p.num_desired < 1) return 0;   // no cycle runs
+  StreamCtl h;
+  int i_host = 0, bd_host = 0;
+  for (int guard = 0;; ++guard) {
+    if (guard > 4 * p.max_restarts + 16) {
+      set_error("lanczos: the stream path did not finish its %d restarts", p.max_restarts);
+      return -5;
+    }
+    const int slots = (p.m - i_host) + (bd_host ? 1 : 0);
+    for (int j = 0; j < slots; ++j) {
+      st_spmv_kernel<VT><<<ntiles, LZ_BLOCK, 0, stream>>>(t, ctl);
+      st_dot_kernel<VT><<<G, LZ_BLOCK, 0, stream>>>(t, ctl);
+      st_update_dot_kernel<VT><<<G, LZ_BLOCK, 0, stream>>>(t, ctl);
+      st_update_norm_kernel<VT><<<G, LZ_BLOCK, 0, stream>>>(t, ctl);
+    }
+    st_restart_kernel<VT><<<1, LZ_BLOCK, 0, stream>>>(t, ctl);
+    st_rotate_kernel<VT><<<G, LZ_BLOCK, 0, stream>>>(t, ctl);
+    t_launches += 4 * slots + 2;
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) {
+      set_error("lanczos: stream-path launch failed: %s", cudaGetErrorString(e));
+      return -5;
+    }
+    if (cudaMemcpyAsync(&h, ctl, sizeof(h), cudaMemcpyDeviceToHost, stream) != cudaSuccess ||
+        cudaStreamSynchronize(stream) != cudaSuccess) {
+      set_error("lanczos: stream-path state read failed: %s",
+                cudaGetErrorString(cudaGetLastError()));
+      return -5;
+    }
+    if (h.stop) break;
+    i_host = h.i;
+    bd_host = h.bd;
+  }
+  return 0;
+}
+
+// team-kernel problems (x staged in shared memory) in batched cooperative
+// launches; larger ones one after another on the stream path
+template <typename VT>
+static int run_noncluster(const DeviceInfo& di, const LanczosProblem* probs, int count,
+                          cudaStream_t stream) {
+  LanczosProblem team[MAX_TEAMS];
+  for (int base = 0; base < count; base += MAX_TEAMS) {
+    const int cnt = (count - base < MAX_TEAMS) ? (count - base) : MAX_TEAMS;
+    int nt = 0;
+    for (int i = 0; i < cnt; ++i) {
+      const LanczosProblem& p = probs[base + i];
+      if (x_fits_smem(p.n, sizeof(VT))) {
+        team[nt++] = p;
+      } else {
+        const int rc = run_stream<VT>(di, p, stream);
+        if (rc) return rc;
+      }
+    }
+    if (nt) {
+      const int rc = run_typed<VT>(di, team, nt, stream);
+      if (rc) return rc;
     }
   }
   return 0;
@@ -1786,8 +1737,8 @@ int lanczos_kernel_kind(int n, int m, int prec) {
     const char* e = getenv("USBS_LANCZOS_CLUSTER");
     return e ? atoi(e) : 1;
   }();
-  if (!enabled) return 0;
-  return (prec == 64 ? cl_fits<double>(n, m) : cl_fits<float>(n, m)) ? 1 : 0;
+  if (enabled && (prec == 64 ? cl_fits<double>(n, m) : cl_fits<float>(n, m))) return 1;
+  return x_fits_smem(n, prec == 64 ? 8 : 4) ? 0 : 2;
 }
 
 // Cluster path: every problem of the launch as one cluster of `csize` CTAs.
@@ -1866,6 +1817,7 @@ static int run_cluster(const LanczosProblem* probs, int count, cudaStream_t stre
     }
   }
   cudaError_t e = cudaLaunchKernelEx(&cfg, lanczos_cluster_kernel<VT>, batch);
+  ++t_launches;
   if (e != cudaSuccess) {
     set_error("lanczos: cluster launch (%d x %d CTAs) failed: %s", count, csize,
               cudaGetErrorString(e));
@@ -1874,17 +1826,20 @@ static int run_cluster(const LanczosProblem* probs, int count, cudaStream_t stre
   return 0;
 }
 
+int lanczos_last_launches() { return t_launches; }
+
 int lanczos_run(const DeviceInfo& di, const LanczosProblem* probs, int count, int prec,
                 cudaStream_t stream) {
+  t_launches = 0;
   if (prec == 64) {
     const int rc = run_cluster<double>(probs, count, stream);
     if (rc <= 0) return rc;
-    return run_typed<double>(di, probs, count, stream);
+    return run_noncluster<double>(di, probs, count, stream);
   }
   if (prec == 32) {
     const int rc = run_cluster<float>(probs, count, stream);
     if (rc <= 0) return rc;
-    return run_typed<float>(di, probs, count, stream);
+    return run_noncluster<float>(di, probs, count, stream);
   }
   set_error("lanczos: precision must be 32 or 64");
   return -2;
@@ -1916,6 +1871,26 @@ int lanczos_tune_entries(long long* keys, int* targets, int cap) {
 void lanczos_tune_clear() {
   std::lock_guard<std::mutex> lk(g_tune_mu);
   g_tune.clear();
+}
+
+// CTAs per SM that every partial-sum kernel of the stream path holds at once
+template <typename VT>
+static int stream_occ() {
+  const void* ks[] = {(const void*)st_dot_kernel<VT>, (const void*)st_update_dot_kernel<VT>,
+                      (const void*)st_update_norm_kernel<VT>, (const void*)st_rotate_kernel<VT>};
+  int best = 1 << 20;
+  for (const void* k : ks) {
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, LZ_BLOCK, 0) != cudaSuccess) {
+      cudaGetLastError();
+      occ = 1;
+    }
+    best = occ < best ? occ : best;
+  }
+  return best < 1 ? 1 : best;
+}
+int lanczos_stream_occupancy(int prec) {
+  return prec == 64 ? stream_occ<double>() : stream_occ<float>();
 }
 
 int lanczos_occupancy(int prec) {

@@ -951,8 +951,9 @@ struct Solver {
     lp.alpha = L.alpha; lp.beta = L.beta; lp.ctl = L.ctl; lp.status = L.status;
     lp.work = L.lz_work;
     lp.rows_per_cta = Pa->lanczos_rows_per_cta;
-    ++launches;
-    return lanczos_run(di, &lp, 1, Pa->precision, st);
+    const int rc = lanczos_run(di, &lp, 1, Pa->precision, st);
+    launches += lanczos_last_launches();
+    return rc;
   }
   // after a host sync: fold the last timed launch into the state's counters
   int collect_lanczos() {
@@ -1425,7 +1426,11 @@ extern "C" {
 
 size_t usbs_solve_workspace_bytes(const usbs_problem* P, const usbs_params* Pa) {
   DeviceInfo di;
-  if (get_device_info(&di)) { di.sm_count = 152; di.lanczos_occ64 = di.lanczos_occ32 = 4; }
+  if (get_device_info(&di)) {
+    di.sm_count = 152;
+    di.lanczos_occ64 = di.lanczos_occ32 = 4;
+    di.stream_occ64 = di.stream_occ32 = 8;
+  }
   Arena ar{nullptr, 0, 0};
   Layout L;
   plan(P, Pa, di, ar, L);
@@ -1557,6 +1562,7 @@ int usbs_solve(const usbs_problem* P, const usbs_params* Pa, usbs_state* S, void
     return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
   };
   double curr_time = 0.0;
+  bool nonfinite = false;
   auto cond = [&](int t, bool* go) -> int {
     double sc[SC_NUM];
     CK(X.read_scalars(sc, 0, SC_NUM));
@@ -1572,6 +1578,11 @@ int usbs_solve(const usbs_problem* P, const usbs_params* Pa, usbs_state* S, void
     // b . y of the current y: y_cand after a descent step (the post kernel's rule)
     r[TR_BY] = (t > 0 && sc[SC_DESCENT] != 0.0) ? sc[SC_BYC] : sc[SC_BY];
     if (cb) cb(cb_user, t);
+    // a NaN gap stops the loop as the reference's comparisons do (every one
+    // is false); the status word says why
+    if (t > 0 && !(std::isfinite(sc[SC_OBJGAP]) && std::isfinite(sc[SC_INFGAP]) &&
+                   std::isfinite(sc[SC_MAXINF]) && std::isfinite(sc[SC_PRIMAL])))
+      nonfinite = true;
     *go = (t == 0) || ((curr_time < Pa->max_time) &&
                        (sc[SC_OBJGAP] > Pa->obj_gap_eps || sc[SC_INFGAP] > Pa->infeas_gap_eps ||
                         sc[SC_MAXINF] > Pa->max_infeas_eps));
@@ -1609,7 +1620,7 @@ int usbs_solve(const usbs_problem* P, const usbs_params* Pa, usbs_state* S, void
   S->max_infeas = sc[SC_MAXINF];
   S->obj_ub = sc[SC_OBJUB];
   S->pen_dual_obj = sc[SC_PEN];
-  S->status = status[0];
+  S->status = status[0] | (nonfinite ? ST_NONFINITE : 0);
   S->elapsed = elapsed();
   S->kernel_launches = X.launches;
   return 0;
@@ -1617,7 +1628,11 @@ int usbs_solve(const usbs_problem* P, const usbs_params* Pa, usbs_state* S, void
 
 size_t usbs_cgal_workspace_bytes(const usbs_problem* P, const usbs_cgal_params* Pa) {
   DeviceInfo di;
-  if (get_device_info(&di)) { di.sm_count = 152; di.lanczos_occ64 = di.lanczos_occ32 = 4; }
+  if (get_device_info(&di)) {
+    di.sm_count = 152;
+    di.lanczos_occ64 = di.lanczos_occ32 = 4;
+    di.stream_occ64 = di.stream_occ32 = 8;
+  }
   Arena ar{nullptr, 0, 0};
   CgalLayout L;
   cgal_plan(P, Pa, di, ar, L);
@@ -1716,8 +1731,8 @@ int usbs_cgal_solve(const usbs_problem* P, const usbs_cgal_params* Pa, usbs_stat
     lp.max_restarts = Pa->lanczos_max_restarts; lp.nnz = P->nnz; lp.tol = Pa->subprob_eps;
     lp.rowptr = P->rowptr; lp.col = P->col; lp.val = L.opL; lp.Q = L.Q;
     lp.alpha = L.alpha; lp.beta = L.beta; lp.ctl = L.ctl; lp.status = L.status; lp.work = L.lz_work;
-    ++launches;
     CK(lanczos_run(di, &lp, 1, Pa->precision, st));
+    launches += lanczos_last_launches();
     ++launches;
     if (Pa->precision == 64)
       cgal_v_kernel<double><<<rgrid(L.n), 256, 0, st>>>(L.n, (const double*)L.Q, L.alpha, L.v, L.sc);

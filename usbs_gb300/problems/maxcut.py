@@ -8,6 +8,7 @@ with C = 1/4 (diag(W 1) - W) symmetrised.  The constraint tensor is the list of
 import numpy as np
 import scipy.sparse as sp
 
+from ..arrays import to_host
 from ..rng import hash_normal_matrix
 from ..state import SDPState, scale_sdp_state, unscale_sdp_state
 
@@ -122,7 +123,7 @@ def explicit_warm_start(old, W, sketch_dim, Omega=None, device="cuda"):
 
 
 def _host(x):
-    return x.detach().cpu().numpy() if hasattr(x, "detach") else np.asarray(x, float)
+    return np.asarray(to_host(x), float)
 
 
 def dual_only_warm_start(old, W, sketch_dim, Omega=None):

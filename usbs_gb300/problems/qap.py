@@ -23,6 +23,7 @@ import numpy as np
 import scipy.sparse as sp
 from scipy.sparse.linalg import eigsh
 
+from ..arrays import to_host
 from ..rng import hash_normal_matrix
 from ..state import SDPState, scale_sdp_state
 
@@ -149,7 +150,7 @@ def initialize_state(D, W, sketch_dim, Omega=None):
 # dual (the reference leaves those map entries uninitialised).
 
 def _host(x):
-    return x.detach().cpu().numpy() if hasattr(x, "detach") else np.asarray(x, float)
+    return np.asarray(to_host(x), float)
 
 
 def _index_map(a, l, num_drop):

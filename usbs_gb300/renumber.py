@@ -17,9 +17,11 @@ import numpy as np
 import scipy.sparse as sp
 from scipy.sparse.csgraph import reverse_cuthill_mckee
 
+from .arrays import to_host
+
 
 def _host(x):
-    return x.detach().cpu().numpy() if hasattr(x, "detach") else np.asarray(x)
+    return np.asarray(to_host(x))
 
 
 def rcm_permutation(C, A_indices, n):

@@ -8,15 +8,22 @@ the solves' kernels overlap on the device.
 
 A problem whose Lanczos basis fits in one thread-block cluster's shared memory
 (``usbs_lanczos_kernel`` = 1) uses cluster-scheduled kernels only, and any number
-of those run side by side. A larger problem uses the cooperative team kernel, whose
-grid is sized for the whole GPU. It therefore runs alone: it waits for the
-running solves to finish, and nothing else is admitted until it is done.
+of those run side by side; so does a problem on the stream path (kind 2, the
+largest ones), whose kernels are ordinary launches that never wait on each
+other. A mid-size problem uses the cooperative team kernel (kind 0), whose grid
+is sized for the whole GPU and must be co-resident. It therefore runs alone: it
+waits for the running solves to finish, and nothing else is admitted until it
+is done.
 
 Admission by memory: the service owns the HBM that was free when it started,
 less ``reserve_bytes``. A request's device footprint (its state and its
 ``usbs_solve`` workspace) is computed exactly at submission. The request is
 admitted only if that footprint plus the footprints of the running solves fits in
-the budget.
+the budget. A request whose footprint alone exceeds the budget can never run: it
+is rejected at submission (``wait()`` raises ``MemoryError``) instead of
+waiting forever. A request that is still queued can be withdrawn with
+``SolverService.cancel()`` (``wait()`` then raises ``RequestCancelled``); a
+solve that has started runs to its end.
 
 The reference has no serving layer. Each result is the same as a solve of that
 request alone: the kernels are deterministic and share no state between solves.
@@ -30,7 +37,11 @@ import numpy as np
 
 from . import _lib, solver
 
-__all__ = ["SolveRequest", "SolverService", "Admission", "footprint_bytes"]
+__all__ = ["SolveRequest", "SolverService", "Admission", "footprint_bytes", "RequestCancelled"]
+
+
+class RequestCancelled(RuntimeError):
+    """Raised by SolveRequest.wait() for a request withdrawn before it started."""
 
 
 class Admission:
@@ -42,6 +53,10 @@ class Admission:
         self.running = 0
         self.running_bytes = 0
         self.exclusive = False
+
+    def ever_fits(self, footprint):
+        """False for a request that exceeds the whole budget (it would never start)."""
+        return footprint <= self.budget
 
     def admissible(self, footprint, exclusive):
         if self.exclusive or self.free_slots == 0:
@@ -160,13 +175,34 @@ class SolverService:
         prm.sketch_mode = 0 if sdim else (1 if req.sdp_state.X is not None else 2)
         prm.sketch_dim = sdim
         req.footprint = footprint_bytes(host, k, sdim, prm, lib)
+        # only the cooperative team kernel (kind 0) needs the GPU to itself
         req.exclusive = lib.usbs_lanczos_kernel(n, kw["lanczos_inner_iterations"],
-                                                req.precision) != 1
+                                                req.precision) == 0
         req.arrival = time.perf_counter()
+        if not self._adm.ever_fits(req.footprint):
+            req.error = MemoryError(f"request needs {req.footprint} bytes of device memory; the "
+                                    f"service budget is {self._adm.budget}")
+            req.finish = req.arrival
+            req._host_layout = None
+            req.done.set()
+            return req
         with self._cv:
             self._queue.append(req)
             self._cv.notify_all()
         return req
+
+    def cancel(self, req):
+        """Withdraw a queued request (True); False once it has started or ended."""
+        with self._cv:
+            try:
+                self._queue.remove(req)
+            except ValueError:
+                return False
+        req.error = RequestCancelled("request cancelled before it started")
+        req.finish = time.perf_counter()
+        req._host_layout = None
+        req.done.set()
+        return True
 
     def shutdown(self):
         with self._cv:

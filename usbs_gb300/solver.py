@@ -21,6 +21,7 @@ import numpy as np
 import scipy.sparse as sp
 
 from . import _lib
+from .arrays import as_torch, to_device, to_host
 from .problem import DeviceProblem, layout
 from .rng import default_q0
 from .state import SDPState
@@ -166,20 +167,14 @@ class DeviceInstance:
         return s
 
 
-def _host(x):
-    if x is None:
-        return None
-    if hasattr(x, "detach"):
-        return x.detach().cpu().numpy()
-    return x
+_host = to_host
 
 
 def _to_dev(x, device):
-    """float64 tensor on `device` (device tensors are not routed through the host)."""
+    """float64 tensor on `device`; device arrays (torch or any DLPack producer)
+    are not routed through the host."""
     import torch
-    if isinstance(x, torch.Tensor):
-        return x.to(device=device, dtype=torch.float64)
-    return torch.as_tensor(np.asarray(x, dtype=np.float64), device=device)
+    return to_device(x, torch.float64, device)
 
 
 def _dev_cols(x, rows, ld, cols, device, dtype):
@@ -187,7 +182,9 @@ def _dev_cols(x, rows, ld, cols, device, dtype):
     import torch
     out = torch.zeros((cols, ld), dtype=dtype, device=device)
     if x is not None:
-        xt = x if isinstance(x, torch.Tensor) else torch.as_tensor(np.asarray(x))
+        xt = as_torch(x)
+        if xt is None:
+            xt = torch.as_tensor(np.asarray(x))
         out[:, :rows] = xt.to(device=device, dtype=dtype).reshape(rows, cols).t()
     return out
 

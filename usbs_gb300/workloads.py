@@ -121,6 +121,16 @@ def serving_stream(num_requests=1024, rate=20.0, seed=4, n_lo=200, n_hi=50000, d
     return reqs
 
 
+def graph_from_spec(spec):
+    """("er", n, edges, seed) or ("torus_unit", side): the graphs named in
+    recorded solves."""
+    if spec[0] == "er":
+        return er_graph(int(spec[1]), int(spec[2]), int(spec[3]))
+    if spec[0] == "torus_unit":
+        return torus_graph(int(spec[1]), 0, weights="unit")
+    raise ValueError(f"unknown graph spec {spec!r}")
+
+
 def stream_adjacency(req):
     n = req["n"]
     A = sp.coo_matrix((np.ones(req["i"].size), (req["i"], req["j"])), shape=(n, n)).tocsr()
