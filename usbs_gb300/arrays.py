@@ -39,3 +39,9 @@ def to_host(x):
     if t is not None:
         return t.detach().cpu().numpy()
     return x
+
+
+def shape_of(x):
+    """The shape of a NumPy array, torch tensor or DLPack producer."""
+    t = as_torch(x)
+    return tuple(t.shape) if t is not None else np.shape(x)

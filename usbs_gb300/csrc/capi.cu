@@ -176,7 +176,7 @@ size_t usbs_eigsh_workspace_bytes(int n, long long nnz, int inner_iterations, in
   const int nctas = lanczos_team_size(di, n, precision);
   size_t b = a256((size_t)(nnz > 0 ? nnz : 1) * vt);
   b += a256(2 * MAXM * sizeof(double));
-  b += lanczos_workspace_bytes(n, ld, inner_iterations, precision, nctas);
+  b += lanczos_workspace_bytes(n, nnz, ld, inner_iterations, precision, nctas);
   return b;
 }
 

@@ -38,7 +38,7 @@ struct LanczosProblem {
   void* work;           // workspace of lanczos_workspace_bytes()
   int rows_per_cta = 0; // cluster path: rows per CTA (0: measured class choice or default)
 };
-size_t lanczos_workspace_bytes(int n, int ld, int m, int prec, int nctas);
+size_t lanczos_workspace_bytes(int n, long long nnz, int ld, int m, int prec, int nctas);
 int lanczos_team_size(const DeviceInfo& di, int n, int prec);
 int lanczos_lanes(int n, long long nnz);
 int lanczos_occupancy(int prec);

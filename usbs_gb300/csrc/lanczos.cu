@@ -48,6 +48,14 @@ struct TeamDesc {
   // tile stride LZ_BLOCK, column stride ld)
   VT* Qw;
   long long qts, qcs;    // tile and column strides (elements)
+  // stream path: the operator in a sliced-ELL layout built on the device (rows
+  // of each 256-row window sorted by length, 32-row slices, each slice
+  // holding at most wcap entries per row; longer rows finish from the CSR)
+  int wcap;
+  int* sl_w;             // width of each slice
+  unsigned char* sl_row; // sorted position -> row offset inside its window
+  int* sl_col;           // slice s: entries from s * 32 * wcap, column-major
+  VT* sl_val;
   VT* vbuf;              // 3 flat vectors: two work vectors, then Q[:, k] of the cycle
   double* part;
   double* Ybuf;
@@ -665,8 +673,9 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
 // Problems whose x does not fit in shared memory (n * sizeof(VT) > 160 KB) run
 // as a sequence of ordinary full-GPU launches instead of one cooperative
 // launch: every Lanczos step is
-//   A1  y = Op x for one 256-row tile per CTA (L lanes per row), x = v * 1/beta
-//       folded in; also stores Q[:, i] = x          (no partial sums)
+//   A1  y = Op x for one 256-row window per CTA on a sliced-ELL copy of the
+//       operator built at the call's start, x = v * 1/beta folded in; also
+//       stores Q[:, i] = x                           (no partial sums)
 //   A2  h1 = Q[:, :i+1]^T y                          (partials, last-CTA sum)
 //   B   q1 = y - Q h1,  h2 = Q^T q1                  (partials, last-CTA sum)
 //   C   q2 = q1 - Q h2, ||q2||^2                     (partials, last-CTA sum)
@@ -698,7 +707,7 @@ struct StShared {
       double ys[LZ_BLOCK];
       double wred[LZ_NW][MP1];
     } st;
-    VT Ys[MAXM * MAXM];
+    __align__(16) VT Ys[MAXM * MAXM];
   } u;
   double h[MP1];
   VT hv[MP1];
@@ -747,18 +756,192 @@ __device__ __forceinline__ void st_reduce(const double* part, int R, int nv, SH&
   __syncthreads();
 }
 
-// A1: one tile per CTA.  Step: vbuf[cur] = Op x, x = (i == k ? Q[:, k] :
-// vbuf[cur ^ 1] / beta), and Q[:, i] = x when i > k.  Breakdown: vbuf[cur ^ 1]
-// = a Gaussian vector keyed by i (the replacement of solver/lanczos.py:107-117).
+// ---- vector helpers of the Q-streaming kernels ----
+// 4 consecutive rows of a column (16-byte aligned: ld is a multiple of 32 and
+// the first row a multiple of 4); rows at or past n read as 0.  The basis is
+// read through the read-only path (no stream kernel writes a column it
+// reads); the work vectors, which B and C update, through L2.
+template <typename VT> struct Row4 { VT v[4]; };
+template <typename VT, bool RO = true>
+__device__ __forceinline__ Row4<VT> ld4(const VT* p, int r4, int n) {
+  Row4<VT> o;
+  if (r4 + 4 <= n) {
+    if constexpr (sizeof(VT) == 4) {
+      const float4 a = RO ? __ldg((const float4*)(p + r4)) : __ldcg((const float4*)(p + r4));
+      o.v[0] = a.x; o.v[1] = a.y; o.v[2] = a.z; o.v[3] = a.w;
+    } else {
+      const double2 a = RO ? __ldg((const double2*)(p + r4)) : __ldcg((const double2*)(p + r4));
+      const double2 b =
+          RO ? __ldg((const double2*)(p + r4 + 2)) : __ldcg((const double2*)(p + r4 + 2));
+      o.v[0] = a.x; o.v[1] = a.y; o.v[2] = b.x; o.v[3] = b.y;
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      o.v[j] = (r4 + j < n) ? (RO ? __ldg(p + r4 + j) : __ldcg(p + r4 + j)) : (VT)0;
+  }
+  return o;
+}
 template <typename VT>
-__global__ void __launch_bounds__(LZ_BLOCK) st_spmv_kernel(const __grid_constant__ TeamDesc<VT> P,
-                                                            StreamCtl* ctl) {
-  __shared__ StShared<VT> sh;
+__device__ __forceinline__ void st4(VT* p, int r4, int n, const Row4<VT>& o) {
+  if (r4 + 4 <= n) {
+    if constexpr (sizeof(VT) == 4) {
+      *(float4*)(p + r4) = make_float4(o.v[0], o.v[1], o.v[2], o.v[3]);
+    } else {
+      *(double2*)(p + r4) = make_double2(o.v[0], o.v[1]);
+      *(double2*)(p + r4 + 2) = make_double2(o.v[2], o.v[3]);
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (r4 + j < n) p[r4 + j] = o.v[j];
+  }
+}
+
+constexpr int ST_ROWS = 4 * LZ_BLOCK;   // rows of one chunk (4 per thread)
+// column loads issued before any is used: 128 bytes per thread either way
+template <typename VT> constexpr int st_batch() { return sizeof(VT) == 4 ? 8 : 4; }
+
+// s = sum_{c < nv} Q[r4.., c] * hv[c] for a thread's 4 rows, in column
+// order, st_batch() column loads in flight at a time
+template <typename VT>
+__device__ __forceinline__ Row4<VT> st_combine(const VT* Q, size_t ld, int r4, int n, int nv,
+                                               const VT* hv) {
+  constexpr int NB = st_batch<VT>();
+  Row4<VT> s;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) s.v[j] = (VT)0;
+#pragma unroll 1
+  for (int c0 = 0; c0 < nv; c0 += NB) {
+    Row4<VT> q[NB];
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+      if (c0 + b < nv) q[b] = ld4(Q + (size_t)(c0 + b) * ld, r4, n);
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+      if (c0 + b < nv) {
+        const VT h = hv[c0 + b];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) s.v[j] += q[b].v[j] * h;
+      }
+  }
+  return s;
+}
+
+// sacc[c][tid] += sum_j Q[r4 + j, c] * x.v[j], c < nv (a per-thread column of
+// shared memory), st_batch() loads in flight at a time
+template <typename VT, typename AT>
+__device__ __forceinline__ void st_dots(const VT* Q, size_t ld, int r4, int n, int nv,
+                                        const Row4<VT>& x, AT* sacc) {
+  constexpr int NB = st_batch<VT>();
+#pragma unroll 1
+  for (int c0 = 0; c0 < nv; c0 += NB) {
+    Row4<VT> q[NB];
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+      if (c0 + b < nv) q[b] = ld4(Q + (size_t)(c0 + b) * ld, r4, n);
+#pragma unroll
+    for (int b = 0; b < NB; ++b)
+      if (c0 + b < nv) {
+        AT d = (AT)0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j) d += (AT)q[b].v[j] * (AT)x.v[j];
+        sacc[(c0 + b) * LZ_BLOCK + threadIdx.x] += d;
+      }
+  }
+}
+
+// out[c * R] = sum over the CTA's threads of sacc[c][t], c < nv: warp w takes
+// columns w, w + 8, ...; lane l sums threads l, l + 32, ... in order
+template <typename AT>
+__device__ __forceinline__ void st_block_cols(const AT* sacc, int nv, double* out, int R) {
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int c = w; c < nv; c += LZ_NW) {
+    AT a = (AT)0;
+#pragma unroll
+    for (int k = 0; k < LZ_BLOCK / 32; ++k) a += sacc[c * LZ_BLOCK + lane + 32 * k];
+    a = warp_sum(a);
+    if (lane == 0) out[(size_t)c * R] = (double)a;
+  }
+}
+
+// the per-thread dot accumulators of A2 and B (dynamic shared memory)
+template <typename VT>
+constexpr size_t st_sacc_bytes() {
+  return (size_t)MP1 * LZ_BLOCK * sizeof(typename Acc<VT>::type);
+}
+
+// chunk range [c0, c1) of ST_ROWS-row chunks of this CTA
+__device__ __forceinline__ void st_chunks(int n, int* c0, int* c1) {
+  const int nch = (n + ST_ROWS - 1) / ST_ROWS, R = gridDim.x;
+  *c0 = (int)((long long)nch * blockIdx.x / R);
+  *c1 = (int)((long long)nch * (blockIdx.x + 1) / R);
+}
+
+// ---- the stream path's operator layout (built once per call) ----
+// Rows of each 256-row window are ordered by length (longest first, then by
+// row) and cut into 32-row slices; slice s keeps entry k of its lane-th row at
+// s * 32 * wcap + 32 k + lane (k < the slice's width, at most wcap; shorter
+// rows are padded with column 0, value 0; rows longer than wcap finish from
+// the CSR).  One CTA per window: each thread ranks its row against the
+// window's others.
+template <typename VT>
+__global__ void __launch_bounds__(LZ_BLOCK) st_sell_build_kernel(
+    const __grid_constant__ TeamDesc<VT> P) {
+  __shared__ int len[LZ_BLOCK];
+  __shared__ int order[LZ_BLOCK];
+  const int w0 = blockIdx.x * LZ_BLOCK, tid = threadIdx.x, r = w0 + tid;
+  const int rows = min(LZ_BLOCK, P.n - w0);
+  len[tid] = (r < P.n) ? P.rowptr[r + 1] - P.rowptr[r] : -1;
+  __syncthreads();
+  if (tid < rows) {
+    const int mine = len[tid];
+    int rank = 0;
+    for (int j = 0; j < rows; ++j) {
+      const int lj = len[j];
+      rank += (lj > mine || (lj == mine && j < tid)) ? 1 : 0;
+    }
+    order[rank] = tid;
+  }
+  __syncthreads();
+  // thread p: sorted position p of the window (slice p / 32, lane p % 32).  A
+  // slice that exists (s < ceil(n / 32)) has a real row at its first position.
+  const int p = tid, s = blockIdx.x * (LZ_BLOCK / 32) + p / 32, lane = p & 31;
+  if (s >= (P.n + 31) / 32) return;
+  const int w = min(len[order[p & ~31]], P.wcap);
+  if (lane == 0) P.sl_w[s] = w;
+  const bool real = p < rows;
+  const int lr = real ? order[p] : p;          // padding lanes: unused positions
+  P.sl_row[32 * s + lane] = (unsigned char)lr;
+  const int lenr = real ? len[lr] : 0;
+  const int b = real ? P.rowptr[w0 + lr] : 0;
+  int* cdst = P.sl_col + (size_t)s * 32 * P.wcap + lane;
+  VT* vdst = P.sl_val + (size_t)s * 32 * P.wcap + lane;
+  for (int k = 0; k < w; ++k) {
+    const bool e = k < lenr;
+    cdst[32 * k] = e ? P.col[b + k] : 0;
+    vdst[32 * k] = e ? P.val[b + k] : (VT)0;
+  }
+}
+
+// A1: y = Op x on the sliced-ELL layout, one CTA per window, one warp per
+// slice, lane = row: the first 16 entries' column / value loads, then their x
+// gathers, all in flight at once.  Step: vbuf[cur] = Op x with x = (i == k ?
+// Q[:, k] : vbuf[cur ^ 1] / beta), and Q[:, i] = x when i > k.  Breakdown:
+// vbuf[cur ^ 1] = a Gaussian vector keyed by i (the replacement of
+// solver/lanczos.py:107-117).  x is not written here, so it is gathered
+// through the read-only (L1) path.
+template <typename VT>
+__global__ void __launch_bounds__(LZ_BLOCK, 8) st_sell_spmv_kernel(
+    const __grid_constant__ TeamDesc<VT> P, StreamCtl* ctl) {
+  typedef typename Acc<VT>::type AT;
+  __shared__ VT ys[LZ_BLOCK];
   int i, nv, buf;
   const int mode = st_mode(ctl, P.m, &i, &nv, &buf);
   if (mode == SM_SKIP) return;
   const size_t ld = (size_t)P.ld;
-  const int base = blockIdx.x * LZ_BLOCK, row = base + threadIdx.x;
+  const int w0 = blockIdx.x * LZ_BLOCK, row = w0 + threadIdx.x;
   if (mode == SM_BREAKDOWN) {
     if (row < P.n) P.vbuf[(size_t)buf * ld + row] = (VT)hash_normal((uint64_t)i, (uint64_t)row);
     return;
@@ -766,19 +949,41 @@ __global__ void __launch_bounds__(LZ_BLOCK) st_spmv_kernel(const __grid_constant
   const int k = __ldcg(&ctl->k);
   const bool wq = i > k;
   const VT xscale = wq ? (VT)__ldcg(&ctl->invb) : (VT)1;
-  const VT* xsrc = wq ? P.vbuf + (size_t)(buf ^ 1) * ld : P.Q + (size_t)k * ld;
-  switch (P.lanes) {
-    case 1: spmv_tile<VT, 1>(P, sh, base, xsrc, xsrc, false); break;
-    case 2: spmv_tile<VT, 2>(P, sh, base, xsrc, xsrc, false); break;
-    case 4: spmv_tile<VT, 4>(P, sh, base, xsrc, xsrc, false); break;
-    case 8: spmv_tile<VT, 8>(P, sh, base, xsrc, xsrc, false); break;
-    case 16: spmv_tile<VT, 16>(P, sh, base, xsrc, xsrc, false); break;
-    default: spmv_tile<VT, 32>(P, sh, base, xsrc, xsrc, false); break;
+  const VT* __restrict__ x = wq ? P.vbuf + (size_t)(buf ^ 1) * ld : P.Q + (size_t)k * ld;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int s = blockIdx.x * (LZ_BLOCK / 32) + warp;
+  if (s < (P.n + 31) / 32) {
+    const int width = P.sl_w[s];
+    const int* cp = P.sl_col + (size_t)s * 32 * P.wcap + lane;
+    const VT* vp = P.sl_val + (size_t)s * 32 * P.wcap + lane;
+    constexpr int PF = 16;
+    int c[PF];
+    VT v[PF], xv[PF];
+#pragma unroll
+    for (int u = 0; u < PF; ++u) {
+      c[u] = (u < width) ? __ldg(cp + 32 * u) : 0;
+      v[u] = (u < width) ? __ldg(vp + 32 * u) : (VT)0;
+    }
+#pragma unroll
+    for (int u = 0; u < PF; ++u) xv[u] = (u < width) ? __ldg(x + c[u]) : (VT)0;
+    AT acc = (AT)0;
+#pragma unroll
+    for (int u = 0; u < PF; ++u) acc += (AT)v[u] * (AT)xv[u];
+    for (int u = PF; u < width; ++u) acc += (AT)__ldg(vp + 32 * u) * (AT)__ldg(x + __ldg(cp + 32 * u));
+    const int lr = P.sl_row[32 * s + lane];
+    const int r = w0 + lr;
+    if (r < P.n && width == P.wcap) {
+      // the rest of a row longer than the slice capacity
+      const int e = P.rowptr[r + 1];
+      for (int q = P.rowptr[r] + P.wcap; q < e; ++q)
+        acc += (AT)__ldg(P.val + q) * (AT)__ldg(x + __ldg(P.col + q));
+    }
+    ys[lr] = (VT)acc;
   }
   __syncthreads();
   if (row < P.n) {
-    P.vbuf[(size_t)buf * ld + row] = (VT)sh.u.st.ys[threadIdx.x] * xscale;
-    if (wq) P.Q[(size_t)i * ld + row] = __ldcg(xsrc + row) * xscale;
+    P.vbuf[(size_t)buf * ld + row] = ys[threadIdx.x] * xscale;
+    if (wq) P.Q[(size_t)i * ld + row] = __ldg(x + row) * xscale;
   }
 }
 
@@ -790,44 +995,57 @@ __global__ void __launch_bounds__(LZ_BLOCK) st_dot_kernel(const __grid_constant_
   __shared__ StShared<VT> sh;
   int i, nv, buf;
   if (st_mode(ctl, P.m, &i, &nv, &buf) == SM_SKIP) return;
-  const int R = gridDim.x, ntiles = (P.n + LZ_BLOCK - 1) / LZ_BLOCK;
-  const int t0 = (int)((long long)ntiles * blockIdx.x / R);
-  const int t1 = (int)((long long)ntiles * (blockIdx.x + 1) / R);
-  const VT* v = P.vbuf + (size_t)buf * P.ld;
-  AT acc[MP1];
-#pragma unroll
-  for (int c = 0; c < MP1; ++c) acc[c] = (AT)0;
-  for (int tile = t0; tile < t1; ++tile) {
-    const int row = tile * LZ_BLOCK + threadIdx.x;
-    if (row < P.n) {
-      const VT y = v[row];
-#pragma unroll
-      for (int c = 0; c < MP1; ++c)
-        if (c < nv) acc[c] += (AT)P.Q[(size_t)c * P.ld + row] * (AT)y;
-    }
+  const int R = gridDim.x;
+  const size_t ld = (size_t)P.ld;
+  int c0, c1;
+  st_chunks(P.n, &c0, &c1);
+  const VT* v = P.vbuf + (size_t)buf * ld;
+  extern __shared__ __align__(16) unsigned char st_dyn[];
+  AT* sacc = (AT*)st_dyn;
+  for (int c = 0; c < nv; ++c) sacc[c * LZ_BLOCK + threadIdx.x] = (AT)0;
+  for (int ch = c0; ch < c1; ++ch) {
+    const int r4 = ch * ST_ROWS + 4 * threadIdx.x;
+    if (r4 < P.n) st_dots(P.Q, ld, r4, P.n, nv, ld4<VT, false>(v, r4, P.n), sacc);
   }
-  block_reduce_cols(acc, nv, sh, P.part + blockIdx.x, R);
+  st_block_cols(sacc, nv, P.part + blockIdx.x, R);
   if (!st_last_cta(&ctl->ticket[0], sh)) return;
   st_reduce<VT>(P.part, R, nv, sh);
   for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) ctl->h1[c] = sh.h[c];
   if (threadIdx.x == 0) ctl->ticket[0] = 0u;
 }
 
-// B: v -= Q h1 (c < nv), h2 = Q^T v; on a step, alpha[i] = h1[i] + h2[i]
+// B: v -= Q h1 (c < nv), h2 = Q^T v; on a step, alpha[i] = h1[i] + h2[i].  The
+// dots re-read the thread's rows of Q, by then in L1 or L2.
 template <typename VT>
-__global__ void __launch_bounds__(LZ_BLOCK) st_update_dot_kernel(
+__global__ void __launch_bounds__(LZ_BLOCK, 3) st_update_dot_kernel(
     const __grid_constant__ TeamDesc<VT> P, StreamCtl* ctl) {
+  typedef typename Acc<VT>::type AT;
   __shared__ StShared<VT> sh;
   int i, nv, buf;
   const int mode = st_mode(ctl, P.m, &i, &nv, &buf);
   if (mode == SM_SKIP) return;
-  const int R = gridDim.x, ntiles = (P.n + LZ_BLOCK - 1) / LZ_BLOCK;
-  const int t0 = (int)((long long)ntiles * blockIdx.x / R);
-  const int t1 = (int)((long long)ntiles * (blockIdx.x + 1) / R);
+  const int R = gridDim.x;
+  const size_t ld = (size_t)P.ld;
   for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) sh.hv[c] = (VT)__ldcg(&ctl->h1[c]);
   __syncthreads();
+  int c0, c1;
+  st_chunks(P.n, &c0, &c1);
+  VT* v = P.vbuf + (size_t)buf * ld;
+  extern __shared__ __align__(16) unsigned char st_dyn[];
+  AT* sacc = (AT*)st_dyn;
+  for (int c = 0; c < nv; ++c) sacc[c * LZ_BLOCK + threadIdx.x] = (AT)0;
+  for (int ch = c0; ch < c1; ++ch) {
+    const int r4 = ch * ST_ROWS + 4 * threadIdx.x;
+    if (r4 >= P.n) continue;
+    Row4<VT> x = ld4<VT, false>(v, r4, P.n);
+    const Row4<VT> s = st_combine(P.Q, ld, r4, P.n, nv, sh.hv);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) x.v[j] -= s.v[j];
+    st4(v, r4, P.n, x);
+    st_dots(P.Q, ld, r4, P.n, nv, x, sacc);
+  }
   double* part = P.part + (size_t)MP1 * R;
-  phase_update_dot(P, sh, t0, t1, nv, P.vbuf + (size_t)buf * P.ld, part + blockIdx.x);
+  st_block_cols(sacc, nv, part + blockIdx.x, R);
   if (!st_last_cta(&ctl->ticket[1], sh)) return;
   st_reduce<VT>(part, R, nv, sh);
   for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) ctl->h2[c] = sh.h[c];
@@ -841,17 +1059,34 @@ __global__ void __launch_bounds__(LZ_BLOCK) st_update_dot_kernel(
 template <typename VT>
 __global__ void __launch_bounds__(LZ_BLOCK) st_update_norm_kernel(
     const __grid_constant__ TeamDesc<VT> P, StreamCtl* ctl) {
+  typedef typename Acc<VT>::type AT;
   __shared__ StShared<VT> sh;
   int i, nv, buf;
   const int mode = st_mode(ctl, P.m, &i, &nv, &buf);
   if (mode == SM_SKIP) return;
-  const int R = gridDim.x, ntiles = (P.n + LZ_BLOCK - 1) / LZ_BLOCK;
-  const int t0 = (int)((long long)ntiles * blockIdx.x / R);
-  const int t1 = (int)((long long)ntiles * (blockIdx.x + 1) / R);
+  const int R = gridDim.x;
+  const size_t ld = (size_t)P.ld;
   for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) sh.hv[c] = (VT)__ldcg(&ctl->h2[c]);
   __syncthreads();
+  int c0, c1;
+  st_chunks(P.n, &c0, &c1);
+  VT* v = P.vbuf + (size_t)buf * ld;
+  AT nrm[MP1];
+  nrm[0] = (AT)0;
+  for (int ch = c0; ch < c1; ++ch) {
+    const int r4 = ch * ST_ROWS + 4 * threadIdx.x;
+    if (r4 >= P.n) continue;
+    Row4<VT> x = ld4<VT, false>(v, r4, P.n);
+    const Row4<VT> s = st_combine(P.Q, ld, r4, P.n, nv, sh.hv);
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      x.v[j] -= s.v[j];
+      nrm[0] += (AT)x.v[j] * (AT)x.v[j];
+    }
+    st4(v, r4, P.n, x);
+  }
   double* part = P.part + (size_t)2 * MP1 * R;
-  phase_update_norm(P, sh, t0, t1, nv, P.vbuf + (size_t)buf * P.ld, part + blockIdx.x);
+  block_reduce_cols(nrm, 1, sh, part + blockIdx.x, R);
   if (!st_last_cta(&ctl->ticket[2], sh)) return;
   st_reduce<VT>(part, R, 1, sh);
   if (threadIdx.x == 0) {
@@ -940,13 +1175,28 @@ __global__ void __launch_bounds__(LZ_BLOCK) st_rotate_kernel(const __grid_consta
 #pragma unroll
       for (int j = 0; j < MAXM; ++j) qr[j] = (j < m) ? P.Q[(size_t)j * ld + row] : (VT)0;
       const VT xl = stepped ? lastv[row] * invb : P.Q[(size_t)m * ld + row];
-      for (int c = 0; c < kn; ++c) {
-        if (c >= m) break;
-        VT s = (VT)0;
+      // four output columns per pass, their Y entries read together (Y is
+      // zero past column kn, so the last pass may overrun kn harmlessly)
+      for (int c0 = 0; c0 < kn; c0 += 4) {
+        VT s[4] = {(VT)0, (VT)0, (VT)0, (VT)0};
 #pragma unroll
         for (int j = 0; j < MAXM; ++j)
-          if (j < m) s += qr[j] * sh.u.Ys[j * MAXM + c];
-        P.Q[(size_t)c * ld + row] = s;
+          if (j < m) {
+            VT y4[4];
+            if constexpr (sizeof(VT) == 4) {
+              const float4 a = *(const float4*)&sh.u.Ys[j * MAXM + c0];
+              y4[0] = a.x; y4[1] = a.y; y4[2] = a.z; y4[3] = a.w;
+            } else {
+              const double2 a = *(const double2*)&sh.u.Ys[j * MAXM + c0];
+              const double2 b = *(const double2*)&sh.u.Ys[j * MAXM + c0 + 2];
+              y4[0] = a.x; y4[1] = a.y; y4[2] = b.x; y4[3] = b.y;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) s[u] += qr[j] * y4[u];
+          }
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+          if (c0 + u < kn) P.Q[(size_t)(c0 + u) * ld + row] = s[u];
       }
       P.Q[(size_t)kn * ld + row] = xl;
       if (kn != m) P.Q[(size_t)m * ld + row] = xl;
@@ -1432,13 +1682,27 @@ static bool x_fits_smem(int n, size_t vt) { return (size_t)n * vt <= (size_t)LZ_
 // and the barrier counters.  Stream path (nctas = its grid): 2 work vectors
 // and the control block in the third vector's place, the same partials and
 // Ritz vectors.
-size_t lanczos_workspace_bytes(int n, int ld, int m, int prec, int nctas) {
-  (void)n; (void)m;
+// entries per row a stream-path slice holds (longer rows finish from the CSR)
+static int sell_wcap(int n, long long nnz) {
+  const long long avg = n > 0 ? (nnz + n - 1) / n : 1;
+  const long long w = avg + avg / 2 + 2;
+  return (int)(w < 4 ? 4 : (w > 64 ? 64 : w));
+}
+static size_t sell_bytes(int n, long long nnz, size_t vt) {
+  const size_t ns = ((size_t)n + 31) / 32;
+  return align256(ns * sizeof(int)) + align256(ns * 32) +
+         align256(ns * 32 * (size_t)sell_wcap(n, nnz) * sizeof(int)) +
+         align256(ns * 32 * (size_t)sell_wcap(n, nnz) * vt);
+}
+
+size_t lanczos_workspace_bytes(int n, long long nnz, int ld, int m, int prec, int nctas) {
+  (void)m;
   const size_t vt = (prec == 64) ? 8 : 4;
   size_t b = align256(3 * (size_t)ld * vt);
   b += align256((size_t)3 * nctas * MP1 * sizeof(double));
   b += align256((size_t)MAXM * MAXM * sizeof(double));
   b += 256;  // barrier counters
+  if (!x_fits_smem(n, vt)) b += sell_bytes(n, nnz, vt);
   return b;
 }
 static_assert(sizeof(StreamCtl) <= 32 * 4 * 32, "the control block takes one 32-row vector slot");
@@ -1569,6 +1833,40 @@ static int run_typed(const DeviceInfo& di, const LanczosProblem* probs, int coun
   return 0;
 }
 
+// CTAs per SM of each partial-sum kernel of the stream path (A2, B, C, the
+// rotation), measured once per precision; each kernel runs one wave of its
+// own size.  Sets the dot kernels' dynamic shared memory limit on the way.
+template <typename VT>
+static const int* stream_occ() {
+  static int occ[4] = {0, 0, 0, 0};
+  static std::once_flag once;
+  std::call_once(once, [] {
+    const void* ks[] = {(const void*)st_dot_kernel<VT>, (const void*)st_update_dot_kernel<VT>,
+                        (const void*)st_update_norm_kernel<VT>,
+                        (const void*)st_rotate_kernel<VT>};
+    const size_t dyn[] = {st_sacc_bytes<VT>(), st_sacc_bytes<VT>(), 0, 0};
+    for (int j = 0; j < 4; ++j) {
+      if (dyn[j])
+        cudaFuncSetAttribute(ks[j], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn[j]);
+      int o = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, ks[j], LZ_BLOCK, dyn[j]) !=
+          cudaSuccess) {
+        cudaGetLastError();
+        o = 1;
+      }
+      occ[j] = o < 1 ? 1 : o;
+    }
+  });
+  return occ;
+}
+// the largest of them (sizes the partial-sum buffers)
+int lanczos_stream_occupancy(int prec) {
+  const int* o = prec == 64 ? stream_occ<double>() : stream_occ<float>();
+  int b = 1;
+  for (int j = 0; j < 4; ++j) b = o[j] > b ? o[j] : b;
+  return b;
+}
+
 // Stream path of one problem.  The host enqueues a cycle's steps (m - i of
 // them, one more after a breakdown), the restart and the rotation, then reads
 // the control block back once (a synchronisation of `stream`) to learn where
@@ -1588,7 +1886,14 @@ static int run_stream(const DeviceInfo& di, const LanczosProblem& p, cudaStream_
     return -2;
   }
   const int ntiles = (p.n + LZ_BLOCK - 1) / LZ_BLOCK;
-  const int G = lanczos_team_size(di, p.n, sizeof(VT) == 8 ? 64 : 32);
+  const int G = lanczos_team_size(di, p.n, sizeof(VT) == 8 ? 64 : 32);   // partials per pass
+  const int* occ = stream_occ<VT>();
+  int g[4];
+  for (int j = 0; j < 4; ++j) {
+    g[j] = di.sm_count * occ[j];
+    if (g[j] > G) g[j] = G;
+    if (g[j] < 1) g[j] = 1;
+  }
   TeamDesc<VT> t;
   memset(&t, 0, sizeof(t));
   t.n = p.n; t.ld = p.ld; t.m = p.m; t.num_desired = p.num_desired;
@@ -1602,9 +1907,18 @@ static int run_stream(const DeviceInfo& di, const LanczosProblem& p, cudaStream_
   StreamCtl* ctl = (StreamCtl*)(t.vbuf + 2 * (size_t)p.ld);
   w += align256(3 * (size_t)p.ld * sizeof(VT));
   t.part = (double*)w; w += align256((size_t)3 * G * MP1 * sizeof(double));
-  t.Ybuf = (double*)w;
+  t.Ybuf = (double*)w; w += align256((size_t)MAXM * MAXM * sizeof(double));
   t.bar = nullptr;
+  w += 256;
+  const int ns = (p.n + 31) / 32;
+  t.wcap = sell_wcap(p.n, p.nnz);
+  t.sl_w = (int*)w; w += align256((size_t)ns * sizeof(int));
+  t.sl_row = (unsigned char*)w; w += align256((size_t)ns * 32);
+  t.sl_col = (int*)w; w += align256((size_t)ns * 32 * t.wcap * sizeof(int));
+  t.sl_val = (VT*)w;
   t.alpha = p.alpha; t.beta = p.beta; t.ctl = p.ctl; t.status = p.status;
+  st_sell_build_kernel<VT><<<ntiles, LZ_BLOCK, 0, stream>>>(t);
+  t_launches += 1;
   if (cudaMemsetAsync(ctl, 0, sizeof(StreamCtl), stream) != cudaSuccess ||
       cudaMemsetAsync(p.ctl, 0, 16 * sizeof(int), stream) != cudaSuccess) {
     set_error("lanczos: memset failed");
@@ -1620,13 +1934,13 @@ static int run_stream(const DeviceInfo& di, const LanczosProblem& p, cudaStream_
     }
     const int slots = (p.m - i_host) + (bd_host ? 1 : 0);
     for (int j = 0; j < slots; ++j) {
-      st_spmv_kernel<VT><<<ntiles, LZ_BLOCK, 0, stream>>>(t, ctl);
-      st_dot_kernel<VT><<<G, LZ_BLOCK, 0, stream>>>(t, ctl);
-      st_update_dot_kernel<VT><<<G, LZ_BLOCK, 0, stream>>>(t, ctl);
-      st_update_norm_kernel<VT><<<G, LZ_BLOCK, 0, stream>>>(t, ctl);
+      st_sell_spmv_kernel<VT><<<ntiles, LZ_BLOCK, 0, stream>>>(t, ctl);
+      st_dot_kernel<VT><<<g[0], LZ_BLOCK, st_sacc_bytes<VT>(), stream>>>(t, ctl);
+      st_update_dot_kernel<VT><<<g[1], LZ_BLOCK, st_sacc_bytes<VT>(), stream>>>(t, ctl);
+      st_update_norm_kernel<VT><<<g[2], LZ_BLOCK, 0, stream>>>(t, ctl);
     }
     st_restart_kernel<VT><<<1, LZ_BLOCK, 0, stream>>>(t, ctl);
-    st_rotate_kernel<VT><<<G, LZ_BLOCK, 0, stream>>>(t, ctl);
+    st_rotate_kernel<VT><<<g[3], LZ_BLOCK, 0, stream>>>(t, ctl);
     t_launches += 4 * slots + 2;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
@@ -1871,26 +2185,6 @@ int lanczos_tune_entries(long long* keys, int* targets, int cap) {
 void lanczos_tune_clear() {
   std::lock_guard<std::mutex> lk(g_tune_mu);
   g_tune.clear();
-}
-
-// CTAs per SM that every partial-sum kernel of the stream path holds at once
-template <typename VT>
-static int stream_occ() {
-  const void* ks[] = {(const void*)st_dot_kernel<VT>, (const void*)st_update_dot_kernel<VT>,
-                      (const void*)st_update_norm_kernel<VT>, (const void*)st_rotate_kernel<VT>};
-  int best = 1 << 20;
-  for (const void* k : ks) {
-    int occ = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k, LZ_BLOCK, 0) != cudaSuccess) {
-      cudaGetLastError();
-      occ = 1;
-    }
-    best = occ < best ? occ : best;
-  }
-  return best < 1 ? 1 : best;
-}
-int lanczos_stream_occupancy(int prec) {
-  return prec == 64 ? stream_occ<double>() : stream_occ<float>();
 }
 
 int lanczos_occupancy(int prec) {

@@ -788,7 +788,7 @@ static int plan(const usbs_problem* P, const usbs_params* Pa, const DeviceInfo& 
   L.ctl = L.status + 16;
   L.skip = ar.take<int>(4);
   const int nct = lanczos_team_size(di, L.n, Pa->precision);
-  L.lz_work = ar.take<char>(lanczos_workspace_bytes(L.n, L.ld, L.mL, Pa->precision, nct));
+  L.lz_work = ar.take<char>(lanczos_workspace_bytes(L.n, P->nnz, L.ld, L.mL, Pa->precision, nct));
   return 0;
 }
 
@@ -1415,7 +1415,7 @@ static void cgal_plan(const usbs_problem* P, const usbs_cgal_params* Pa, const D
   L.status = ar.take<int>(32);
   L.ctl = L.status + 16;
   const int nct = lanczos_team_size(di, L.n, Pa->precision);
-  L.lz_work = ar.take<char>(lanczos_workspace_bytes(L.n, L.ld, L.mL, Pa->precision, nct));
+  L.lz_work = ar.take<char>(lanczos_workspace_bytes(L.n, P->nnz, L.ld, L.mL, Pa->precision, nct));
 }
 
 }  // namespace usbs

@@ -33,9 +33,8 @@ import ctypes
 import threading
 import time
 
-import numpy as np
-
 from . import _lib, solver
+from .arrays import shape_of
 
 __all__ = ["SolveRequest", "SolverService", "Admission", "footprint_bytes", "RequestCancelled"]
 
@@ -167,7 +166,7 @@ class SolverService:
         req._host_layout = host
         n = kw["n"]
         k = kw["k_curr"] + kw["k_past"]
-        sdim = 0 if req.sdp_state.Omega is None else int(np.shape(req.sdp_state.Omega)[1])
+        sdim = 0 if req.sdp_state.Omega is None else int(shape_of(req.sdp_state.Omega)[1])
         prm = solver.UsbsParams()
         prm.k_curr, prm.k_past = kw["k_curr"], kw["k_past"]
         prm.lanczos_inner_iterations = kw["lanczos_inner_iterations"]

@@ -21,7 +21,7 @@ import numpy as np
 import scipy.sparse as sp
 
 from . import _lib
-from .arrays import as_torch, to_device, to_host
+from .arrays import as_torch, shape_of, to_device, to_host
 from .problem import DeviceProblem, layout
 from .rng import default_q0
 from .state import SDPState
@@ -261,7 +261,7 @@ def usbs(sdp_state, n, m, trace_ub, trace_factor, rho, beta, k_curr, k_past, max
         Pm = Om = None
     elif sdp_state.Omega is not None:
         mode = 0
-        sdim = int(sdp_state.Omega.shape[1])
+        sdim = int(shape_of(sdp_state.Omega)[1])
         Om = _dev_cols(sdp_state.Omega, n, ld, sdim, dev, f64)
         Pm = _dev_cols(sdp_state.P, n, ld, sdim, dev, f64)
         X = None
@@ -367,7 +367,7 @@ def cgal(sdp_state, n, m, trace_ub, beta0, max_iters, max_time, obj_gap_eps, inf
     z = _to_dev(sdp_state.z, dev).clone()
     if sdp_state.Omega is not None:
         mode = 0
-        sdim = int(sdp_state.Omega.shape[1])
+        sdim = int(shape_of(sdp_state.Omega)[1])
         Om = _dev_cols(sdp_state.Omega, n, ld, sdim, dev, f64)
         Pm = _dev_cols(sdp_state.P, n, ld, sdim, dev, f64)
         X = None
