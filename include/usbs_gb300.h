@@ -149,8 +149,11 @@ int usbs_eigsh_smallest(int n, long long nnz, const int* rowptr, const int* col,
  *  - Allocates nothing: no cudaMalloc/cudaFree, no allocating library call.
  *    Scratch is a 16 MiB static device array in the library image.
  *  - The first call on each device looks up that array's address
- *    (cudaGetSymbolAddress, with that device current) and caches it.  Make
- *    that first call before any stream capture on the device.
+ *    (cudaGetSymbolAddress, with that device current) and caches it, keyed
+ *    by the current CUDA context: a call under another context (after a
+ *    device reset, or with a context the caller made current through the
+ *    driver API) looks it up again.  Make the first call on a device, and
+ *    the first after such a change, before any stream capture on it.
  *  - Problems whose usbs_eigsh_workspace_bytes() exceeds
  *    USBS_EIGSH_STATIC_SCRATCH_BYTES are rejected (-2, usbs_last_error()).
  *    The scratch holds the assembled operator (nnz values), three n-vectors

@@ -17,11 +17,22 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr())
 
 
-def _setup(device, precision):
+# the three Lanczos paths: one cluster (ER 600), the cooperative team kernel
+# (ER 15,000 in FP64) and the stream path (RGG 25,000 in FP64, ER 45,000 in
+# FP32), whose scratch also holds per-CTA partial sums, barrier counters or
+# the loop's control block and the operator's sliced-ELL copy
+GRAPHS = {"er600": lambda: wl.er_graph(600, 6000, 5),
+          "er15k": lambda: wl.er_graph(15000, 60000, 21),
+          "rgg25k": lambda: wl.rgg_knn_graph(25000, 6, 22),
+          "er45k": lambda: wl.er_graph(45000, 120000, 23)}
+KIND = {"er600": 1, "er15k": 0, "rgg25k": 2, "er45k": 2}
+
+
+def _setup(device, precision, graph="er600"):
     import torch
     from oracle import maxcut as omaxcut
     from usbs_gb300.problem import DeviceProblem, layout
-    Wg = wl.er_graph(600, 6000, 5)
+    Wg = GRAPHS[graph]()
     st = omaxcut.initialize_state(Wg, 4)
     n = st.C.shape[0]
     prob = DeviceProblem(layout(st.C, st.A_data, st.A_indices, m=n), device)
@@ -59,11 +70,15 @@ def _call(lib, noalloc, prob, n, vt, y, q0, precision, nd=6, inner=32, restarts=
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("precision,rtol", [(64, 1e-12), (32, 1e-6)])
-def test_noalloc_matches_workspace_entry_point(cuda, precision, rtol):
+@pytest.mark.parametrize("graph,precision,rtol", [("er600", 64, 1e-12), ("er600", 32, 1e-6),
+                                                  ("er15k", 64, 1e-12), ("rgg25k", 64, 1e-12),
+                                                  ("er45k", 32, 1e-6)])
+def test_noalloc_matches_workspace_entry_point(cuda, graph, precision, rtol):
     from usbs_gb300 import _lib
     lib = _lib.load()
-    prob, n, vt, ys, q0s = _setup(cuda, precision)
+    prob, n, vt, ys, q0s = _setup(cuda, precision, graph)
+    assert lib.usbs_lanczos_kernel(n, 32, precision) == KIND[graph]
+    assert lib.usbs_eigsh_workspace_bytes(n, prob.nnz, 32, precision) <= STATIC_SCRATCH_BYTES
     # two no-alloc calls in a row on different inputs: the second reuses the
     # scratch the first left behind
     got = [_call(lib, True, prob, n, vt, ys[i], q0s[i], precision) for i in range(2)]

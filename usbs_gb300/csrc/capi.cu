@@ -50,18 +50,47 @@ static size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 // Fixed device scratch of usbs_eigsh_smallest_noalloc: part of the module
 // image, so it exists on every device that loads the library and is never
-// allocated or freed at run time.  Its address is looked up once per device.
+// allocated or freed at run time.  Its address belongs to a CUDA context (the
+// module is loaded once per context), so it is looked up once per device and
+// looked up again when the current context of that device has changed (a
+// device reset, or a caller that made another context current through the
+// driver API).
 static __device__ __align__(256) unsigned char g_eigsh_scratch[USBS_EIGSH_STATIC_SCRATCH_BYTES];
-static void* g_eigsh_scratch_addr[64];
+struct ScratchAddr {
+  void* ctx;
+  void* ptr;
+};
+static ScratchAddr g_eigsh_scratch_addr[64];
 static std::mutex g_eigsh_scratch_mu;
+
+// the calling thread's current CUDA context (driver handle), or null
+static void* current_context() {
+  typedef int (*CtxGetCurrent)(void**);
+  static const CtxGetCurrent fn = [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) !=
+            cudaSuccess ||
+        q != cudaDriverEntryPointSuccess) {
+      cudaGetLastError();
+      f = nullptr;
+    }
+    return (CtxGetCurrent)f;
+  }();
+  void* ctx = nullptr;
+  if (fn && fn(&ctx) == 0) return ctx;
+  return nullptr;
+}
 
 static int eigsh_static_scratch(void** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) { set_error("cudaGetDevice: %s", cudaGetErrorString(e)); return -5; }
   if (dev < 0 || dev >= 64) { set_error("device index %d out of range", dev); return -2; }
+  void* ctx = current_context();
   std::lock_guard<std::mutex> lk(g_eigsh_scratch_mu);
-  if (!g_eigsh_scratch_addr[dev]) {
+  ScratchAddr& a = g_eigsh_scratch_addr[dev];
+  if (!a.ptr || a.ctx != ctx) {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_eigsh_scratch);
     if (e != cudaSuccess || !p) {
@@ -69,9 +98,10 @@ static int eigsh_static_scratch(void** out) {
                 cudaGetErrorString(e));
       return -5;
     }
-    g_eigsh_scratch_addr[dev] = p;
+    a.ptr = p;
+    a.ctx = current_context();   // the lookup made the device's context current if none was
   }
-  *out = g_eigsh_scratch_addr[dev];
+  *out = a.ptr;
   return 0;
 }
 

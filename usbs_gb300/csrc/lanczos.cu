@@ -690,7 +690,7 @@ lanczos_team_kernel(const __grid_constant__ TeamBatch<VT> batch) {
 // start and derives the same mode (step, breakdown replacement, or nothing
 // to do), so the host enqueues a cycle's launches without reading anything
 // back, and reads the block once per restart.
-struct StreamCtl {
+struct __align__(16) StreamCtl {
   int i, k, bd, cur;           // step, saved vectors, breakdown pending, work vector in use
   int stop, rot, stepped;      // loop ended; rotation pending; the finished cycle had steps
   int restarts, breakdowns, steps, sum_nv, sum_kn, nconv;
@@ -716,15 +716,20 @@ struct StShared {
 
 enum { SM_SKIP = 0, SM_STEP = 1, SM_BREAKDOWN = 2 };
 
-// the step's mode from the control block (the same in every kernel of a step)
-__device__ __forceinline__ int st_mode(const StreamCtl* c, int m, int* i, int* nv, int* buf) {
-  const int stop = __ldcg(&c->stop), bd = __ldcg(&c->bd), ii = __ldcg(&c->i),
-            cur = __ldcg(&c->cur);
+// the step's mode from the control block's first eight ints (i, k, bd, cur,
+// stop, rot, ...; the same in every kernel of a step), read as two 16-byte
+// loads in one round trip
+__device__ __forceinline__ int st_mode_of(int4 a, int4 b, int m, int* i, int* nv, int* buf) {
+  const int ii = a.x, bd = a.z, cur = a.w, stop = b.x, rot = b.y;
   *i = ii;
-  if (stop || __ldcg(&c->rot)) return SM_SKIP;
+  if (stop || rot) return SM_SKIP;
   if (bd) { *nv = ii; *buf = cur ^ 1; return SM_BREAKDOWN; }
   if (ii < m) { *nv = ii + 1; *buf = cur; return SM_STEP; }
   return SM_SKIP;
+}
+__device__ __forceinline__ int st_mode(const StreamCtl* c, int m, int* i, int* nv, int* buf) {
+  const int4* p = (const int4*)c;
+  return st_mode_of(__ldcg(p), __ldcg(p + 1), m, i, nv, buf);
 }
 
 // ticket of the last CTA: true in every thread of the CTA that finished last
@@ -937,8 +942,17 @@ __global__ void __launch_bounds__(LZ_BLOCK, 8) st_sell_spmv_kernel(
     const __grid_constant__ TeamDesc<VT> P, StreamCtl* ctl) {
   typedef typename Acc<VT>::type AT;
   __shared__ VT ys[LZ_BLOCK];
+  // every load that depends on no other is issued first: the control block,
+  // the slice's width and row map
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int s = blockIdx.x * (LZ_BLOCK / 32) + warp;
+  const bool has = s < (P.n + 31) / 32;
+  const int4 ca = __ldcg((const int4*)ctl), cb = __ldcg((const int4*)ctl + 1);
+  const double invb_d = __ldcg(&ctl->invb);
+  const int width = has ? __ldg(P.sl_w + s) : 0;
+  const int lr = has ? (int)__ldg(P.sl_row + 32 * s + lane) : 0;
   int i, nv, buf;
-  const int mode = st_mode(ctl, P.m, &i, &nv, &buf);
+  const int mode = st_mode_of(ca, cb, P.m, &i, &nv, &buf);
   if (mode == SM_SKIP) return;
   const size_t ld = (size_t)P.ld;
   const int w0 = blockIdx.x * LZ_BLOCK, row = w0 + threadIdx.x;
@@ -946,14 +960,12 @@ __global__ void __launch_bounds__(LZ_BLOCK, 8) st_sell_spmv_kernel(
     if (row < P.n) P.vbuf[(size_t)buf * ld + row] = (VT)hash_normal((uint64_t)i, (uint64_t)row);
     return;
   }
-  const int k = __ldcg(&ctl->k);
+  const int k = ca.y;
   const bool wq = i > k;
-  const VT xscale = wq ? (VT)__ldcg(&ctl->invb) : (VT)1;
+  const VT xscale = wq ? (VT)invb_d : (VT)1;
   const VT* __restrict__ x = wq ? P.vbuf + (size_t)(buf ^ 1) * ld : P.Q + (size_t)k * ld;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int s = blockIdx.x * (LZ_BLOCK / 32) + warp;
-  if (s < (P.n + 31) / 32) {
-    const int width = P.sl_w[s];
+  const VT xrow = (wq && row < P.n) ? __ldg(x + row) : (VT)0;
+  if (has) {
     const int* cp = P.sl_col + (size_t)s * 32 * P.wcap + lane;
     const VT* vp = P.sl_val + (size_t)s * 32 * P.wcap + lane;
     constexpr int PF = 16;
@@ -970,7 +982,6 @@ __global__ void __launch_bounds__(LZ_BLOCK, 8) st_sell_spmv_kernel(
 #pragma unroll
     for (int u = 0; u < PF; ++u) acc += (AT)v[u] * (AT)xv[u];
     for (int u = PF; u < width; ++u) acc += (AT)__ldg(vp + 32 * u) * (AT)__ldg(x + __ldg(cp + 32 * u));
-    const int lr = P.sl_row[32 * s + lane];
     const int r = w0 + lr;
     if (r < P.n && width == P.wcap) {
       // the rest of a row longer than the slice capacity
@@ -983,7 +994,7 @@ __global__ void __launch_bounds__(LZ_BLOCK, 8) st_sell_spmv_kernel(
   __syncthreads();
   if (row < P.n) {
     P.vbuf[(size_t)buf * ld + row] = ys[threadIdx.x] * xscale;
-    if (wq) P.Q[(size_t)i * ld + row] = __ldg(x + row) * xscale;
+    if (wq) P.Q[(size_t)i * ld + row] = xrow * xscale;
   }
 }
 
