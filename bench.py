@@ -556,7 +556,7 @@ def errors_vs_oracle(g, o):
     rel = lambda a, b: abs(a - b) / max(abs(b), 1e-300)
     return {"primal_obj_rel": rel(g["primal_obj"], o["primal_obj"]),
             "dual_obj_rel": rel(g["dual_obj"], o["dual_obj"]),
-            "lambda_min_rel": rel(g["cand_eig0"], o["cand_eig0"]),
+            "lambda_min_abs": abs(g["cand_eig0"] - o["cand_eig0"]),
             "obj_gap_abs": abs(g["obj_gap"] - o["obj_gap"]),
             "infeas_gap_abs": abs(g["infeas_gap"] - o["infeas_gap"]),
             "max_infeas_abs": abs(g["max_infeas"] - o["max_infeas"])}
@@ -581,6 +581,33 @@ def device_final(st, n, iters, device, precision, eps=-1.0, q0=None):
     rec = dict(tr[-1])
     rec["dual_obj"] = float(np.asarray(st.b) @ out.y.cpu().numpy())
     return rec, info, sec
+
+
+TRACE_KEYS = ("primal_obj", "obj_ub", "lb_spec_est", "pen_dual_obj", "cand_pen_dual_obj",
+              "cand_eig0", "obj_gap", "infeas_gap", "max_infeas", "tr_X")
+
+
+def trajectory_vs_oracle(st, n, device, q0, iters):
+    """Per outer iteration t < iters, the largest of |dev - oracle| / max(1,
+    |oracle|) over the traced values, FP64 and mixed precision."""
+    import torch
+    from oracle import usbs as ousbs
+    from usbs_gb300 import solver
+    S = SETTINGS
+    args = (n, n, S["trace_factor"] * n * st.SCALE_X, S["trace_factor"], S["rho"], S["beta"],
+            S["k_curr"], S["k_past"], iters, np.inf, -1.0, -1.0, -1.0,
+            S["lanczos_inner_iterations"], S["lanczos_max_restarts"], S["subprob_eps"],
+            S["subprob_max_iters"])
+    otr = []
+    ousbs.usbs(st, *args, q0=q0, trace=otr)
+    out = {}
+    for prec in (64, 32):
+        _, gtr, _ = solver.usbs(st, *args, q0=q0, precision=prec, device=device,
+                                return_trace=True)
+        torch.cuda.synchronize()
+        out[f"fp{prec}"] = [max(abs(a[k] - b[k]) / max(1.0, abs(a[k])) for k in TRACE_KEYS)
+                            for a, b in zip(otr, gtr)]
+    return out
 
 
 def golden_solves():
@@ -891,16 +918,17 @@ def main():
             solves = {"device": solves_leg(device), "oracle": oracle_solve_rates()}
         except Exception as exc:  # the main line is still reported
             solves = {"error": str(exc)[:200]}
+    trajectory = None
     if rank == 0:
-        # final state of one step's solve (it_step iterations from the cold
-        # start, same start vector) against the FP64 oracle
-        otr, oout, oby, _ = oracle_trace(st, n, it_step, q0=q0)
-        orec = dict(otr[-1])
-        orec["dual_obj"] = oby
-        errors = {"iterations": it_step}
-        for prec in (32, 64):
-            grec, _, _ = device_final(st, n, it_step, device, prec, q0=q0)
-            errors[f"fp{prec}"] = errors_vs_oracle(grec, orec)
+        # the first outer iterations on this instance (same start vector) against
+        # the FP64 oracle: largest relative difference over the traced values
+        trajectory = trajectory_vs_oracle(st, n, device, q0, 3)
+        # the solution's errors against the FP64 oracle's, on an instance that
+        # both solve to the reference's stop test at 1e-4
+        if solves and "device" in solves:
+            rec = solves["device"].get("er60_1e-4", {})
+            errors = {"instance": "er60 to 1e-4 (tests/golden/oracle_solves.json)",
+                      **{p: rec[p]["errors_vs_oracle"] for p in ("fp64", "fp32") if p in rec}}
 
     cpu = None
     if rank == 0:
@@ -920,6 +948,7 @@ def main():
             "fp64": {"value": fp64_value, "unit": UNIT, "dtype": "f64",
                      "note": "the same timed steps on the plain FP64 device path"},
             "errors_vs_oracle": errors,
+            "trajectory_vs_oracle": trajectory,
             "solves": solves,
             "roofline": {"kernel": lz_kernel, "bound": "hbm",
                          "achieved": achieved, "peak": peak, "unit": "GB/s",

@@ -31,7 +31,7 @@
 extern "C" {
 #endif
 
-#define USBS_GB300_ABI_VERSION 4
+#define USBS_GB300_ABI_VERSION 5
 
 /* ABI version of the loaded library (USBS_GB300_ABI_VERSION). */
 int usbs_abi_version(void);
@@ -279,6 +279,10 @@ typedef struct usbs_params {
   int sketch_dim;           /* columns of Omega (mode 0) */
   int lanczos_rows_per_cta; /* cluster Lanczos: rows per CTA (>= 16); 0: the class's tuned
                                choice (usbs_lanczos_autotune), else 64 */
+  int lanczos_path;         /* 0: the library's choice (usbs_lanczos_kernel); 2: a problem too
+                               large for one cluster always takes the stream path, never the
+                               cooperative launch, so the solve never needs the GPU to itself
+                               (a service running several solves at once sets this) */
 } usbs_params;
 
 /* Iterate state (device arrays, column-major with leading dimension ld) and

@@ -37,3 +37,10 @@ def test_exclusive_request_waits_for_drain_and_holds_the_line():
 def test_request_larger_than_the_budget_never_fits():
     adm = Admission(budget_bytes=100, max_slots=2)
     assert adm.ever_fits(100) and not adm.ever_fits(101)
+
+
+def test_request_waiting_for_its_warm_start_parent_does_not_block_others():
+    adm = Admission(budget_bytes=100, max_slots=4)
+    queue = [(10, False, False), (20, False, True)]
+    assert adm.pick(queue) == 1
+    assert adm.pick([(10, False, True), (20, False, True)]) == 0

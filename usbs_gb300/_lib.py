@@ -75,7 +75,7 @@ def load(build_if_missing=True):
         fn = getattr(lib, name)
         fn.restype = res
         fn.argtypes = args
-    if lib.usbs_abi_version() != 4:
+    if lib.usbs_abi_version() != 5:
         raise LibraryError("libusbs_gb300 ABI version mismatch")
     _lib = lib
     return lib

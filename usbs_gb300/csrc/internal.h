@@ -37,9 +37,12 @@ struct LanczosProblem {
   int* status;
   void* work;           // workspace of lanczos_workspace_bytes()
   int rows_per_cta = 0; // cluster path: rows per CTA (0: measured class choice or default)
+  int no_coop = 0;      // 1: never the cooperative team kernel (the stream path instead)
 };
-size_t lanczos_workspace_bytes(int n, long long nnz, int ld, int m, int prec, int nctas);
-int lanczos_team_size(const DeviceInfo& di, int n, int prec);
+// `stream`: size for the stream path even where the team kernel would fit
+size_t lanczos_workspace_bytes(int n, long long nnz, int ld, int m, int prec, int nctas,
+                               bool stream = false);
+int lanczos_team_size(const DeviceInfo& di, int n, int prec, bool stream = false);
 int lanczos_lanes(int n, long long nnz);
 int lanczos_occupancy(int prec);
 int lanczos_stream_occupancy(int prec);

@@ -52,9 +52,9 @@ struct TeamDesc {
   // of each 256-row window sorted by length, 32-row slices, each slice
   // holding at most wcap entries per row; longer rows finish from the CSR)
   int wcap;
-  int* sl_w;             // width of each slice
+  int* sl_ptr;           // slice s: entries [sl_ptr[s], sl_ptr[s + 1]), column-major
   unsigned char* sl_row; // sorted position -> row offset inside its window
-  int* sl_col;           // slice s: entries from s * 32 * wcap, column-major
+  int* sl_col;
   VT* sl_val;
   VT* vbuf;              // 3 flat vectors: two work vectors, then Q[:, k] of the cycle
   double* part;
@@ -887,12 +887,12 @@ __device__ __forceinline__ void st_chunks(int n, int* c0, int* c1) {
 // ---- the stream path's operator layout (built once per call) ----
 // Rows of each 256-row window are ordered by length (longest first, then by
 // row) and cut into 32-row slices; slice s keeps entry k of its lane-th row at
-// s * 32 * wcap + 32 k + lane (k < the slice's width, at most wcap; shorter
-// rows are padded with column 0, value 0; rows longer than wcap finish from
-// the CSR).  One CTA per window: each thread ranks its row against the
-// window's others.
+// sl_ptr[s] + 32 k + lane for k below the slice's width (its longest row's
+// length, at most wcap; shorter rows are padded with column 0, value 0; rows
+// longer than wcap finish from the CSR).  Three launches: the order and the
+// widths per window, a prefix sum of the slice sizes, the entries.
 template <typename VT>
-__global__ void __launch_bounds__(LZ_BLOCK) st_sell_build_kernel(
+__global__ void __launch_bounds__(LZ_BLOCK) st_sell_order_kernel(
     const __grid_constant__ TeamDesc<VT> P) {
   __shared__ int len[LZ_BLOCK];
   __shared__ int order[LZ_BLOCK];
@@ -914,15 +914,46 @@ __global__ void __launch_bounds__(LZ_BLOCK) st_sell_build_kernel(
   // slice that exists (s < ceil(n / 32)) has a real row at its first position.
   const int p = tid, s = blockIdx.x * (LZ_BLOCK / 32) + p / 32, lane = p & 31;
   if (s >= (P.n + 31) / 32) return;
-  const int w = min(len[order[p & ~31]], P.wcap);
-  if (lane == 0) P.sl_w[s] = w;
-  const bool real = p < rows;
-  const int lr = real ? order[p] : p;          // padding lanes: unused positions
+  const int lr = (p < rows) ? order[p] : p;      // padding lanes: unused positions
   P.sl_row[32 * s + lane] = (unsigned char)lr;
-  const int lenr = real ? len[lr] : 0;
-  const int b = real ? P.rowptr[w0 + lr] : 0;
-  int* cdst = P.sl_col + (size_t)s * 32 * P.wcap + lane;
-  VT* vdst = P.sl_val + (size_t)s * 32 * P.wcap + lane;
+  if (lane == 0) P.sl_ptr[s + 1] = 32 * min(len[order[p]], P.wcap);
+}
+
+// sl_ptr[1..ns] (slice sizes) -> offsets, sl_ptr[0] = 0; one CTA of 1024
+__global__ void __launch_bounds__(1024) st_sell_scan_kernel(int ns, int* sl_ptr) {
+  __shared__ int part[1024];
+  const int tid = threadIdx.x, per = (ns + 1023) / 1024;
+  const int t0 = min(tid * per, ns), t1 = min(t0 + per, ns);
+  int sum = 0;
+  for (int i = t0; i < t1; ++i) sum += sl_ptr[i + 1];
+  part[tid] = sum;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    const int v = tid >= off ? part[tid - off] : 0;
+    __syncthreads();
+    part[tid] += v;
+    __syncthreads();
+  }
+  int base = tid ? part[tid - 1] : 0;
+  for (int i = t0; i < t1; ++i) {
+    base += sl_ptr[i + 1];
+    sl_ptr[i + 1] = base;
+  }
+  if (tid == 0) sl_ptr[0] = 0;
+}
+
+template <typename VT>
+__global__ void __launch_bounds__(LZ_BLOCK) st_sell_fill_kernel(
+    const __grid_constant__ TeamDesc<VT> P) {
+  const int w0 = blockIdx.x * LZ_BLOCK, p = threadIdx.x;
+  const int s = blockIdx.x * (LZ_BLOCK / 32) + p / 32, lane = p & 31;
+  if (s >= (P.n + 31) / 32) return;
+  const int base = P.sl_ptr[s], w = (P.sl_ptr[s + 1] - base) >> 5;
+  const int r = w0 + P.sl_row[32 * s + lane];
+  const int b = (r < P.n) ? P.rowptr[r] : 0;
+  const int lenr = (r < P.n) ? P.rowptr[r + 1] - b : 0;
+  int* cdst = P.sl_col + base + lane;
+  VT* vdst = P.sl_val + base + lane;
   for (int k = 0; k < w; ++k) {
     const bool e = k < lenr;
     cdst[32 * k] = e ? P.col[b + k] : 0;
@@ -949,7 +980,8 @@ __global__ void __launch_bounds__(LZ_BLOCK, 8) st_sell_spmv_kernel(
   const bool has = s < (P.n + 31) / 32;
   const int4 ca = __ldcg((const int4*)ctl), cb = __ldcg((const int4*)ctl + 1);
   const double invb_d = __ldcg(&ctl->invb);
-  const int width = has ? __ldg(P.sl_w + s) : 0;
+  const int sb = has ? __ldg(P.sl_ptr + s) : 0;
+  const int width = has ? (__ldg(P.sl_ptr + s + 1) - sb) >> 5 : 0;
   const int lr = has ? (int)__ldg(P.sl_row + 32 * s + lane) : 0;
   int i, nv, buf;
   const int mode = st_mode_of(ca, cb, P.m, &i, &nv, &buf);
@@ -966,8 +998,8 @@ __global__ void __launch_bounds__(LZ_BLOCK, 8) st_sell_spmv_kernel(
   const VT* __restrict__ x = wq ? P.vbuf + (size_t)(buf ^ 1) * ld : P.Q + (size_t)k * ld;
   const VT xrow = (wq && row < P.n) ? __ldg(x + row) : (VT)0;
   if (has) {
-    const int* cp = P.sl_col + (size_t)s * 32 * P.wcap + lane;
-    const VT* vp = P.sl_val + (size_t)s * 32 * P.wcap + lane;
+    const int* cp = P.sl_col + sb + lane;
+    const VT* vp = P.sl_val + sb + lane;
     constexpr int PF = 16;
     int c[PF];
     VT v[PF], xv[PF];
@@ -1054,6 +1086,88 @@ __global__ void __launch_bounds__(LZ_BLOCK, 3) st_update_dot_kernel(
     for (int j = 0; j < 4; ++j) x.v[j] -= s.v[j];
     st4(v, r4, P.n, x);
     st_dots(P.Q, ld, r4, P.n, nv, x, sacc);
+  }
+  double* part = P.part + (size_t)MP1 * R;
+  st_block_cols(sacc, nv, part + blockIdx.x, R);
+  if (!st_last_cta(&ctl->ticket[1], sh)) return;
+  st_reduce<VT>(part, R, nv, sh);
+  for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) ctl->h2[c] = sh.h[c];
+  if (threadIdx.x == 0) {
+    if (mode == SM_STEP) ctl->alpha[i] = __ldcg(&ctl->h1[i]) + sh.h[i];
+    ctl->ticket[1] = 0u;
+  }
+}
+
+// B, one pass over Q: each thread keeps its rows of the nv basis columns in
+// registers (8-byte loads: two FP32 rows or one FP64 row), forms
+// v -= Q h1, then h2 = Q^T v from the same registers.
+template <typename VT>
+__global__ void __launch_bounds__(LZ_BLOCK, 2) st_update_dot1_kernel(
+    const __grid_constant__ TeamDesc<VT> P, StreamCtl* ctl) {
+  typedef typename Acc<VT>::type AT;
+  constexpr int RW = 8 / (int)sizeof(VT);           // rows per thread
+  constexpr int CROWS = RW * LZ_BLOCK;              // rows per chunk
+  __shared__ StShared<VT> sh;
+  int i, nv, buf;
+  const int mode = st_mode(ctl, P.m, &i, &nv, &buf);
+  if (mode == SM_SKIP) return;
+  const int R = gridDim.x, n = P.n;
+  const size_t ld = (size_t)P.ld;
+  for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) sh.hv[c] = (VT)__ldcg(&ctl->h1[c]);
+  extern __shared__ __align__(16) unsigned char st_dyn[];
+  AT* sacc = (AT*)st_dyn;
+  for (int c = 0; c < nv; ++c) sacc[c * LZ_BLOCK + threadIdx.x] = (AT)0;
+  __syncthreads();
+  const int nch = (n + CROWS - 1) / CROWS;
+  const int c0 = (int)((long long)nch * blockIdx.x / R);
+  const int c1 = (int)((long long)nch * (blockIdx.x + 1) / R);
+  VT* v = P.vbuf + (size_t)buf * ld;
+  for (int ch = c0; ch < c1; ++ch) {
+    const int r0 = ch * CROWS + RW * threadIdx.x;
+    if (r0 >= n) continue;
+    const bool full = r0 + RW <= n;
+    VT q[MP1][RW];
+#pragma unroll
+    for (int c = 0; c < MP1; ++c)
+      if (c < nv) {
+        const VT* src = P.Q + (size_t)c * ld + r0;
+        if constexpr (RW == 2) {
+          if (full) {
+            const float2 a = __ldg((const float2*)src);
+            q[c][0] = a.x; q[c][1] = a.y;
+          } else {
+            q[c][0] = __ldg(src); q[c][1] = (VT)0;
+          }
+        } else {
+          q[c][0] = __ldg(src);
+        }
+      }
+    VT x[RW], s[RW];
+#pragma unroll
+    for (int j = 0; j < RW; ++j) {
+      x[j] = (r0 + j < n) ? __ldcg(v + r0 + j) : (VT)0;
+      s[j] = (VT)0;
+    }
+#pragma unroll
+    for (int c = 0; c < MP1; ++c)
+      if (c < nv) {
+        const VT h = sh.hv[c];
+#pragma unroll
+        for (int j = 0; j < RW; ++j) s[j] += q[c][j] * h;
+      }
+#pragma unroll
+    for (int j = 0; j < RW; ++j) {
+      x[j] -= s[j];
+      if (r0 + j < n) v[r0 + j] = x[j];
+    }
+#pragma unroll
+    for (int c = 0; c < MP1; ++c)
+      if (c < nv) {
+        AT d = (AT)0;
+#pragma unroll
+        for (int j = 0; j < RW; ++j) d += (AT)q[c][j] * (AT)x[j];
+        sacc[c * LZ_BLOCK + threadIdx.x] += d;
+      }
   }
   double* part = P.part + (size_t)MP1 * R;
   st_block_cols(sacc, nv, part + blockIdx.x, R);
@@ -1701,19 +1815,20 @@ static int sell_wcap(int n, long long nnz) {
 }
 static size_t sell_bytes(int n, long long nnz, size_t vt) {
   const size_t ns = ((size_t)n + 31) / 32;
-  return align256(ns * sizeof(int)) + align256(ns * 32) +
+  return align256((ns + 1) * sizeof(int)) + align256(ns * 32) +
          align256(ns * 32 * (size_t)sell_wcap(n, nnz) * sizeof(int)) +
          align256(ns * 32 * (size_t)sell_wcap(n, nnz) * vt);
 }
 
-size_t lanczos_workspace_bytes(int n, long long nnz, int ld, int m, int prec, int nctas) {
+size_t lanczos_workspace_bytes(int n, long long nnz, int ld, int m, int prec, int nctas,
+                               bool stream) {
   (void)m;
   const size_t vt = (prec == 64) ? 8 : 4;
   size_t b = align256(3 * (size_t)ld * vt);
   b += align256((size_t)3 * nctas * MP1 * sizeof(double));
   b += align256((size_t)MAXM * MAXM * sizeof(double));
   b += 256;  // barrier counters
-  if (!x_fits_smem(n, vt)) b += sell_bytes(n, nnz, vt);
+  if (stream || !x_fits_smem(n, vt)) b += sell_bytes(n, nnz, vt);
   return b;
 }
 static_assert(sizeof(StreamCtl) <= 32 * 4 * 32, "the control block takes one 32-row vector slot");
@@ -1725,8 +1840,8 @@ int lanczos_lanes(int n, long long nnz) {
   return L;
 }
 
-int lanczos_team_size(const DeviceInfo& di, int n, int prec) {
-  if (!x_fits_smem(n, prec == 64 ? 8 : 4)) {
+int lanczos_team_size(const DeviceInfo& di, int n, int prec, bool stream) {
+  if (stream || !x_fits_smem(n, prec == 64 ? 8 : 4)) {
     // stream path: the grid of its partial-sum kernels, one wave
     const int tiles = (n + LZ_BLOCK - 1) / LZ_BLOCK;
     const int occ = (prec == 64) ? di.stream_occ64 : di.stream_occ32;
@@ -1852,7 +1967,7 @@ static const int* stream_occ() {
   static int occ[4] = {0, 0, 0, 0};
   static std::once_flag once;
   std::call_once(once, [] {
-    const void* ks[] = {(const void*)st_dot_kernel<VT>, (const void*)st_update_dot_kernel<VT>,
+    const void* ks[] = {(const void*)st_dot_kernel<VT>, (const void*)st_update_dot1_kernel<VT>,
                         (const void*)st_update_norm_kernel<VT>,
                         (const void*)st_rotate_kernel<VT>};
     const size_t dyn[] = {st_sacc_bytes<VT>(), st_sacc_bytes<VT>(), 0, 0};
@@ -1897,7 +2012,7 @@ static int run_stream(const DeviceInfo& di, const LanczosProblem& p, cudaStream_
     return -2;
   }
   const int ntiles = (p.n + LZ_BLOCK - 1) / LZ_BLOCK;
-  const int G = lanczos_team_size(di, p.n, sizeof(VT) == 8 ? 64 : 32);   // partials per pass
+  const int G = lanczos_team_size(di, p.n, sizeof(VT) == 8 ? 64 : 32, true);   // partials per pass
   const int* occ = stream_occ<VT>();
   int g[4];
   for (int j = 0; j < 4; ++j) {
@@ -1923,13 +2038,19 @@ static int run_stream(const DeviceInfo& di, const LanczosProblem& p, cudaStream_
   w += 256;
   const int ns = (p.n + 31) / 32;
   t.wcap = sell_wcap(p.n, p.nnz);
-  t.sl_w = (int*)w; w += align256((size_t)ns * sizeof(int));
+  if ((long long)ns * 32 * t.wcap > 0x7fffffffLL) {
+    set_error("lanczos: n=%d is too large for the stream path's operator layout", p.n);
+    return -2;
+  }
+  t.sl_ptr = (int*)w; w += align256((size_t)(ns + 1) * sizeof(int));
   t.sl_row = (unsigned char*)w; w += align256((size_t)ns * 32);
   t.sl_col = (int*)w; w += align256((size_t)ns * 32 * t.wcap * sizeof(int));
   t.sl_val = (VT*)w;
   t.alpha = p.alpha; t.beta = p.beta; t.ctl = p.ctl; t.status = p.status;
-  st_sell_build_kernel<VT><<<ntiles, LZ_BLOCK, 0, stream>>>(t);
-  t_launches += 1;
+  st_sell_order_kernel<VT><<<ntiles, LZ_BLOCK, 0, stream>>>(t);
+  st_sell_scan_kernel<<<1, 1024, 0, stream>>>(ns, t.sl_ptr);
+  st_sell_fill_kernel<VT><<<ntiles, LZ_BLOCK, 0, stream>>>(t);
+  t_launches += 3;
   if (cudaMemsetAsync(ctl, 0, sizeof(StreamCtl), stream) != cudaSuccess ||
       cudaMemsetAsync(p.ctl, 0, 16 * sizeof(int), stream) != cudaSuccess) {
     set_error("lanczos: memset failed");
@@ -1947,7 +2068,7 @@ static int run_stream(const DeviceInfo& di, const LanczosProblem& p, cudaStream_
     for (int j = 0; j < slots; ++j) {
       st_sell_spmv_kernel<VT><<<ntiles, LZ_BLOCK, 0, stream>>>(t, ctl);
       st_dot_kernel<VT><<<g[0], LZ_BLOCK, st_sacc_bytes<VT>(), stream>>>(t, ctl);
-      st_update_dot_kernel<VT><<<g[1], LZ_BLOCK, st_sacc_bytes<VT>(), stream>>>(t, ctl);
+      st_update_dot1_kernel<VT><<<g[1], LZ_BLOCK, st_sacc_bytes<VT>(), stream>>>(t, ctl);
       st_update_norm_kernel<VT><<<g[2], LZ_BLOCK, 0, stream>>>(t, ctl);
     }
     st_restart_kernel<VT><<<1, LZ_BLOCK, 0, stream>>>(t, ctl);
@@ -1982,7 +2103,7 @@ static int run_noncluster(const DeviceInfo& di, const LanczosProblem* probs, int
     int nt = 0;
     for (int i = 0; i < cnt; ++i) {
       const LanczosProblem& p = probs[base + i];
-      if (x_fits_smem(p.n, sizeof(VT))) {
+      if (x_fits_smem(p.n, sizeof(VT)) && !p.no_coop) {
         team[nt++] = p;
       } else {
         const int rc = run_stream<VT>(di, p, stream);

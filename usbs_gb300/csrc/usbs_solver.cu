@@ -787,8 +787,10 @@ static int plan(const usbs_problem* P, const usbs_params* Pa, const DeviceInfo& 
   L.status = ar.take<int>(32);
   L.ctl = L.status + 16;
   L.skip = ar.take<int>(4);
-  const int nct = lanczos_team_size(di, L.n, Pa->precision);
-  L.lz_work = ar.take<char>(lanczos_workspace_bytes(L.n, P->nnz, L.ld, L.mL, Pa->precision, nct));
+  const bool stream = Pa->lanczos_path == 2;
+  const int nct = lanczos_team_size(di, L.n, Pa->precision, stream);
+  L.lz_work = ar.take<char>(
+      lanczos_workspace_bytes(L.n, P->nnz, L.ld, L.mL, Pa->precision, nct, stream));
   return 0;
 }
 
@@ -951,6 +953,7 @@ struct Solver {
     lp.alpha = L.alpha; lp.beta = L.beta; lp.ctl = L.ctl; lp.status = L.status;
     lp.work = L.lz_work;
     lp.rows_per_cta = Pa->lanczos_rows_per_cta;
+    lp.no_coop = Pa->lanczos_path == 2 ? 1 : 0;
     const int rc = lanczos_run(di, &lp, 1, Pa->precision, st);
     launches += lanczos_last_launches();
     return rc;
@@ -1451,6 +1454,10 @@ int usbs_solve(const usbs_problem* P, const usbs_params* Pa, usbs_state* S, void
     return -2;
   }
   if (Pa->precision != 64 && Pa->precision != 32) { set_error("precision must be 32 or 64"); return -2; }
+  if (Pa->lanczos_path != 0 && Pa->lanczos_path != 2) {
+    set_error("usbs_solve: lanczos_path must be 0 or 2");
+    return -2;
+  }
   if (Pa->lanczos_rows_per_cta != 0 && Pa->lanczos_rows_per_cta < 16) {
     set_error("usbs_solve: lanczos_rows_per_cta must be 0 or >= 16");
     return -2;

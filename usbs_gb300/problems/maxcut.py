@@ -8,7 +8,7 @@ with C = 1/4 (diag(W 1) - W) symmetrised.  The constraint tensor is the list of
 import numpy as np
 import scipy.sparse as sp
 
-from ..arrays import to_host
+from ..arrays import as_torch, to_device, to_host
 from ..rng import hash_normal_matrix
 from ..state import SDPState, scale_sdp_state, unscale_sdp_state
 
@@ -52,11 +52,37 @@ def initialize_state(W, sketch_dim, Omega=None):
     return scale_sdp_state(st)
 
 
+def _device_of(*xs):
+    """The device of the first device tensor among xs, else None (host)."""
+    for x in xs:
+        t = as_torch(x) if x is not None else None
+        if t is not None and t.is_cuda:
+            return t.device
+    return None
+
+
+def _padded(x, n, dev):
+    """x with zero rows appended to n rows: a float64 tensor on `dev`, or a
+    NumPy array when dev is None."""
+    if dev is None:
+        a = np.asarray(to_host(x), float)
+        out = np.zeros((n,) + a.shape[1:])
+        out[:a.shape[0]] = a
+        return out
+    import torch
+    t = to_device(x, torch.float64, dev)
+    out = torch.zeros((n,) + tuple(t.shape[1:]), dtype=torch.float64, device=dev)
+    out[:t.shape[0]] = t
+    return out
+
+
 def implicit_warm_start(old, W, sketch_dim, Omega_pad=None):
     """Grow a solved instance to the graph W (utils/maxcut_helpers.py:95-161):
     pad X / P with zero rows, extend Omega, carry y and z, correct the primal
     objective for the changed diagonal of C, rescale with SCALE_X = 1/n and
-    SCALE_C = 1/||C||_F."""
+    SCALE_C = 1/||C||_F.  When the old iterate is on the device (a finished
+    solve's result), the new one is formed there, without a host round trip."""
+    dev = _device_of(old.y, old.z, old.P, old.X)
     old = unscale_sdp_state(old)
     C = objective(W)
     n = C.shape[0]
@@ -64,17 +90,31 @@ def implicit_warm_start(old, W, sketch_dim, Omega_pad=None):
     A_data, A_idx, b, mask = problem_data(n)
     X, P, Om = old.X, old.P, old.Omega
     if old.X is not None:
-        X = np.zeros((n, n))
-        X[:n_old, :n_old] = np.asarray(old.X)
+        if dev is None:
+            X = np.zeros((n, n))
+            X[:n_old, :n_old] = np.asarray(old.X)
+        else:
+            import torch
+            X = torch.zeros((n, n), dtype=torch.float64, device=dev)
+            X[:n_old, :n_old] = to_device(old.X, X.dtype, dev)
     if old.P is not None:
-        P = np.zeros((n, sketch_dim))
-        P[:n_old] = np.asarray(old.P)
+        P = _padded(old.P, n, dev)
         pad = hash_normal_matrix(n, n - n_old, sketch_dim) if Omega_pad is None else Omega_pad
-        Om = np.concatenate([_host(old.Omega), pad], axis=0)
+        Om = _padded(old.Omega, n, dev)
+        Om[n_old:] = pad if dev is None else to_device(pad, Om.dtype, dev)
     m_old = np.asarray(old.b).shape[0]
-    y = np.zeros(n); y[:m_old] = _host(old.y)
-    z = np.zeros(n); z[:m_old] = np.asarray(old.z)
-    primal = old.primal_obj - old.C.diagonal() @ np.asarray(old.z) + C.diagonal() @ z
+    y = _padded(old.y, n, dev)
+    z = _padded(old.z, n, dev)
+    z_old = z[:m_old]
+    dC_old = old.C.diagonal()
+    dC = C.diagonal()
+    if dev is None:
+        corr = -dC_old @ z_old + dC @ z
+    else:
+        import torch
+        corr = float(-(torch.as_tensor(dC_old, device=dev) @ z_old)
+                     + torch.as_tensor(dC, device=dev) @ z)
+    primal = old.primal_obj + corr
     st = SDPState(C=C, A_indices=A_idx, A_data=A_data, b=b, b_ineq_mask=mask, X=X, P=P,
                   Omega=Om, y=y, z=z, tr_X=old.tr_X, primal_obj=primal,
                   SCALE_C=1.0 / np.linalg.norm(C.data), SCALE_X=1.0 / float(n),
@@ -127,13 +167,15 @@ def _host(x):
 
 
 def dual_only_warm_start(old, W, sketch_dim, Omega=None):
-    """Keep only the dual y (utils/maxcut_helpers.py:232-289)."""
+    """Keep only the dual y (utils/maxcut_helpers.py:232-289); a device y
+    stays on the device."""
+    dev = _device_of(old.y)
     old = unscale_sdp_state(old)
     C = objective(W)
     n = C.shape[0]
     A_data, A_idx, b, mask = problem_data(n)
     X, P, Om = _iterate(n, sketch_dim, Omega)
-    y = np.zeros(n); y[:np.asarray(old.b).shape[0]] = _host(old.y)
+    y = _padded(old.y, n, dev)
     st = SDPState(C=C, A_indices=A_idx, A_data=A_data, b=b, b_ineq_mask=mask, X=X, P=P,
                   Omega=Om, y=y, z=np.zeros(n), tr_X=0.0, primal_obj=0.0,
                   SCALE_C=1.0 / np.linalg.norm(C.data), SCALE_X=1.0 / float(n),

@@ -176,7 +176,10 @@ def _constraint_map(old_idx, new_idx, old_m):
 
 
 def _carry(old, D, W, sketch_dim):
-    old = old._replace(y=_host(old.y), z=_host(old.z))
+    # the QAP transforms move rows through the lifted index map on the host
+    old = old._replace(y=_host(old.y), z=_host(old.z),
+                       P=None if old.P is None else _host(old.P),
+                       X=None if old.X is None else _host(old.X))
     from ..state import unscale_sdp_state
     old = unscale_sdp_state(old)
     C, A_data, A_idx, b, mask, scale_c, scale_x, sa = _problem(D, W)

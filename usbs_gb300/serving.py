@@ -10,10 +10,18 @@ A problem whose Lanczos basis fits in one thread-block cluster's shared memory
 (``usbs_lanczos_kernel`` = 1) uses cluster-scheduled kernels only, and any number
 of those run side by side; so does a problem on the stream path (kind 2, the
 largest ones), whose kernels are ordinary launches that never wait on each
-other. A mid-size problem uses the cooperative team kernel (kind 0), whose grid
-is sized for the whole GPU and must be co-resident. It therefore runs alone: it
-waits for the running solves to finish, and nothing else is admitted until it
-is done.
+other. By default the service runs every larger problem on the stream path
+(``lanczos_path=2``), so no request ever needs the GPU to itself. With
+``lanczos_path=0`` a mid-size problem uses the cooperative team kernel (kind 0),
+whose grid is sized for the whole GPU and must be co-resident; such a request
+runs alone: it waits for the running solves to finish, and nothing else is
+admitted until it is done.
+
+Warm starts from resident state: a request may name an earlier request
+(``warm_from``) and a transform (``warm_start(parent_result, cold_state) ->
+SDPState``, e.g. the MaxCut implicit warm start). It is admitted once its
+parent has finished; the transform then builds its initial state from the
+parent's result, which is still on the device, without a host round trip.
 
 Admission by memory: the service owns the HBM that was free when it started,
 less ``reserve_bytes``. A request's device footprint (its state and its
@@ -78,10 +86,15 @@ class Admission:
             self.exclusive = False
 
     def pick(self, queue):
-        """Index of the first admissible request in arrival order, or None.  A
-        request that does not fit does not block smaller ones behind it, except
-        an exclusive one, which holds the line until the GPU drains."""
-        for i, (footprint, exclusive) in enumerate(queue):
+        """Index of the first admissible request in arrival order, or None.
+        Entries are (footprint, exclusive) or (footprint, exclusive, ready); a
+        request that is not ready (its warm-start parent still running) or
+        does not fit does not block the ones behind it, except an exclusive
+        one, which holds the line until the GPU drains."""
+        for i, e in enumerate(queue):
+            footprint, exclusive = e[0], e[1]
+            if len(e) > 2 and not e[2]:
+                continue
             if self.admissible(footprint, exclusive):
                 return i
             if exclusive:
@@ -93,8 +106,12 @@ class SolveRequest:
     """One usbs() call.  ``kwargs`` are usbs()'s arguments after ``sdp_state``
     (n, m, trace_ub, ... as keywords); ``precision`` 32 or 64."""
 
-    def __init__(self, sdp_state, precision=32, tag=None, **kwargs):
+    def __init__(self, sdp_state, precision=32, tag=None, warm_from=None, warm_start=None,
+                 **kwargs):
         self.sdp_state = sdp_state
+        self.warm_from = warm_from
+        self.warm_start = warm_start
+        self.warmed = False
         self.precision = int(precision)
         self.kwargs = kwargs
         self.tag = tag
@@ -138,9 +155,10 @@ class SolverService:
     not set their own (0: the library's single-solve choice)."""
 
     def __init__(self, device="cuda", max_slots=8, reserve_bytes=2 << 30, mem_info=None,
-                 lanczos_rows_per_cta=0):
+                 lanczos_rows_per_cta=0, lanczos_path=2):
         import torch
         self.device = torch.device(device)
+        self.lanczos_path = int(lanczos_path)
         self.max_slots = int(max_slots)
         self.rows_per_cta = int(lanczos_rows_per_cta)
         self.reserve = int(reserve_bytes)
@@ -173,10 +191,11 @@ class SolverService:
         prm.precision = req.precision
         prm.sketch_mode = 0 if sdim else (1 if req.sdp_state.X is not None else 2)
         prm.sketch_dim = sdim
+        prm.lanczos_path = self.lanczos_path
         req.footprint = footprint_bytes(host, k, sdim, prm, lib)
         # only the cooperative team kernel (kind 0) needs the GPU to itself
-        req.exclusive = lib.usbs_lanczos_kernel(n, kw["lanczos_inner_iterations"],
-                                                req.precision) == 0
+        req.exclusive = self.lanczos_path != 2 and lib.usbs_lanczos_kernel(
+            n, kw["lanczos_inner_iterations"], req.precision) == 0
         req.arrival = time.perf_counter()
         if not self._adm.ever_fits(req.footprint):
             req.error = MemoryError(f"request needs {req.footprint} bytes of device memory; the "
@@ -219,7 +238,9 @@ class SolverService:
     # ------------------------------------------------------------ scheduling
     def _next(self):
         """Called with the lock held: pop the next admissible request."""
-        i = self._adm.pick([(r.footprint, r.exclusive) for r in self._queue])
+        i = self._adm.pick([(r.footprint, r.exclusive,
+                             r.warm_from is None or r.warm_from.done.is_set())
+                            for r in self._queue])
         if i is None:
             return None
         req = self._queue[i]
@@ -243,12 +264,20 @@ class SolverService:
             req.start = time.perf_counter()
             try:
                 with torch.cuda.stream(stream):
-                    inst = solver.DeviceInstance(req.sdp_state, self.device,
-                                                 host_layout=req._host_layout)
+                    state, host_layout = req.sdp_state, req._host_layout
                     kw = dict(req.kwargs)
+                    parent = req.warm_from
+                    if parent is not None and parent.result is not None and req.warm_start:
+                        # the parent's result is still on the device
+                        state = req.warm_start(parent.result, req.sdp_state)
+                        host_layout = None
+                        req.warmed = True
+                        kw["trace_ub"] = kw["trace_factor"] * kw["n"] * state.SCALE_X
+                    inst = solver.DeviceInstance(state, self.device, host_layout=host_layout)
                     if self.rows_per_cta:
                         kw.setdefault("lanczos_rows_per_cta", self.rows_per_cta)
-                    out, info = solver.usbs(req.sdp_state, precision=req.precision,
+                    kw.setdefault("lanczos_path", self.lanczos_path)
+                    out, info = solver.usbs(state, precision=req.precision,
                                             device=self.device, return_info=True,
                                             instance=inst, stream=stream, **kw)
                     stream.synchronize()

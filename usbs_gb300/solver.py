@@ -49,7 +49,7 @@ class UsbsParams(ctypes.Structure):
                 ("subprob_eps", ctypes.c_double), ("subprob_max_iters", ctypes.c_int),
                 ("cond_exp_base", ctypes.c_double), ("precision", ctypes.c_int),
                 ("sketch_mode", ctypes.c_int), ("sketch_dim", ctypes.c_int),
-                ("lanczos_rows_per_cta", ctypes.c_int)]
+                ("lanczos_rows_per_cta", ctypes.c_int), ("lanczos_path", ctypes.c_int)]
 
 
 class UsbsState(ctypes.Structure):
@@ -233,14 +233,17 @@ def usbs(sdp_state, n, m, trace_ub, trace_factor, rho, beta, k_curr, k_past, max
          lanczos_max_restarts, subprob_eps, subprob_max_iters, cond_exp_base=1.0,
          callback_fn=None, callback_static_args=None, callback_nonstatic_args=None, *, q0=None,
          precision=64, device="cuda", return_trace=False, return_info=False, instance=None,
-         stream=None, debug=None, log=None, renumber=False, lanczos_rows_per_cta=0):
+         stream=None, debug=None, log=None, renumber=False, lanczos_rows_per_cta=0,
+         lanczos_path=0):
     """``log``: True prints, a callable receives, the reference's per-check
     line (solver/usbs.py:514-530) at every condition check, t = 0 included.
     ``renumber``: solve the RCM-renumbered problem (locality for the device's
     sparse gathers) and return the result in the original numbering; the
     callback still sees P and Omega in the original numbering.
     ``lanczos_rows_per_cta``: rows per CTA of the cluster Lanczos (0: the
-    library's choice; a solve service that shares the GPU packs tighter)."""
+    library's choice; a solve service that shares the GPU packs tighter).
+    ``lanczos_path``: 2 keeps every problem too large for one cluster on the
+    stream path (no cooperative launch, so the solve can share the GPU)."""
     import torch
     if not torch.cuda.is_available():
         raise RuntimeError("usbs_gb300.usbs needs a CUDA device (GB300); none is visible")
@@ -288,6 +291,7 @@ def usbs(sdp_state, n, m, trace_ub, trace_factor, rho, beta, k_curr, k_past, max
     prm.cond_exp_base = float(cond_exp_base)
     prm.precision, prm.sketch_mode, prm.sketch_dim = int(precision), mode, sdim
     prm.lanczos_rows_per_cta = int(lanczos_rows_per_cta)
+    prm.lanczos_path = int(lanczos_path)
     pst = UsbsState()
     pst.ld = ld
     pst.y, pst.z, pst.V = _ptr(y), _ptr(z), _ptr(V)
