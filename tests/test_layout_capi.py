@@ -89,7 +89,7 @@ def test_library_builds_and_exports_every_declared_symbol():
         assert hasattr(lib, name), f"{name} declared in include/usbs_gb300.h but not exported"
     assert set(names) <= set(_lib.SIGNATURES), "ctypes signatures missing for some entry points"
     lib.usbs_abi_version.restype = ctypes.c_int
-    assert lib.usbs_abi_version() == 4
+    assert lib.usbs_abi_version() == 5
 
 
 def _as_set(A_data, A_idx, b, mask):
