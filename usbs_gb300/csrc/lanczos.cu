@@ -727,9 +727,13 @@ __device__ __forceinline__ int st_mode_of(int4 a, int4 b, int m, int* i, int* nv
   if (ii < m) { *nv = ii + 1; *buf = cur; return SM_STEP; }
   return SM_SKIP;
 }
+// Reads of the control block go through the read-only (L1) path: within a
+// kernel only its last CTA writes the block, after every other CTA has
+// finished, and the L1 caches start empty at each launch.  (Through L2 alone,
+// every warp of every CTA would queue on the same L2 line.)
 __device__ __forceinline__ int st_mode(const StreamCtl* c, int m, int* i, int* nv, int* buf) {
   const int4* p = (const int4*)c;
-  return st_mode_of(__ldcg(p), __ldcg(p + 1), m, i, nv, buf);
+  return st_mode_of(__ldg(p), __ldg(p + 1), m, i, nv, buf);
 }
 
 // ticket of the last CTA: true in every thread of the CTA that finished last
@@ -978,8 +982,8 @@ __global__ void __launch_bounds__(LZ_BLOCK, 8) st_sell_spmv_kernel(
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const int s = blockIdx.x * (LZ_BLOCK / 32) + warp;
   const bool has = s < (P.n + 31) / 32;
-  const int4 ca = __ldcg((const int4*)ctl), cb = __ldcg((const int4*)ctl + 1);
-  const double invb_d = __ldcg(&ctl->invb);
+  const int4 ca = __ldg((const int4*)ctl), cb = __ldg((const int4*)ctl + 1);
+  const double invb_d = __ldg(&ctl->invb);
   const int sb = has ? __ldg(P.sl_ptr + s) : 0;
   const int width = has ? (__ldg(P.sl_ptr + s + 1) - sb) >> 5 : 0;
   const int lr = has ? (int)__ldg(P.sl_row + 32 * s + lane) : 0;
@@ -1069,7 +1073,7 @@ __global__ void __launch_bounds__(LZ_BLOCK, 3) st_update_dot_kernel(
   if (mode == SM_SKIP) return;
   const int R = gridDim.x;
   const size_t ld = (size_t)P.ld;
-  for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) sh.hv[c] = (VT)__ldcg(&ctl->h1[c]);
+  for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) sh.hv[c] = (VT)__ldg(&ctl->h1[c]);
   __syncthreads();
   int c0, c1;
   st_chunks(P.n, &c0, &c1);
@@ -1113,7 +1117,7 @@ __global__ void __launch_bounds__(LZ_BLOCK, 2) st_update_dot1_kernel(
   if (mode == SM_SKIP) return;
   const int R = gridDim.x, n = P.n;
   const size_t ld = (size_t)P.ld;
-  for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) sh.hv[c] = (VT)__ldcg(&ctl->h1[c]);
+  for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) sh.hv[c] = (VT)__ldg(&ctl->h1[c]);
   extern __shared__ __align__(16) unsigned char st_dyn[];
   AT* sacc = (AT*)st_dyn;
   for (int c = 0; c < nv; ++c) sacc[c * LZ_BLOCK + threadIdx.x] = (AT)0;
@@ -1191,7 +1195,7 @@ __global__ void __launch_bounds__(LZ_BLOCK) st_update_norm_kernel(
   if (mode == SM_SKIP) return;
   const int R = gridDim.x;
   const size_t ld = (size_t)P.ld;
-  for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) sh.hv[c] = (VT)__ldcg(&ctl->h2[c]);
+  for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) sh.hv[c] = (VT)__ldg(&ctl->h2[c]);
   __syncthreads();
   int c0, c1;
   st_chunks(P.n, &c0, &c1);
@@ -1279,12 +1283,12 @@ template <typename VT>
 __global__ void __launch_bounds__(LZ_BLOCK) st_rotate_kernel(const __grid_constant__ TeamDesc<VT> P,
                                                               StreamCtl* ctl) {
   __shared__ StShared<VT> sh;
-  if (!__ldcg(&ctl->rot)) return;
-  const int m = P.m, kn = __ldcg(&ctl->k);
-  const bool stepped = __ldcg(&ctl->stepped) != 0;
-  const VT invb = (VT)__ldcg(&ctl->invb);
+  if (!__ldg(&ctl->rot)) return;
+  const int m = P.m, kn = __ldg(&ctl->k);
+  const bool stepped = __ldg(&ctl->stepped) != 0;
+  const VT invb = (VT)__ldg(&ctl->invb);
   const size_t ld = (size_t)P.ld;
-  const VT* lastv = P.vbuf + (size_t)(__ldcg(&ctl->cur) ^ 1) * ld;
+  const VT* lastv = P.vbuf + (size_t)(__ldg(&ctl->cur) ^ 1) * ld;
   for (int e = threadIdx.x; e < m * MAXM; e += LZ_BLOCK) {
     const int j = e / MAXM, c = e - j * MAXM;
     sh.u.Ys[e] = (c < kn) ? (VT)__ldcg(P.Ybuf + j * m + c) : (VT)0;
@@ -2014,10 +2018,18 @@ static int run_stream(const DeviceInfo& di, const LanczosProblem& p, cudaStream_
   const int ntiles = (p.n + LZ_BLOCK - 1) / LZ_BLOCK;
   const int G = lanczos_team_size(di, p.n, sizeof(VT) == 8 ? 64 : 32, true);   // partials per pass
   const int* occ = stream_occ<VT>();
+  // each kernel: at most one wave, and every CTA the same number of row
+  // chunks (A2 and C use 4 rows per thread, B 8 bytes per thread), so no
+  // CTA runs a last chunk alone
   int g[4];
   for (int j = 0; j < 4; ++j) {
-    g[j] = di.sm_count * occ[j];
-    if (g[j] > G) g[j] = G;
+    const int rows = (j == 1) ? (8 / (int)sizeof(VT)) * LZ_BLOCK : (j == 3 ? LZ_BLOCK : ST_ROWS);
+    const int nch = (p.n + rows - 1) / rows;
+    int gmax = di.sm_count * occ[j];
+    if (gmax > G) gmax = G;
+    if (gmax < 1) gmax = 1;
+    const int per = (nch + gmax - 1) / gmax;
+    g[j] = (nch + per - 1) / per;
     if (g[j] < 1) g[j] = 1;
   }
   TeamDesc<VT> t;
