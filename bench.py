@@ -665,6 +665,83 @@ def solves_leg(device):
     return out
 
 
+def serving_stream_leg(device, count=1024, iters=20, slots=16, serial_sample=32):
+    """The serving workload: `count` Erdos-Renyi MaxCut requests with Poisson
+    arrivals at 20/s, n log-uniform in [200, 50000], mean degree uniform in
+    [4, 40], unit weights; 30% are variants of an earlier request (1% of its
+    edges re-sampled) warm-started from that request's result on the device
+    (implicit warm start).  Each request runs `iters` outer iterations in mixed
+    precision through SolverService (the 1e-4 stop is thousands of iterations
+    away at the reference's settings), released at its arrival time.  Reported
+    beside the plain FP64 single-instance path run one request after another on
+    the first `serial_sample` cold requests."""
+    import torch
+    from usbs_gb300 import solver, workloads as wl
+    from usbs_gb300.problems import maxcut
+    from usbs_gb300.serving import SolveRequest, SolverService
+    S = SETTINGS
+    reqs = wl.serving_stream(count, 20.0, 4, 200, 50000, 4.0, 40.0, 0.3, 0.01)
+    prep = []
+    for r in reqs:                               # host set-up, before the clock starts
+        W = wl.stream_adjacency(r)
+        st = maxcut.initialize_state(W, S["sketch_dim"])
+        prep.append((r, W, st, solver.host_problem_layout(st)))
+
+    def kw(n):
+        return dict(n=n, m=n, trace_ub=S["trace_factor"] * n, trace_factor=S["trace_factor"],
+                    rho=S["rho"], beta=S["beta"], k_curr=S["k_curr"], k_past=S["k_past"],
+                    max_iters=iters, max_time=np.inf, obj_gap_eps=-1.0, infeas_gap_eps=-1.0,
+                    max_infeas_eps=-1.0, lanczos_inner_iterations=S["lanczos_inner_iterations"],
+                    lanczos_max_restarts=S["lanczos_max_restarts"],
+                    subprob_eps=S["subprob_eps"], subprob_max_iters=S["subprob_max_iters"])
+
+    # serial FP64 single-instance path on a sample of cold requests
+    cold = [(r, st) for r, _, st, _ in prep if r["warm_from"] < 0][:serial_sample]
+    solver.usbs(cold[0][1], precision=64, device=device, **kw(cold[0][0]["n"]))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for r, st in cold:
+        solver.usbs(st, precision=64, device=device, **kw(r["n"]))
+    torch.cuda.synchronize()
+    serial = (time.perf_counter() - t0) / len(cold)
+    with SolverService(device=device, max_slots=slots, reserve_bytes=8 << 30) as svc:
+        handles = []
+        t0 = time.perf_counter()
+        for r, W, st, lay in prep:
+            while time.perf_counter() - t0 < r["arrival"]:
+                time.sleep(0.0005)
+            warm = r["warm_from"] >= 0
+            req = SolveRequest(
+                st, precision=32, host_layout=lay,
+                warm_from=handles[r["warm_from"]] if warm else None,
+                warm_start=(lambda res, cold_st, W=W: maxcut.implicit_warm_start(
+                    res, W, S["sketch_dim"])) if warm else None,
+                **kw(r["n"]))
+            handles.append(svc.submit(req))
+        for h in handles:
+            h.wait(7200)
+        wall = time.perf_counter() - t0
+    lat = np.array([h.latency for h in handles])
+    gaps = np.array([h.info["obj_gap"] for h in handles])
+    ns = np.array([r["n"] for r in reqs])
+    big = ns > 20000
+    return {"requests": count, "arrivals": "Poisson 20/s", "n_range": [200, 50000],
+            "degree_range": [4, 40], "warm_fraction": 0.3,
+            "warm_started": int(sum(h.warmed for h in handles)),
+            "outer_iterations_each": iters, "slots": slots, "precision": "mixed",
+            "solves_per_s": count / wall, "wall_s": wall,
+            "p50_latency_s": float(np.percentile(lat, 50)),
+            "p99_latency_s": float(np.percentile(lat, 99)),
+            "p99_latency_s_n_over_20000": float(np.percentile(lat[big], 99)) if big.any()
+            else None,
+            "median_obj_gap_reached": float(np.median(gaps)),
+            "serial_fp64_solves_per_s": 1.0 / serial,
+            "serial_sample": len(cold),
+            "ratio_vs_serial_fp64": (count / wall) * serial,
+            "note": "the serial FP64 rate is measured on the first cold requests, whose sizes "
+                    "follow the same distribution"}
+
+
 def profile_case(args):
     """One untimed run of a single piece of the workload, for profiler captures."""
     import torch
@@ -930,6 +1007,13 @@ def main():
             errors = {"instance": "er60 to 1e-4 (tests/golden/oracle_solves.json)",
                       **{p: rec[p]["errors_vs_oracle"] for p in ("fp64", "fp32") if p in rec}}
 
+    stream_serving = None
+    if rank == 0 and not args.no_serving:
+        try:
+            stream_serving = serving_stream_leg(device)
+        except Exception as exc:  # the main line is still reported
+            stream_serving = {"error": str(exc)[:200]}
+
     cpu = None
     if rank == 0:
         it, sec = cpu_oracle_iterations(st, n, args.cpu_iters)
@@ -964,6 +1048,7 @@ def main():
             "qap_l30": qapl,
             "eigsh_batched_48": batched,
             "serving": serving,
+            "serving_stream_1024": stream_serving,
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": int(h2d),
                     "d2h_bytes_per_step": int(d2h)},

@@ -162,3 +162,64 @@ def test_qap_explicit_warm_start_sketch_matches_oracle(cuda):
     _same_qap(pqap.explicit_warm_start(old, D, W, 6),
               oqap.get_explicit_warm_start_state(old, D, W, 6), rtol=1e-8)
 
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["implicit", "dual_only"])
+def test_warm_start_from_a_device_result_stays_on_the_device(cuda, kind):
+    """A finished solve's result (device tensors) warm-starts the grown problem
+    on the device: same values as the host transform of the same state, and the
+    iterate never leaves the GPU."""
+    import torch
+    from usbs_gb300 import solver
+    Wo, Wn = _graphs()
+    st = pmaxcut.initialize_state(Wo, 10)
+    n = st.C.shape[0]
+    res = solver.usbs(st, n, n, 2.0 * n, 2.0, 0.01, 0.25, 4, 1, 3, np.inf, -1.0, -1.0, -1.0, 32,
+                      10, 1e-7, 100, precision=64)
+    assert res.y.is_cuda and res.z.is_cuda and res.P.is_cuda
+    host = res._replace(y=res.y.cpu().numpy(), z=res.z.cpu().numpy(), P=res.P.cpu().numpy())
+    fn = pmaxcut.implicit_warm_start if kind == "implicit" else pmaxcut.dual_only_warm_start
+    dev_ws, host_ws = fn(res, Wn, 10), fn(host, Wn, 10)
+    fields = ("y", "z", "P", "Omega") if kind == "implicit" else ("y",)
+    for f in fields:
+        d = getattr(dev_ws, f)
+        assert isinstance(d, torch.Tensor) and d.is_cuda, f
+        np.testing.assert_allclose(d.cpu().numpy(), np.asarray(getattr(host_ws, f)), rtol=1e-13,
+                                   atol=1e-13)
+    assert abs(dev_ws.primal_obj - host_ws.primal_obj) <= 1e-12 * max(1.0, abs(host_ws.primal_obj))
+    assert dev_ws.tr_X == host_ws.tr_X and dev_ws.SCALE_X == host_ws.SCALE_X
+    # and the grown problem solves from either start to the same iterates
+    m = Wn.shape[0]
+    a = solver.usbs(dev_ws, m, m, 2.0 * m * dev_ws.SCALE_X, 2.0, 0.01, 0.25, 4, 1, 2, np.inf,
+                    -1.0, -1.0, -1.0, 32, 10, 1e-7, 100, precision=64)
+    b = solver.usbs(host_ws, m, m, 2.0 * m * host_ws.SCALE_X, 2.0, 0.01, 0.25, 4, 1, 2, np.inf,
+                    -1.0, -1.0, -1.0, 32, 10, 1e-7, 100, precision=64)
+    np.testing.assert_allclose(a.y.cpu().numpy(), b.y.cpu().numpy(), rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.gpu
+def test_service_warm_starts_a_request_from_its_parent(cuda):
+    from usbs_gb300.serving import SolveRequest, SolverService
+    Wo, Wn = _graphs()
+    n, m = Wo.shape[0], Wn.shape[0]
+    base = dict(trace_factor=2.0, rho=0.01, beta=0.25, k_curr=4, k_past=1, max_iters=3,
+                max_time=np.inf, obj_gap_eps=-1.0, infeas_gap_eps=-1.0, max_infeas_eps=-1.0,
+                lanczos_inner_iterations=32, lanczos_max_restarts=10, subprob_eps=1e-7,
+                subprob_max_iters=100)
+    with SolverService(max_slots=4, reserve_bytes=1 << 30) as svc:
+        parent = svc.submit(SolveRequest(pmaxcut.initialize_state(Wo, 10), precision=64, n=n,
+                                         m=n, trace_ub=2.0 * n, **base))
+        child = svc.submit(SolveRequest(
+            pmaxcut.initialize_state(Wn, 10), precision=64, n=m, m=m, trace_ub=2.0 * m,
+            warm_from=parent, warm_start=lambda res, cold: pmaxcut.implicit_warm_start(res, Wn, 10),
+            **base))
+        child.wait(600)
+        assert child.warmed and child.start >= parent.finish
+        # the same warm start done by hand from the parent's result
+        from usbs_gb300 import solver
+        ws = pmaxcut.implicit_warm_start(parent.result, Wn, 10)
+        ref = solver.usbs(ws, m, m, 2.0 * m * ws.SCALE_X, precision=64, **{
+            k: v for k, v in base.items() if k != "trace_factor"}, trace_factor=2.0)
+    np.testing.assert_allclose(child.result.y.cpu().numpy(), ref.y.cpu().numpy(), rtol=1e-12,
+                               atol=1e-14)

@@ -104,11 +104,14 @@ class Admission:
 
 class SolveRequest:
     """One usbs() call.  ``kwargs`` are usbs()'s arguments after ``sdp_state``
-    (n, m, trace_ub, ... as keywords); ``precision`` 32 or 64."""
+    (n, m, trace_ub, ... as keywords); ``precision`` 32 or 64.  ``host_layout``
+    (optional): the problem's layout prepared ahead (solver.host_problem_layout),
+    so that submit() does no host work on it."""
 
     def __init__(self, sdp_state, precision=32, tag=None, warm_from=None, warm_start=None,
-                 **kwargs):
+                 host_layout=None, **kwargs):
         self.sdp_state = sdp_state
+        self.host_layout = host_layout
         self.warm_from = warm_from
         self.warm_start = warm_start
         self.warmed = False
@@ -180,7 +183,8 @@ class SolverService:
         lib = _lib.load()
         solver._sigs(lib)
         kw = req.kwargs
-        host = solver.host_problem_layout(req.sdp_state)
+        host = req.host_layout if req.host_layout is not None else \
+            solver.host_problem_layout(req.sdp_state)
         req._host_layout = host
         n = kw["n"]
         k = kw["k_curr"] + kw["k_past"]
