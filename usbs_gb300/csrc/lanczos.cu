@@ -1034,106 +1034,6 @@ __global__ void __launch_bounds__(LZ_BLOCK, 8) st_sell_spmv_kernel(
   }
 }
 
-// A (fused): A1 and A2 in one kernel.  Each CTA walks windows b, b + grid, ...:
-// the window's y = Op x by the sliced-ELL SpMV above (x gathers, latency
-// bound), then the dots of its 256 rows with the basis columns (streaming),
-// accumulated per thread in shared memory; so the basis streams while other
-// warps of the SM wait on gathers.  Breakdown mode: the window's rows of the
-// Gaussian replacement vector and their dots with the first i columns.
-template <typename VT>
-__global__ void __launch_bounds__(LZ_BLOCK) st_spmv_dot_kernel(
-    const __grid_constant__ TeamDesc<VT> P, StreamCtl* ctl) {
-  typedef typename Acc<VT>::type AT;
-  __shared__ VT ys[LZ_BLOCK];
-  __shared__ StShared<VT> sh;
-  const int4 ca = __ldg((const int4*)ctl), cb = __ldg((const int4*)ctl + 1);
-  const double invb_d = __ldg(&ctl->invb);
-  int i, nv, buf;
-  const int mode = st_mode_of(ca, cb, P.m, &i, &nv, &buf);
-  if (mode == SM_SKIP) return;
-  const size_t ld = (size_t)P.ld;
-  const int k = ca.y;
-  const bool step = mode == SM_STEP;
-  const bool wq = step && i > k;
-  const VT xscale = wq ? (VT)invb_d : (VT)1;
-  const VT* __restrict__ x = wq ? P.vbuf + (size_t)(buf ^ 1) * ld : P.Q + (size_t)k * ld;
-  VT* vout = P.vbuf + (size_t)buf * ld;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const int ns = (P.n + 31) / 32, nwin = (P.n + LZ_BLOCK - 1) / LZ_BLOCK;
-  extern __shared__ __align__(16) unsigned char st_dyn[];
-  AT* sacc = (AT*)st_dyn;
-  for (int c = 0; c < nv; ++c) sacc[c * LZ_BLOCK + threadIdx.x] = (AT)0;
-  for (int win = blockIdx.x; win < nwin; win += gridDim.x) {
-    const int w0 = win * LZ_BLOCK, row = w0 + threadIdx.x;
-    VT y = (VT)0, xn = (VT)0;
-    if (step) {
-      const int s = win * (LZ_BLOCK / 32) + warp;
-      const bool has = s < ns;
-      const int sb = has ? __ldg(P.sl_ptr + s) : 0;
-      const int width = has ? (__ldg(P.sl_ptr + s + 1) - sb) >> 5 : 0;
-      const int lr = has ? (int)__ldg(P.sl_row + 32 * s + lane) : 0;
-      if (wq && row < P.n) xn = __ldg(x + row) * xscale;
-      if (has) {
-        const int* cp = P.sl_col + sb + lane;
-        const VT* vp = P.sl_val + sb + lane;
-        constexpr int PF = 16;
-        int c[PF];
-        VT v[PF], xv[PF];
-#pragma unroll
-        for (int u = 0; u < PF; ++u) {
-          c[u] = (u < width) ? __ldg(cp + 32 * u) : 0;
-          v[u] = (u < width) ? __ldg(vp + 32 * u) : (VT)0;
-        }
-#pragma unroll
-        for (int u = 0; u < PF; ++u) xv[u] = (u < width) ? __ldg(x + c[u]) : (VT)0;
-        AT acc = (AT)0;
-#pragma unroll
-        for (int u = 0; u < PF; ++u) acc += (AT)v[u] * (AT)xv[u];
-        for (int u = PF; u < width; ++u)
-          acc += (AT)__ldg(vp + 32 * u) * (AT)__ldg(x + __ldg(cp + 32 * u));
-        const int r = w0 + lr;
-        if (r < P.n && width == P.wcap) {
-          const int e = P.rowptr[r + 1];
-          for (int q = P.rowptr[r] + P.wcap; q < e; ++q)
-            acc += (AT)__ldg(P.val + q) * (AT)__ldg(x + __ldg(P.col + q));
-        }
-        ys[lr] = (VT)acc;
-      }
-      __syncthreads();
-      if (row < P.n) {
-        y = ys[threadIdx.x] * xscale;
-        vout[row] = y;
-        if (wq) P.Q[(size_t)i * ld + row] = xn;
-      }
-      __syncthreads();    // ys is reused by the next window
-    } else if (row < P.n) {
-      y = (VT)hash_normal((uint64_t)i, (uint64_t)row);
-      P.vbuf[(size_t)buf * ld + row] = y;
-    }
-    if (row < P.n) {
-      // dots of the row with the basis columns c < nv (column i is x itself)
-      constexpr int NB = 8;
-#pragma unroll 1
-      for (int c0 = 0; c0 < nv; c0 += NB) {
-        VT q[NB];
-#pragma unroll
-        for (int b = 0; b < NB; ++b) {
-          const int c = c0 + b;
-          q[b] = (c < nv) ? ((wq && c == i) ? xn : __ldg(P.Q + (size_t)c * ld + row)) : (VT)0;
-        }
-#pragma unroll
-        for (int b = 0; b < NB; ++b)
-          if (c0 + b < nv) sacc[(c0 + b) * LZ_BLOCK + threadIdx.x] += (AT)q[b] * (AT)y;
-      }
-    }
-  }
-  st_block_cols(sacc, nv, P.part + blockIdx.x, gridDim.x);
-  if (!st_last_cta(&ctl->ticket[0], sh)) return;
-  st_reduce<VT>(P.part, gridDim.x, nv, sh);
-  for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) ctl->h1[c] = sh.h[c];
-  if (threadIdx.x == 0) ctl->ticket[0] = 0u;
-}
-
 // A2: h1[c] = Q[:, c] . v for c < nv (v = the step's y, or the breakdown vector)
 template <typename VT>
 __global__ void __launch_bounds__(LZ_BLOCK) st_dot_kernel(const __grid_constant__ TeamDesc<VT> P,
@@ -2071,8 +1971,7 @@ static const int* stream_occ() {
   static int occ[4] = {0, 0, 0, 0};
   static std::once_flag once;
   std::call_once(once, [] {
-    const void* ks[] = {(const void*)st_spmv_dot_kernel<VT>,
-                        (const void*)st_update_dot1_kernel<VT>,
+    const void* ks[] = {(const void*)st_dot_kernel<VT>, (const void*)st_update_dot1_kernel<VT>,
                         (const void*)st_update_norm_kernel<VT>,
                         (const void*)st_rotate_kernel<VT>};
     const size_t dyn[] = {st_sacc_bytes<VT>(), st_sacc_bytes<VT>(), 0, 0};
@@ -2124,8 +2023,7 @@ static int run_stream(const DeviceInfo& di, const LanczosProblem& p, cudaStream_
   // CTA runs a last chunk alone
   int g[4];
   for (int j = 0; j < 4; ++j) {
-    const int rows = (j == 1) ? (8 / (int)sizeof(VT)) * LZ_BLOCK
-                              : ((j == 0 || j == 3) ? LZ_BLOCK : ST_ROWS);
+    const int rows = (j == 1) ? (8 / (int)sizeof(VT)) * LZ_BLOCK : (j == 3 ? LZ_BLOCK : ST_ROWS);
     const int nch = (p.n + rows - 1) / rows;
     int gmax = di.sm_count * occ[j];
     if (gmax > G) gmax = G;
@@ -2180,13 +2078,14 @@ static int run_stream(const DeviceInfo& di, const LanczosProblem& p, cudaStream_
     }
     const int slots = (p.m - i_host) + (bd_host ? 1 : 0);
     for (int j = 0; j < slots; ++j) {
-      st_spmv_dot_kernel<VT><<<g[0], LZ_BLOCK, st_sacc_bytes<VT>(), stream>>>(t, ctl);
+      st_sell_spmv_kernel<VT><<<ntiles, LZ_BLOCK, 0, stream>>>(t, ctl);
+      st_dot_kernel<VT><<<g[0], LZ_BLOCK, st_sacc_bytes<VT>(), stream>>>(t, ctl);
       st_update_dot1_kernel<VT><<<g[1], LZ_BLOCK, st_sacc_bytes<VT>(), stream>>>(t, ctl);
       st_update_norm_kernel<VT><<<g[2], LZ_BLOCK, 0, stream>>>(t, ctl);
     }
     st_restart_kernel<VT><<<1, LZ_BLOCK, 0, stream>>>(t, ctl);
     st_rotate_kernel<VT><<<g[3], LZ_BLOCK, 0, stream>>>(t, ctl);
-    t_launches += 3 * slots + 2;
+    t_launches += 4 * slots + 2;
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) {
       set_error("lanczos: stream-path launch failed: %s", cudaGetErrorString(e));
