@@ -736,6 +736,15 @@ __device__ __forceinline__ int st_mode(const StreamCtl* c, int m, int* i, int* n
   return st_mode_of(__ldg(p), __ldg(p + 1), m, i, nv, buf);
 }
 
+// Programmatic dependent launch: each stream kernel lets the next one in the
+// stream launch as soon as all of its own CTAs have started, then waits until
+// the previous kernel has finished and its writes are visible.  The next
+// kernel's launch thus overlaps this one's tail; no data is read early.
+__device__ __forceinline__ void st_pdl_prologue() {
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+}
+
 // ticket of the last CTA: true in every thread of the CTA that finished last
 // (its partial sums, fenced by their writers, are then visible to it)
 template <typename SH>
@@ -975,6 +984,7 @@ __global__ void __launch_bounds__(LZ_BLOCK) st_sell_fill_kernel(
 template <typename VT>
 __global__ void __launch_bounds__(LZ_BLOCK, 8) st_sell_spmv_kernel(
     const __grid_constant__ TeamDesc<VT> P, StreamCtl* ctl) {
+  st_pdl_prologue();
   typedef typename Acc<VT>::type AT;
   __shared__ VT ys[LZ_BLOCK];
   // every load that depends on no other is issued first: the control block,
@@ -1038,6 +1048,7 @@ __global__ void __launch_bounds__(LZ_BLOCK, 8) st_sell_spmv_kernel(
 template <typename VT>
 __global__ void __launch_bounds__(LZ_BLOCK) st_dot_kernel(const __grid_constant__ TeamDesc<VT> P,
                                                            StreamCtl* ctl) {
+  st_pdl_prologue();
   typedef typename Acc<VT>::type AT;
   __shared__ StShared<VT> sh;
   int i, nv, buf;
@@ -1061,53 +1072,13 @@ __global__ void __launch_bounds__(LZ_BLOCK) st_dot_kernel(const __grid_constant_
   if (threadIdx.x == 0) ctl->ticket[0] = 0u;
 }
 
-// B: v -= Q h1 (c < nv), h2 = Q^T v; on a step, alpha[i] = h1[i] + h2[i].  The
-// dots re-read the thread's rows of Q, by then in L1 or L2.
-template <typename VT>
-__global__ void __launch_bounds__(LZ_BLOCK, 3) st_update_dot_kernel(
-    const __grid_constant__ TeamDesc<VT> P, StreamCtl* ctl) {
-  typedef typename Acc<VT>::type AT;
-  __shared__ StShared<VT> sh;
-  int i, nv, buf;
-  const int mode = st_mode(ctl, P.m, &i, &nv, &buf);
-  if (mode == SM_SKIP) return;
-  const int R = gridDim.x;
-  const size_t ld = (size_t)P.ld;
-  for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) sh.hv[c] = (VT)__ldg(&ctl->h1[c]);
-  __syncthreads();
-  int c0, c1;
-  st_chunks(P.n, &c0, &c1);
-  VT* v = P.vbuf + (size_t)buf * ld;
-  extern __shared__ __align__(16) unsigned char st_dyn[];
-  AT* sacc = (AT*)st_dyn;
-  for (int c = 0; c < nv; ++c) sacc[c * LZ_BLOCK + threadIdx.x] = (AT)0;
-  for (int ch = c0; ch < c1; ++ch) {
-    const int r4 = ch * ST_ROWS + 4 * threadIdx.x;
-    if (r4 >= P.n) continue;
-    Row4<VT> x = ld4<VT, false>(v, r4, P.n);
-    const Row4<VT> s = st_combine(P.Q, ld, r4, P.n, nv, sh.hv);
-#pragma unroll
-    for (int j = 0; j < 4; ++j) x.v[j] -= s.v[j];
-    st4(v, r4, P.n, x);
-    st_dots(P.Q, ld, r4, P.n, nv, x, sacc);
-  }
-  double* part = P.part + (size_t)MP1 * R;
-  st_block_cols(sacc, nv, part + blockIdx.x, R);
-  if (!st_last_cta(&ctl->ticket[1], sh)) return;
-  st_reduce<VT>(part, R, nv, sh);
-  for (int c = threadIdx.x; c < nv; c += LZ_BLOCK) ctl->h2[c] = sh.h[c];
-  if (threadIdx.x == 0) {
-    if (mode == SM_STEP) ctl->alpha[i] = __ldcg(&ctl->h1[i]) + sh.h[i];
-    ctl->ticket[1] = 0u;
-  }
-}
-
 // B, one pass over Q: each thread keeps its rows of the nv basis columns in
 // registers (8-byte loads: two FP32 rows or one FP64 row), forms
 // v -= Q h1, then h2 = Q^T v from the same registers.
 template <typename VT>
 __global__ void __launch_bounds__(LZ_BLOCK, 2) st_update_dot1_kernel(
     const __grid_constant__ TeamDesc<VT> P, StreamCtl* ctl) {
+  st_pdl_prologue();
   typedef typename Acc<VT>::type AT;
   constexpr int RW = 8 / (int)sizeof(VT);           // rows per thread
   constexpr int CROWS = RW * LZ_BLOCK;              // rows per chunk
@@ -1188,6 +1159,7 @@ __global__ void __launch_bounds__(LZ_BLOCK, 2) st_update_dot1_kernel(
 template <typename VT>
 __global__ void __launch_bounds__(LZ_BLOCK) st_update_norm_kernel(
     const __grid_constant__ TeamDesc<VT> P, StreamCtl* ctl) {
+  st_pdl_prologue();
   typedef typename Acc<VT>::type AT;
   __shared__ StShared<VT> sh;
   int i, nv, buf;
@@ -1247,6 +1219,7 @@ __global__ void __launch_bounds__(LZ_BLOCK) st_update_norm_kernel(
 template <typename VT>
 __global__ void __launch_bounds__(LZ_BLOCK, 1) st_restart_kernel(
     const __grid_constant__ TeamDesc<VT> P, StreamCtl* ctl) {
+  st_pdl_prologue();
   __shared__ LzShared<VT> sh;
   const int m = P.m, tid = threadIdx.x;
   if (ctl->stop || ctl->rot || ctl->bd || ctl->i < m) return;
@@ -1282,6 +1255,7 @@ __global__ void __launch_bounds__(LZ_BLOCK, 1) st_restart_kernel(
 template <typename VT>
 __global__ void __launch_bounds__(LZ_BLOCK) st_rotate_kernel(const __grid_constant__ TeamDesc<VT> P,
                                                               StreamCtl* ctl) {
+  st_pdl_prologue();
   __shared__ StShared<VT> sh;
   if (!__ldg(&ctl->rot)) return;
   const int m = P.m, kn = __ldg(&ctl->k);
@@ -2002,6 +1976,24 @@ int lanczos_stream_occupancy(int prec) {
 // the control block back once (a synchronisation of `stream`) to learn where
 // the next cycle starts and whether the loop has ended.  The loop state is
 // on the device, so a step that is not needed only returns.
+// a stream kernel launched with programmatic stream serialisation (see
+// st_pdl_prologue)
+template <typename... KArgs, typename... Args>
+static cudaError_t launch_pdl(void (*kernel)(KArgs...), int grid, size_t smem,
+                              cudaStream_t stream, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)grid);
+  cfg.blockDim = dim3(LZ_BLOCK);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 template <typename VT>
 static int run_stream(const DeviceInfo& di, const LanczosProblem& p, cudaStream_t stream) {
   if (p.m > MAXM || p.m < 1 || p.n < 1 || p.ld < p.n) {
@@ -2077,16 +2069,18 @@ static int run_stream(const DeviceInfo& di, const LanczosProblem& p, cudaStream_
       return -5;
     }
     const int slots = (p.m - i_host) + (bd_host ? 1 : 0);
-    for (int j = 0; j < slots; ++j) {
-      st_sell_spmv_kernel<VT><<<ntiles, LZ_BLOCK, 0, stream>>>(t, ctl);
-      st_dot_kernel<VT><<<g[0], LZ_BLOCK, st_sacc_bytes<VT>(), stream>>>(t, ctl);
-      st_update_dot1_kernel<VT><<<g[1], LZ_BLOCK, st_sacc_bytes<VT>(), stream>>>(t, ctl);
-      st_update_norm_kernel<VT><<<g[2], LZ_BLOCK, 0, stream>>>(t, ctl);
+    cudaError_t e = cudaSuccess;
+    for (int j = 0; j < slots && e == cudaSuccess; ++j) {
+      e = launch_pdl(st_sell_spmv_kernel<VT>, ntiles, 0, stream, t, ctl);
+      if (e == cudaSuccess) e = launch_pdl(st_dot_kernel<VT>, g[0], st_sacc_bytes<VT>(), stream, t, ctl);
+      if (e == cudaSuccess)
+        e = launch_pdl(st_update_dot1_kernel<VT>, g[1], st_sacc_bytes<VT>(), stream, t, ctl);
+      if (e == cudaSuccess) e = launch_pdl(st_update_norm_kernel<VT>, g[2], 0, stream, t, ctl);
     }
-    st_restart_kernel<VT><<<1, LZ_BLOCK, 0, stream>>>(t, ctl);
-    st_rotate_kernel<VT><<<g[3], LZ_BLOCK, 0, stream>>>(t, ctl);
+    if (e == cudaSuccess) e = launch_pdl(st_restart_kernel<VT>, 1, 0, stream, t, ctl);
+    if (e == cudaSuccess) e = launch_pdl(st_rotate_kernel<VT>, g[3], 0, stream, t, ctl);
     t_launches += 4 * slots + 2;
-    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaGetLastError();
     if (e != cudaSuccess) {
       set_error("lanczos: stream-path launch failed: %s", cudaGetErrorString(e));
       return -5;
