@@ -794,6 +794,8 @@ def main():
     ap.add_argument("--iters-per-step", type=int, default=10)
     ap.add_argument("--cpu-iters", type=int, default=24)
     ap.add_argument("--no-spmv", action="store_true")
+    ap.add_argument("--no-solves", action="store_true",
+                    help="skip the solves-to-a-gap leg (the main line is unchanged)")
     ap.add_argument("--no-serving", action="store_true",
                     help="skip the serving, QAP and batched-eigsh legs (the main line is unchanged)")
     ap.add_argument("--profile-case", choices=["usbs", "spmv", "eigsh-rgg"], default=None,
@@ -990,7 +992,7 @@ def main():
     _, fp64_value = replica_throughput(e4.elapsed_time(e5), fp64_iters, world, device)
 
     solves = errors = None
-    if rank == 0 and not args.no_serving:
+    if rank == 0 and not args.no_solves:
         try:
             solves = {"device": solves_leg(device), "oracle": oracle_solve_rates()}
         except Exception as exc:  # the main line is still reported

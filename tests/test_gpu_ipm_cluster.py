@@ -44,8 +44,8 @@ print(json.dumps(out))
 """ % ROOT
 
 
-def _run(ctas):
-    env = dict(os.environ, USBS_IPM_CTAS=str(ctas))
+def _run(ctas, cl_ls=1):
+    env = dict(os.environ, USBS_IPM_CTAS=str(ctas), USBS_IPM_CL_LS=str(cl_ls))
     r = subprocess.run([sys.executable, "-c", SCRIPT], env=env, capture_output=True, text=True,
                        timeout=900)
     assert r.returncode == 0, r.stderr[-3000:]
@@ -56,6 +56,13 @@ def _run(ctas):
 def test_cluster_ipm_is_bit_identical_to_one_cta(cuda, ctas):
     one, many = _run(1), _run(ctas)
     assert one.keys() == many.keys()
+    for key in one:
+        assert one[key]["trace"] == many[key]["trace"], key
+        assert one[key]["y"] == many[key]["y"], key
+
+
+def test_cluster_ipm_with_the_one_cta_line_search_is_bit_identical(cuda):
+    one, many = _run(1), _run(4, cl_ls=0)
     for key in one:
         assert one[key]["trace"] == many[key]["trace"], key
         assert one[key]["y"] == many[key]["y"], key

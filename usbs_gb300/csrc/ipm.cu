@@ -876,7 +876,7 @@ __global__ void __launch_bounds__(IPM_BLOCK, 1) ipm_kernel(const __grid_constant
     // first PD point undecided, every CTA runs the single-CTA search below
     int clS = -1, clT = -1;
     bool cl_done = false;
-    if (C > 1) {
+    if (C > 1 && A.cl_line_search) {
       if (wid == 0) {
         const int half = lane >> 4, sub = lane & 15;
         const double* M = half ? sh.T : sh.S;
@@ -1175,7 +1175,13 @@ static int ipm_ctas() {
   return c;
 }
 
-int launch_ipm(const IpmArgs& a, cudaStream_t st) {
+int launch_ipm(const IpmArgs& a_in, cudaStream_t st) {
+  IpmArgs a = a_in;
+  static const int cl_ls = [] {
+    const char* e = getenv("USBS_IPM_CL_LS");
+    return e ? atoi(e) : 1;
+  }();
+  a.cl_line_search = cl_ls;
   const int s = a.k * (a.k + 1) / 2;
   const int C = ipm_ctas();
   const size_t dyn = (size_t)(C > 1 ? 3 : 2) * s * s * sizeof(double);

@@ -118,7 +118,11 @@ def _problem(D, W):
     sa = 1.0 / rownorm
     A_mat = sp.csr_matrix((sa[A_idx[:, 0]] * A_data, (A_idx[:, 0], A_idx[:, 1] * N + A_idx[:, 2])),
                           shape=(m, N * N))
-    lam = eigsh(A_mat @ A_mat.T, k=1, which="LM", return_eigenvectors=False,
+    # ||A||_2^2 by ARPACK as in the reference, from a fixed start vector: the
+    # default random start makes the scaling, and with it every later bit of
+    # the solve, differ between processes
+    AAt = A_mat @ A_mat.T
+    lam = eigsh(AAt, k=1, which="LM", return_eigenvectors=False, v0=np.ones(AAt.shape[0]),
                 maxiter=np.iinfo(np.int32).max)[0]
     return C, A_data, A_idx, b, mask, scale_c, scale_x, sa / np.sqrt(lam)
 
