@@ -13,7 +13,6 @@
 //    iteration derives from it (solver/usbs.py:409-412, 568-585, 627-644).
 //  * cholqr_kernel  R^-1 of one (shifted) Cholesky-QR pass for the new bundle
 //    basis (replaces the Householder QR of solver/usbs.py:641-642).
-#include <stdlib.h>
 #include "common.cuh"
 #include "dense.cuh"
 #include "internal.h"
@@ -375,240 +374,17 @@ __device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* dinv,
   __syncthreads();
 }
 
-// ---- the IPM on a thread-block cluster ----
-// With C > 1 CTAs in the cluster every CTA runs the whole interior-point loop
-// on identical data (so every scalar, vector and branch is the same in all of
-// them), except three parts split across the cluster: the Newton matrix's
-// columns (CTA r owns columns c with c % C == r, assembled and eliminated only
-// there), the LU's trailing updates, and the line search's grid points.  The
-// LU performs exactly the single-CTA arithmetic, so the results are the same.
-__device__ __forceinline__ unsigned ipm_cl_rank() {
-  unsigned r;
-  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
-  return r;
-}
-__device__ __forceinline__ unsigned ipm_cl_size() {
-  unsigned r;
-  asm volatile("mov.u32 %0, %%cluster_nctarank;" : "=r"(r));
-  return r;
-}
-__device__ __forceinline__ void ipm_cl_sync() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\n\t"
-               "barrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-__device__ __forceinline__ uint32_t ipm_cl_map(const void* p, unsigned rank) {
-  const uint32_t a = (uint32_t)__cvta_generic_to_shared(p);
-  uint32_t r;
-  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
-  return r;
-}
-__device__ __forceinline__ void ipm_cl_st(uint32_t a, double v) {
-  asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(a), "d"(v) : "memory");
-}
-__device__ __forceinline__ void ipm_cl_st(uint32_t a, int v) {
-  asm volatile("st.shared::cluster.s32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
-}
-__device__ __forceinline__ void ipm_cl_st(uint32_t a, unsigned v) {
-  asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
-}
-
-// LU with partial pivoting and solve over a cluster of C CTAs (this is rank
-// r): the single-CTA ipm_lu_solve with column c of A held by CTA c % C at
-// AL[(c / C) * lda + i].  Per column j the owner of column j+1 updates it,
-// picks its pivot and forms its multipliers (warp 0, the look-ahead) and
-// writes them, the pivot row and the reciprocal into every CTA; the other
-// threads of every CTA apply column j's update to their own columns; one
-// cluster barrier ends the column.  b, the multipliers and the pivot
-// reciprocals are replicated.  For the back substitution the columns of U are
-// gathered into CTA 0 (Uf, column-major) and the solution is written back into
-// every CTA's b.
-__device__ void ipm_lu_solve_cl(double* AL, int lda, double* b, int n, double* dinv, double* lcol,
-                                double* lnext, int* pnext, double* Uf, int* ok_out, unsigned C,
-                                unsigned r) {
-  const int tid = threadIdx.x, lane = tid & 31;
-  const int nloc = (n - (int)r + (int)C - 1) / (int)C;   // columns r, r + C, ...
-  double* lc = lcol;
-  double* ln = lnext;
-  // warp 0 of the owner of column j: pivot, reciprocal and multipliers of the
-  // (updated) column values v, written into every CTA's `lout`
-  auto pick = [&](int j, const double (&v)[LU_RPL], double* lout) {
-    unsigned long long best = 0ull;
-    int bi = 0x7fffffff;
-#pragma unroll
-    for (int q = 0; q < LU_RPL; ++q) {
-      const int i = j + lane + 32 * q;
-      if (i < n) {
-        const unsigned long long kk = abs_key(v[q]);
-        if (bi == 0x7fffffff || kk > best) { best = kk; bi = i; }
-      }
-    }
-    const unsigned hi = (unsigned)(best >> 32), lo = (unsigned)best;
-    const unsigned mhi = __reduce_max_sync(0xffffffffu, hi);
-    const bool th = (bi != 0x7fffffff) && hi == mhi;
-    const unsigned mlo = __reduce_max_sync(0xffffffffu, th ? lo : 0u);
-    const bool tl = th && lo == mlo;
-    const unsigned mrow = __reduce_min_sync(0xffffffffu, tl ? (unsigned)bi : 0xffffffffu);
-    double bv;
-    if (mrow == 0xffffffffu) {
-      bi = j;
-      bv = v[0];
-      bv = __shfl_sync(0xffffffffu, bv, 0);
-    } else {
-      bi = (int)mrow;
-      const int off = bi - j;
-      double sel = 0.0;
-#pragma unroll
-      for (int q = 0; q < LU_RPL; ++q) if (q == (off >> 5)) sel = v[q];
-      bv = __shfl_sync(0xffffffffu, sel, off & 31);
-    }
-    const double inv = (bv == 0.0) ? 1.0 : 1.0 / bv;
-    for (unsigned rr = 0; rr < C; ++rr) {
-      const uint32_t lo_a = ipm_cl_map(lout, rr);
-#pragma unroll
-      for (int q = 0; q < LU_RPL; ++q) {
-        const int i = j + lane + 32 * q;
-        if (i < n) ipm_cl_st(lo_a + 8u * (uint32_t)i, v[q] * inv);
-      }
-      if (lane == 0) {
-        ipm_cl_st(ipm_cl_map(pnext + (j & 1), rr), bi);
-        ipm_cl_st(ipm_cl_map(dinv + j, rr), inv);
-      }
-    }
-    if (lane == 0 && bv == 0.0) *ok_out = 0;
-  };
-  if (tid == 0) *ok_out = 1;
-  __syncthreads();
-  if (r == 0 && tid < 32) {          // column 0 is CTA 0's first column
-    double v[LU_RPL];
-#pragma unroll
-    for (int q = 0; q < LU_RPL; ++q) {
-      const int i = lane + 32 * q;
-      v[q] = (i < n) ? AL[i] : 0.0;
-    }
-    pick(0, v, lc);
-  }
-  ipm_cl_sync();
-  for (int j = 0; j < n; ++j) {
-    const int piv = pnext[j & 1];
-    if (piv != j) {
-      for (int q = tid; q < nloc; q += blockDim.x) {
-        const int c = q * (int)C + (int)r;
-        if (c >= j) {
-          const double t = AL[q * lda + j];
-          AL[q * lda + j] = AL[q * lda + piv];
-          AL[q * lda + piv] = t;
-        }
-      }
-      if (tid == 0) {
-        const double t = b[j]; b[j] = b[piv]; b[piv] = t;
-        lc[piv] = lc[j];
-      }
-      __syncthreads();
-    }
-    const int w = n - j - 1;
-    if (w == 0) break;
-    const unsigned o1 = (unsigned)((j + 1) % (int)C);
-    const bool look = (r == o1) && tid < 32;
-    if (look) {
-      double* colj1 = AL + (size_t)((j + 1) / (int)C) * lda;
-      const double ujn = colj1[j];
-      double a[LU_RPL], l[LU_RPL];
-#pragma unroll
-      for (int q = 0; q < LU_RPL; ++q) {
-        const int i = j + 1 + lane + 32 * q;
-        a[q] = (i < n) ? colj1[i] : 0.0;
-        l[q] = (i < n) ? lc[i] : 0.0;
-      }
-      double v[LU_RPL];
-#pragma unroll
-      for (int q = 0; q < LU_RPL; ++q) {
-        const int i = j + 1 + lane + 32 * q;
-        v[q] = a[q] - l[q] * ujn;
-        if (i < n) colj1[i] = v[q];
-      }
-      pick(j + 1, v, ln);
-    } else {
-      const int t = (r == o1) ? tid - 32 : tid;
-      const int nt = (r == o1) ? (int)blockDim.x - 32 : (int)blockDim.x;
-      if (t < w) {
-        const int i = j + 1 + t;
-        b[i] = b[i] - lc[i] * b[j];
-      }
-      // own columns c >= j + 2: local index from q0 on
-      int q0 = (j + 2 - (int)r + (int)C - 1) / (int)C;
-      if (q0 < 0) q0 = 0;
-      const int ncols = nloc - q0;
-      if (ncols > 0 && w > 1) {
-        const int cpp = nt / w > 0 ? nt / w : 1;
-        const int cc = t / w, rr = t - (t / w) * w;
-        if (cc < cpp && t < cpp * w) {
-          const int i = j + 1 + rr;
-          const double li = lc[i];
-          for (int q = q0 + cc; q < nloc; q += cpp) {
-            double* col = AL + (size_t)q * lda;
-            col[i] = col[i] - li * col[j];
-          }
-        }
-      }
-    }
-    ipm_cl_sync();
-    double* tsw = lc; lc = ln; ln = tsw;
-  }
-  // U into CTA 0, column-major (lda), then the back substitution there
-  {
-    const uint32_t ub = ipm_cl_map(Uf, 0);
-    for (int e = tid; e < nloc * n; e += blockDim.x) {
-      const int q = e / n, i = e - q * n;
-      const int c = q * (int)C + (int)r;
-      ipm_cl_st(ub + 8u * (uint32_t)(c * lda + i), AL[q * lda + i]);
-    }
-  }
-  ipm_cl_sync();
-  if (r == 0 && tid < 32) {
-    double br[LU_RPL];
-#pragma unroll
-    for (int q = 0; q < LU_RPL; ++q) br[q] = (lane + 32 * q < n) ? b[lane + 32 * q] : 0.0;
-    for (int j = n - 1; j >= 0; --j) {
-      const int oq = j >> 5, ol = j & 31;
-      double bj = 0.0;
-#pragma unroll
-      for (int q = 0; q < LU_RPL; ++q) if (q == oq) bj = br[q];
-      bj = __shfl_sync(0xffffffffu, bj, ol) * dinv[j];
-      const double* colj = Uf + (size_t)j * lda;
-#pragma unroll
-      for (int q = 0; q < LU_RPL; ++q) {
-        const int i = lane + 32 * q;
-        if (i == j) br[q] = bj;
-        else if (i < j) br[q] -= colj[i] * bj;
-      }
-    }
-    for (unsigned rr = 0; rr < C; ++rr) {
-      const uint32_t bb = ipm_cl_map(b, rr);
-#pragma unroll
-      for (int q = 0; q < LU_RPL; ++q)
-        if (lane + 32 * q < n) ipm_cl_st(bb + 8u * (uint32_t)(lane + 32 * q), br[q]);
-    }
-  }
-  ipm_cl_sync();
-}
-
 __global__ void __launch_bounds__(IPM_BLOCK, 1) ipm_kernel(const __grid_constant__ IpmArgs A) {
   extern __shared__ double dyn[];
   __shared__ IpmShared sh;
   __shared__ IpmScal sc;
   __shared__ double grid[256];
   __shared__ int s_piv, s_ok;
-  __shared__ double lnx[IPM_MAXS];   // cluster LU: multipliers of the next column
-  __shared__ int pnx[2];             // cluster LU: pivot rows, by column parity
-  __shared__ unsigned lsmask[8];     // cluster line search: PD masks by CTA
   if (A.skip && *A.skip) return;
   const int k = A.k, s = k * (k + 1) / 2, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   const int nw = IPM_BLOCK / 32;
-  const unsigned C = ipm_cl_size(), crank = ipm_cl_rank();
-  const bool lead = crank == 0;      // writes the outputs
   double* Q11 = dyn;            // s*s (mode 0)
-  double* coeff = dyn + s * s;  // s*s (with C > 1: this CTA's columns c % C == crank)
-  double* Uf = dyn + 2 * s * s; // C > 1, CTA 0: U gathered for the back substitution
+  double* coeff = dyn + s * s;  // s*s
   double* sm = A.smalls;
   if (tid == 0) {
     int a = 0, o = 0;
@@ -775,10 +551,8 @@ __global__ void __launch_bounds__(IPM_BLOCK, 1) ipm_kernel(const __grid_constant
     // so that the off-diagonal / diagonal branch is uniform across most warps
     // (stored column-major for the LU: coeff[a2 * s + a] is row a, column a2;
     // consecutive threads take consecutive rows of one column)
-    const int nloc = (C > 1) ? (s - (int)crank + (int)C - 1) / (int)C : s;
-    for (int e = tid; e < s * nloc; e += IPM_BLOCK) {
-      const int ca = e / s, a = e - ca * s;
-      const int a2 = (C > 1) ? ca * (int)C + (int)crank : sh.cord[ca];
+    for (int e = tid; e < s * s; e += IPM_BLOCK) {
+      const int ca = e / s, a = e - ca * s, a2 = sh.cord[ca];
       double v = symkron_sum(sh.T, sh.Si, k, sh.bi[a], sh.ci[a], sh.bi[a2], sh.ci[a2]);
       if (A.mode == 0) {
         v = Q11[a * s + a2] + v;
@@ -786,7 +560,7 @@ __global__ void __launch_bounds__(IPM_BLOCK, 1) ipm_kernel(const __grid_constant
       } else {
         v += lbc * (sh.sI[a] * sh.sI[a2]);
       }
-      coeff[((C > 1) ? ca : a2) * s + a] = v;
+      coeff[a2 * s + a] = v;
     }
     if (tid == 0) {
       if (A.mode == 0) {
@@ -813,10 +587,7 @@ __global__ void __launch_bounds__(IPM_BLOCK, 1) ipm_kernel(const __grid_constant
     }
     __syncthreads();
     if (tid == 0) { const long long c = clock64(); ph0 += c - tclk; tclk = c; }
-    if (C > 1)
-      ipm_lu_solve_cl(coeff, s, sh.ord, s, sh.dinv, sh.lcol, lnx, pnx, Uf, &s_ok, C, crank);
-    else
-      ipm_lu_solve(coeff, s, sh.ord, s, sh.dinv, sh.lcol, &s_piv, &s_ok);
+    ipm_lu_solve(coeff, s, sh.ord, s, sh.dinv, sh.lcol, &s_piv, &s_ok);
     if (tid == 0) { const long long c = clock64(); ph1 += c - tclk; tclk = c; }
     if (tid == 0 && !s_ok) atomicOr(A.status, ST_SMALL_DENSE_FAIL);
     // sh.ord now holds dsS
@@ -871,31 +642,6 @@ __global__ void __launch_bounds__(IPM_BLOCK, 1) ipm_kernel(const __grid_constant
     // ---- line search over the grid 0.9^j (solver/usbs.py:134-154): the largest
     // grid step keeping S (lanes 0-15) and T (lanes 16-31) positive definite is the
     // first positive-definite grid index ----
-    // with C > 1, one round over the first 16 C grid points split across the
-    // cluster (CTA r tests points 16 r .. 16 r + 15); if that leaves S's or T's
-    // first PD point undecided, every CTA runs the single-CTA search below
-    int clS = -1, clT = -1;
-    bool cl_done = false;
-    if (C > 1 && A.cl_line_search) {
-      if (wid == 0) {
-        const int half = lane >> 4, sub = lane & 15;
-        const double* M = half ? sh.T : sh.S;
-        const double* dM = half ? sh.dT : sh.dS;
-        const int jg = 16 * (int)crank + sub;
-        const bool pd = jg < ngrid &&
-                        pd_test(M, dM, (jg < 256) ? grid[jg] : pow(0.9, (double)jg), k);
-        const unsigned bal = __ballot_sync(0xffffffffu, pd);
-        if (lane == 0)
-          for (unsigned rr = 0; rr < C; ++rr) ipm_cl_st(ipm_cl_map(&lsmask[crank], rr), bal);
-      }
-      ipm_cl_sync();
-      for (unsigned rr = 0; rr < C; ++rr) {
-        const unsigned m = lsmask[rr];
-        if (clS < 0 && (m & 0xffffu)) clS = 16 * (int)rr + __ffs(m & 0xffffu) - 1;
-        if (clT < 0 && (m >> 16)) clT = 16 * (int)rr + __ffs(m >> 16) - 1;
-      }
-      cl_done = (clS >= 0 || ngrid <= 16 * (int)C) && (clT >= 0 || ngrid <= 16 * (int)C);
-    }
     if (wid == 0) {
       const int half = lane >> 4, sub = lane & 15;
       const double* M = half ? sh.T : sh.S;
@@ -906,13 +652,13 @@ __global__ void __launch_bounds__(IPM_BLOCK, 1) ipm_kernel(const __grid_constant
       // the bracket: at most three rounds of 16 tests per matrix.
       auto gstep = [&](int j) { return (j < 256) ? grid[j] : pow(0.9, (double)j); };
       int first = -1;
-      if (!cl_done) {
+      {
         const bool pd = (sub < ngrid) && pd_test(M, dM, gstep(sub), k);
         const unsigned bal = __ballot_sync(0xffffffffu, pd);
         const unsigned mine = half ? (bal >> 16) : (bal & 0xffffu);
         if (mine) first = __ffs(mine) - 1;
       }
-      const bool need2 = !cl_done && (first < 0) && (ngrid > 16);
+      const bool need2 = (first < 0) && (ngrid > 16);
       if (__any_sync(0xffffffffu, need2)) {
         const int jc = min(31 + 16 * sub, ngrid - 1);
         const bool pd = need2 && (16 + 16 * sub < ngrid) && pd_test(M, dM, gstep(jc), k);
@@ -927,8 +673,8 @@ __global__ void __launch_bounds__(IPM_BLOCK, 1) ipm_kernel(const __grid_constant
         const unsigned mine3 = half ? (bal3 >> 16) : (bal3 & 0xffffu);
         if (need3 && mine3) first = 16 + 16 * q + __ffs(mine3) - 1;
       }
-      const int firstS = cl_done ? clS : __shfl_sync(0xffffffffu, first, 0);
-      const int firstT = cl_done ? clT : __shfl_sync(0xffffffffu, first, 16);
+      const int firstS = __shfl_sync(0xffffffffu, first, 0);
+      const int firstT = __shfl_sync(0xffffffffu, first, 16);
       if (lane == 0) {
         const double cS = (firstS < 0) ? 0.0 : (firstS < 256 ? grid[firstS] : pow(0.9, (double)firstS));
         const double cT = (firstT < 0) ? 0.0 : (firstT < 256 ? grid[firstT] : pow(0.9, (double)firstT));
@@ -962,7 +708,7 @@ __global__ void __launch_bounds__(IPM_BLOCK, 1) ipm_kernel(const __grid_constant
         double mun = (d + sc.eta * sc.zeta + sc.omega * (1 - trS - sc.eta)) / (2 * k + 4.0);
         mun *= (st > 0.2) ? (0.5 - 0.4 * st * st) : 1.0;
         if (!(isnan(mun) || mun <= mu)) mun = mu;
-        if (lead && A.dbg && sc.it < 128) {
+        if (A.dbg && sc.it < 128) {
           double* d = A.dbg + sc.it * 8;
           d[0] = mun; d[1] = st; d[2] = sc.eta; d[3] = sc.zeta; d[4] = sc.omega;
           d[5] = sc.d_eta; d[6] = sc.d_omega; d[7] = trS;
@@ -976,14 +722,11 @@ __global__ void __launch_bounds__(IPM_BLOCK, 1) ipm_kernel(const __grid_constant
     __syncthreads();
     if (tid == 0) { const long long c = clock64(); ph3 += c - tclk; }
   }
-  // no CTA of a cluster leaves while another may still address its memory
-  if (C > 1) ipm_cl_sync();
-  if (lead && tid == 0 && A.prof) {
+  if (tid == 0 && A.prof) {
     A.prof[0] += (double)ph0; A.prof[1] += (double)ph1; A.prof[2] += (double)ph2;
     A.prof[3] += (double)ph3;
   }
   // ---- outputs ----
-  if (!lead) return;
   if (A.mode == 0) {
     for (int e = tid; e < k * k; e += IPM_BLOCK) sm[A.o_Sout + e] = tr * sh.S[e];
     if (tid == 0) {
@@ -1164,53 +907,17 @@ __global__ void cholqr_kernel(CholQRArgs A) {
   for (int e = lane; e < k * k; e += 32) sm[A.o_Rinv + e] = Ri[e];
 }
 
-// CTAs of an IPM solve (a thread-block cluster; 1 = the single-CTA kernel):
-// USBS_IPM_CTAS (1..8) overrides the default of 4
-static int ipm_ctas() {
-  static const int c = [] {
-    const char* e = getenv("USBS_IPM_CTAS");
-    const int v = e ? atoi(e) : 4;
-    return (v >= 1 && v <= 8) ? v : 4;
-  }();
-  return c;
-}
-
-int launch_ipm(const IpmArgs& a_in, cudaStream_t st) {
-  IpmArgs a = a_in;
-  static const int cl_ls = [] {
-    const char* e = getenv("USBS_IPM_CL_LS");
-    return e ? atoi(e) : 1;
-  }();
-  a.cl_line_search = cl_ls;
+int launch_ipm(const IpmArgs& a, cudaStream_t st) {
   const int s = a.k * (a.k + 1) / 2;
-  const int C = ipm_ctas();
-  const size_t dyn = (size_t)(C > 1 ? 3 : 2) * s * s * sizeof(double);
+  const size_t dyn = (size_t)2 * s * s * sizeof(double);
   static bool attr = false;
   if (!attr) {
     cudaFuncSetAttribute(ipm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         3 * IPM_MAXS * IPM_MAXS * (int)sizeof(double));
-    cudaFuncSetAttribute(ipm_kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+                         2 * IPM_MAXS * IPM_MAXS * (int)sizeof(double));
     attr = true;
   }
-  cudaError_t e;
-  if (C == 1) {
-    ipm_kernel<<<1, IPM_BLOCK, dyn, st>>>(a);
-    e = cudaGetLastError();
-  } else {
-    cudaLaunchConfig_t cfg = {};
-    cfg.gridDim = dim3((unsigned)C);
-    cfg.blockDim = dim3(IPM_BLOCK);
-    cfg.dynamicSmemBytes = dyn;
-    cfg.stream = st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = (unsigned)C;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    e = cudaLaunchKernelEx(&cfg, ipm_kernel, a);
-  }
+  ipm_kernel<<<1, IPM_BLOCK, dyn, st>>>(a);
+  cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) { set_error("ipm launch: %s", cudaGetErrorString(e)); return -5; }
   return 0;
 }

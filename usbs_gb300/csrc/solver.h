@@ -63,7 +63,6 @@ struct IpmArgs {
   const int* skip;     // non-zero: instance inactive, kernel returns
   double* dbg;         // optional: per-iteration history, 8 doubles per IPM iteration
   double* prof;        // optional: clock64 cycles per phase (4 doubles, accumulated)
-  int cl_line_search;  // set by launch_ipm: a cluster tests its first 16 C grid points at once
 };
 
 struct EigSArgs {
