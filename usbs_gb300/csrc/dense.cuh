@@ -153,20 +153,56 @@ __device__ inline bool warp_syev(double* A, int lda, int n, double* w, double* Z
   return true;
 }
 
-// Cyclic parallel Jacobi eigensolver (float) for a symmetric n x n matrix, run
-// by a whole CTA (blockDim a multiple of 32, >= 64) at order M (32 or 16;
-// indices >= n are padding that couples to nothing): M/2 disjoint rotations per round in
-// round-robin ("chess tournament") order, Rutishauser's rotation formulas,
-// sweeps until the off-diagonal Frobenius norm is below 4 eps ||A||_F.  Each
-// round: threads 0-15 form the rotations, then the 512 row updates and the
-// column updates (A and Z) are spread over the CTA.  A (row-major, lda >= M,
-// room for 2 lda + n M floats) is destroyed; w receives the eigenvalues
-// ascending, Z (row-major, ldz >= M) the eigenvectors as columns.  Returns
-// false (uniformly) if 20 sweeps do not converge.  pidx needs M ints, rc/rs
-// M/2 floats, red 32 floats.
+// Rotation (c, s) that zeroes the (p, q) entry of the symmetric 2 x 2 block
+// [[app, apq], [apq, aqq]] (Rutishauser's formulas).
+__device__ __forceinline__ void jacobi_rot(float app, float aqq, float apq, float& c, float& sn) {
+  c = 1.0f;
+  sn = 0.0f;
+  if (apq != 0.0f) {
+    const float theta = (aqq - app) / (2.0f * apq);
+    const float t = copysignf(1.0f, theta) / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
+    c = rsqrtf(t * t + 1.0f);
+    sn = t * c;
+  }
+}
+
+// Pair i (0 <= i < M/2) of round r (0 <= r < M-1) of the round-robin
+// ("chess tournament") order, p < q: index 0 stays, 1..M-1 rotate.
 template <int M>
-__device__ inline bool cta_jacobi_f32(float* A, int lda, int n, float* w, float* Z, int ldz,
-                                      int* pidx, float* rc, float* rs, float* red) {
+__device__ __forceinline__ void jacobi_pair(int r, int i, int& p, int& q) {
+  if (i == 0) {
+    p = 0;
+    q = 1 + r;
+  } else {
+    p = r + i;
+    p = (p >= M - 1) ? p - (M - 1) : p;
+    p += 1;
+    q = r - i + M - 1;
+    q = (q >= M - 1) ? q - (M - 1) : q;
+    q += 1;
+  }
+  if (p > q) { const int t = p; p = q; q = t; }
+}
+
+// Cyclic parallel Jacobi eigensolver (float) for a symmetric n x n matrix, run
+// by a whole CTA (blockDim a multiple of 32) at order M (32 or 16; indices >= n
+// are padding that couples to nothing): M/2 disjoint rotations per round in
+// round-robin order, sweeps until the off-diagonal Frobenius norm is below
+// 4 eps ||A||_F.
+// One CTA barrier per round: A is double-buffered (a round reads one buffer
+// and writes the other), and every warp forms the round's M/2 rotations itself
+// (lane l: pair l mod M/2) and hands them to its threads by shuffle.  Thread
+// (I, J) maps the 2 x 2 block of pairs (I, J) through the row rotation of I
+// and the column rotation of J (the pairs are disjoint, so the block depends
+// only on itself), and rotates rows J and J + M/2 of Z by pair I.
+// A and A2 (row-major, lda >= M, each with room for 2 lda + n M floats) are
+// destroyed; w receives the eigenvalues ascending, Z (row-major, ldz >= M) the
+// eigenvectors as columns.  Returns false (uniformly) if 20 sweeps do not
+// converge.  red needs 2 floats.
+template <int M>
+__device__ inline bool cta_jacobi_f32(float* A, float* A2, int lda, int n, float* w, float* Z,
+                                      int ldz, float* red) {
+  static_assert(M == 16 || M == 32, "order 16 or 32");
   const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, wid = tid >> 5;
   constexpr int H = M / 2;
   for (int e = tid; e < M * M; e += nt) {
@@ -183,12 +219,14 @@ __device__ inline bool cta_jacobi_f32(float* A, int lda, int n, float* w, float*
   }
   __syncthreads();
   const float tol2 = red[0];
+  float* cur = A;
+  float* nxt = A2;
   bool ok = false;
   for (int sweep = 0; sweep < 20; ++sweep) {
     if (wid == 0) {
       float off = 0.0f;
       for (int i = 0; i < M; ++i) {
-        const float a = (lane < M && lane != i) ? A[i * lda + lane] : 0.0f;
+        const float a = (lane < M && lane != i) ? cur[i * lda + lane] : 0.0f;
         off += a * a;
       }
       off = warp_sum(off);
@@ -197,64 +235,49 @@ __device__ inline bool cta_jacobi_f32(float* A, int lda, int n, float* w, float*
     __syncthreads();
     if (red[1] <= tol2) { ok = true; break; }
     for (int r = 0; r < M - 1; ++r) {
-      if (tid < H) {
-        int p, q;
-        if (tid == 0) { p = 0; q = 1 + r; }
-        else {
-          p = r + tid; p = (p >= M - 1) ? p - (M - 1) : p; p += 1;
-          q = r - tid + M - 1; q = (q >= M - 1) ? q - (M - 1) : q; q += 1;
+      int pl, ql;
+      jacobi_pair<M>(r, lane % H, pl, ql);
+      float cl, sl;
+      jacobi_rot(cur[pl * lda + pl], cur[ql * lda + ql], cur[pl * lda + ql], cl, sl);
+      for (int base = 0; base < H * H; base += nt) {      // trip count uniform over the CTA
+        const int e = base + tid;
+        const int I = (e / H) % H, J = e % H;
+        const float c = __shfl_sync(0xffffffffu, cl, I), sn = __shfl_sync(0xffffffffu, sl, I);
+        const float c2 = __shfl_sync(0xffffffffu, cl, J), s2 = __shfl_sync(0xffffffffu, sl, J);
+        if (e < H * H) {
+          int p, q, p2, q2;
+          jacobi_pair<M>(r, I, p, q);
+          jacobi_pair<M>(r, J, p2, q2);
+          const float app = cur[p * lda + p2], apq = cur[p * lda + q2];
+          const float aqp = cur[q * lda + p2], aqq = cur[q * lda + q2];
+          // rows
+          const float bpp = c * app - sn * aqp, bpq = c * apq - sn * aqq;
+          const float bqp = sn * app + c * aqp, bqq = sn * apq + c * aqq;
+          // columns
+          nxt[p * lda + p2] = c2 * bpp - s2 * bpq;
+          nxt[p * lda + q2] = s2 * bpp + c2 * bpq;
+          nxt[q * lda + p2] = c2 * bqp - s2 * bqq;
+          nxt[q * lda + q2] = s2 * bqp + c2 * bqq;
+#pragma unroll
+          for (int j = J; j < M; j += H) {
+            const float zp = Z[j * ldz + p], zq = Z[j * ldz + q];
+            Z[j * ldz + p] = c * zp - sn * zq;
+            Z[j * ldz + q] = sn * zp + c * zq;
+          }
         }
-        if (p > q) { const int t = p; p = q; q = t; }
-        const float apq = A[p * lda + q];
-        float c = 1.0f, sn = 0.0f;
-        if (apq != 0.0f) {
-          const float theta = (A[q * lda + q] - A[p * lda + p]) / (2.0f * apq);
-          const float t = copysignf(1.0f, theta) / (fabsf(theta) + sqrtf(theta * theta + 1.0f));
-          c = rsqrtf(t * t + 1.0f);
-          sn = t * c;
-        }
-        pidx[2 * tid] = p;
-        pidx[2 * tid + 1] = q;
-        rc[tid] = c;
-        rs[tid] = sn;
       }
       __syncthreads();
-      // J^T A J in one pass: the 16 pairs are disjoint, so the 2 x 2 block of
-      // pairs (I, J) depends only on itself; thread (I, J) applies the row
-      // rotation of I, then the column rotation of J (the operations of a
-      // row pass followed by a column pass), and Z J by (row, pair)
-      for (int e = tid; e < H * H; e += nt) {
-        const int I = e / H, J = e % H;
-        const int p = pidx[2 * I], q = pidx[2 * I + 1], p2 = pidx[2 * J], q2 = pidx[2 * J + 1];
-        const float c = rc[I], sn = rs[I], c2 = rc[J], s2 = rs[J];
-        const float app = A[p * lda + p2], apq = A[p * lda + q2];
-        const float aqp = A[q * lda + p2], aqq = A[q * lda + q2];
-        // rows
-        const float bpp = c * app - sn * aqp, bpq = c * apq - sn * aqq;
-        const float bqp = sn * app + c * aqp, bqq = sn * apq + c * aqq;
-        // columns
-        A[p * lda + p2] = c2 * bpp - s2 * bpq;
-        A[p * lda + q2] = s2 * bpp + c2 * bpq;
-        A[q * lda + p2] = c2 * bqp - s2 * bqq;
-        A[q * lda + q2] = s2 * bqp + c2 * bqq;
-      }
-      for (int e = tid; e < H * M; e += nt) {
-        const int pr = e / M, j = e % M;
-        const int p = pidx[2 * pr], q = pidx[2 * pr + 1];
-        const float c = rc[pr], sn = rs[pr];
-        const float bp = Z[j * ldz + p], bq = Z[j * ldz + q];
-        Z[j * ldz + p] = c * bp - sn * bq;
-        Z[j * ldz + q] = sn * bp + c * bq;
-      }
-      __syncthreads();
+      float* t = cur;
+      cur = nxt;
+      nxt = t;
     }
   }
   // eigenvalues from the diagonal, sorted ascending with their vectors: each
-  // value's rank (ties by index) is its position; A's diagonal is no longer
-  // needed, so A's first row holds the values and A's second the ranks
-  float* wv = A;
-  int* rk = (int*)(A + lda);
-  if (tid < M) wv[tid] = (tid < n) ? A[tid * lda + tid] : 0.0f;
+  // value's rank (ties by index) is its position; the spare buffer's first
+  // row holds the values, its second the ranks, the rest the old Z
+  float* wv = nxt;
+  int* rk = (int*)(nxt + lda);
+  if (tid < M) wv[tid] = (tid < n) ? cur[tid * lda + tid] : 0.0f;
   __syncthreads();
   if (tid < n) {
     const float v = wv[tid];
@@ -267,8 +290,8 @@ __device__ inline bool cta_jacobi_f32(float* A, int lda, int n, float* w, float*
     w[r] = v;
   }
   __syncthreads();
-  // permute Z's columns: Z[:, rank[c]] = Z_old[:, c], through A's rows 2.. as scratch
-  float* zs = A + 2 * lda;   // n x n, stride M
+  // permute Z's columns: Z[:, rank[c]] = Z_old[:, c]
+  float* zs = nxt + 2 * lda;   // n x n, stride M
   for (int e = tid; e < n * n; e += nt) {
     const int i = e / n, c = e - (e / n) * n;
     zs[i * M + c] = Z[i * ldz + c];

@@ -750,8 +750,9 @@ __global__ void __launch_bounds__(IPM_BLOCK) eigS_kernel(EigSArgs A) {
   constexpr int L = 16;                               // ld of the FP64 k x k blocks
   __shared__ double Sd[L * L], Z[L * L], R[L * L], S2[L * L], Wb[L * L], lam[L];
   __shared__ double GW[IPM_MAXK * IPM_MAXK], red[IPM_BLOCK / 32];
-  __shared__ float Af[2 * (L + 1) + L * L + L], Zf[L * (L + 1)], wf[L], rcf[L], rsf[L], redf[32];
-  __shared__ int pidx[L], order[L];
+  __shared__ float Af[2 * (L + 1) + L * L + L], Af2[2 * (L + 1) + L * L + L], Zf[L * (L + 1)];
+  __shared__ float wf[L], redf[32];
+  __shared__ int order[L];
   const int k = A.k, kc = A.k_curr, tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
   double* sm = A.smalls;
   const double* S = sm + A.o_Sout;
@@ -763,7 +764,7 @@ __global__ void __launch_bounds__(IPM_BLOCK) eigS_kernel(EigSArgs A) {
     Af[r * (L + 1) + c] = (float)S[e];
   }
   __syncthreads();
-  bool ok = cta_jacobi_f32<L>(Af, L + 1, k, wf, Zf, L + 1, pidx, rcf, rsf, redf);
+  bool ok = cta_jacobi_f32<L>(Af, Af2, L + 1, k, wf, Zf, L + 1, redf);
   for (int e = tid; e < k * k; e += IPM_BLOCK) {
     const int r = e / k, c = e - r * k;
     Z[r * L + c] = (double)Zf[r * (L + 1) + c];

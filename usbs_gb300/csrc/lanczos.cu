@@ -85,6 +85,7 @@ struct LzShared {
       double ys[LZ_BLOCK];
       double wred[LZ_NW][MP1];
     } st;
+    VT cys[LZ_BLOCK];            // cluster kernel: row results of the SpMV, in the vector type
     struct {                     // restart on CTA 0 (T, X, R, S, W row-major, ld MP1)
       double T[MAXM * MP1];
       double X[MAXM * MP1];
@@ -96,12 +97,13 @@ struct LzShared {
   } u;
   double h[MP1];
   VT hv[MP1];                    // h in the vector type, converted once per reduction
+  double bnorm;                  // cluster kernel: sqrt(h[0]) of a norm reduction ...
+  VT binv;                       // ... and 1 / bnorm in the vector type
   double alpha[MAXM];
   double beta[MAXM];
   double ritz[MAXM];
   double red[LZ_NW];
-  float wf[MAXM], rc[MAXM / 2], rsn[MAXM / 2], redf[32];
-  int pidx[MAXM];
+  float wf[MAXM], redf[32];
   int order[MAXM];
   int k_next, nconv;
   long long eig_cycles;          // cycles in the projected eigensolver (thread 0)
@@ -378,7 +380,7 @@ __device__ void restart_select(const D& P, LzShared<VT>& sh, int k, bool write_o
   // eigh(T) (solver/lanczos.py:203): FP32 parallel Jacobi by the CTA ...
   {
     const long long c0 = clock64();
-    const bool ok = cta_jacobi_f32<32>(Tf, MP1, m, sh.wf, Zf, MP1, sh.pidx, sh.rc, sh.rsn, sh.redf);
+    const bool ok = cta_jacobi_f32<32>(Tf, (float*)sh.u.rs.W, MP1, m, sh.wf, Zf, MP1, sh.redf);
     if (tid == 0) sh.eig_cycles += clock64() - c0;
     if (!ok && tid == 0) atomicOr(P.status, ST_SMALL_DENSE_FAIL);
   }
@@ -1395,8 +1397,12 @@ __host__ __device__ inline ClLayout cl_layout(int m, int rc, int csr_cap) {
 
 // h[c] = sum over the cluster's CTAs r = 0..C-1 of part_r[c], c < nv, summed
 // as a fixed pairwise tree (FP64 adds are ~64 cycles dependent on this part).
+// With norm set (nv = 1), lane 0 also forms sh.bnorm = sqrt(h[0]) and
+// sh.binv = 1 / bnorm once for the CTA (FP64 square roots and divisions are
+// long dependent DFMA chains on this part's narrow FP64 pipe).
 template <typename VT>
-__device__ __forceinline__ void cl_reduce(const double* part, int C, int nv, LzShared<VT>& sh) {
+__device__ __forceinline__ void cl_reduce(const double* part, int C, int nv, LzShared<VT>& sh,
+                                          bool norm = false) {
   const int lane = threadIdx.x & 31;
   if (threadIdx.x < 32) {
     for (int c = lane; c < nv; c += 32) {
@@ -1409,6 +1415,11 @@ __device__ __forceinline__ void cl_reduce(const double* part, int C, int nv, LzS
         for (int r = 0; r < h; ++r) v[r] = v[r] + v[r + h];
       sh.h[c] = v[0];
       sh.hv[c] = (VT)v[0];
+      if (norm) {
+        const double b = sqrt(v[0]);
+        sh.bnorm = b;
+        sh.binv = (VT)(1.0 / b);
+      }
     }
   }
   __syncthreads();
@@ -1458,17 +1469,37 @@ __device__ void cl_phase_spmv(const ClCtx<VT>& X, LzShared<VT>& sh, int i, const
           else { pb[q] = P.rowptr[X.r0 + lr] + lig; pe[q] = P.rowptr[X.r0 + lr + 1]; }
         }
       }
+      // the first entry of each of the CH rows: all gathers in flight at once
+      VT av[CH], xv[CH];
+#pragma unroll
+      for (int q = 0; q < CH; ++q) {
+        av[q] = (VT)0;
+        xv[q] = (VT)0;
+        if (pb[q] < pe[q]) {
+          if (X.staged) {
+            const int w = X.cg[pb[q]];
+            av[q] = X.vs[pb[q]];
+            xv[q] = cl_ld(cl_map(xbase + (w & 0xffffff), (unsigned)w >> 24), (VT)0);
+          } else {
+            const int gc = P.col[pb[q]];
+            const int o = gc / rc;
+            av[q] = P.val[pb[q]];
+            xv[q] = cl_ld(cl_map(xbase + (gc - o * rc), (unsigned)o), (VT)0);
+          }
+        }
+      }
       AT sacc[CH];
 #pragma unroll
       for (int q = 0; q < CH; ++q) {
         sacc[q] = (AT)0;
+        if (pb[q] < pe[q]) sacc[q] += (AT)av[q] * (AT)xv[q];
         if (X.staged) {
-          for (int p = pb[q]; p < pe[q]; p += L) {
+          for (int p = pb[q] + L; p < pe[q]; p += L) {
             const int w = X.cg[p];
             sacc[q] += (AT)X.vs[p] * (AT)cl_ld(cl_map(xbase + (w & 0xffffff), (unsigned)w >> 24), (VT)0);
           }
         } else {
-          for (int p = pb[q]; p < pe[q]; p += L) {
+          for (int p = pb[q] + L; p < pe[q]; p += L) {
             const int gc = P.col[p];
             const int o = gc / rc;
             sacc[q] += (AT)P.val[p] * (AT)cl_ld(cl_map(xbase + (gc - o * rc), (unsigned)o), (VT)0);
@@ -1479,13 +1510,13 @@ __device__ void cl_phase_spmv(const ClCtx<VT>& X, LzShared<VT>& sh, int i, const
       for (int q = 0; q < CH; ++q) {
 #pragma unroll
         for (int o = L >> 1; o > 0; o >>= 1) sacc[q] += __shfl_xor_sync(0xffffffffu, sacc[q], o);
-        if (lig == 0) sh.u.st.ys[(q0 + q) * GPP + g] = (double)sacc[q];
+        if (lig == 0) sh.u.cys[(q0 + q) * GPP + g] = (VT)sacc[q];
       }
     }
     __syncthreads();
     const int lr = base + tid;
     if (lr < X.rows) {
-      const VT y = (VT)sh.u.st.ys[tid] * xscale;
+      const VT y = sh.u.cys[tid] * xscale;
       vout[lr] = y;
       VT xn = (VT)0;
       if (wq) {
@@ -1644,8 +1675,8 @@ lanczos_cluster_kernel(const __grid_constant__ ClusterBatch<VT> batch) {
         invb = (VT)1;
         wq = false;
       } else {
-        cl_reduce(part2, C, 1, sh);
-        const double b = sqrt(sh.h[0]);
+        cl_reduce(part2, C, 1, sh, true);
+        const double b = sh.bnorm;
         if (tid == 0) sh.beta[i - 1] = b;
         if (b < 1e-15) {
           // Krylov space exhausted: random vector orthogonalised twice
@@ -1660,10 +1691,10 @@ lanczos_cluster_kernel(const __grid_constant__ ClusterBatch<VT> batch) {
           cl_reduce(part1, C, i, sh);
           cl_phase_update_norm(X, sh, i, buf, part2);
           cl_sync();
-          cl_reduce(part2, C, 1, sh);
-          invb = (VT)(1.0 / sqrt(sh.h[0]));
+          cl_reduce(part2, C, 1, sh, true);
+          invb = sh.binv;
         } else {
-          invb = (VT)(1.0 / b);
+          invb = sh.binv;
         }
         xbase = X.vb + (size_t)prev * rc;
         wq = true;
@@ -1696,8 +1727,8 @@ lanczos_cluster_kernel(const __grid_constant__ ClusterBatch<VT> batch) {
     // ---- restart ----
     const bool stepped = (k < m);
     if (stepped) {
-      cl_reduce(part2, C, 1, sh);
-      const double b = sqrt(sh.h[0]);
+      cl_reduce(part2, C, 1, sh, true);
+      const double b = sh.bnorm;
       if (tid == 0) sh.beta[m - 1] = b;
       if (b < 1e-15) {
         ++breakdowns;
@@ -1710,10 +1741,10 @@ lanczos_cluster_kernel(const __grid_constant__ ClusterBatch<VT> batch) {
         cl_reduce(part1, C, m, sh);
         cl_phase_update_norm(X, sh, m, buf, part2);
         cl_sync();
-        cl_reduce(part2, C, 1, sh);
-        invb = (VT)(1.0 / sqrt(sh.h[0]));
+        cl_reduce(part2, C, 1, sh, true);
+        invb = sh.binv;
       } else {
-        invb = (VT)(1.0 / b);
+        invb = sh.binv;
       }
     }
     __syncthreads();
