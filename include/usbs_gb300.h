@@ -158,7 +158,9 @@ int usbs_eigsh_smallest(int n, long long nnz, const int* rowptr, const int* col,
  *    USBS_EIGSH_STATIC_SCRATCH_BYTES are rejected (-2, usbs_last_error()).
  *    The scratch holds the assembled operator (nnz values), three n-vectors
  *    and at most 0.5 MB of partial sums, so with 32 inner iterations problems
- *    up to about nnz + 3n = 2.0e6 (FP64) or 4.0e6 (FP32) fit.
+ *    up to about nnz + 3n = 2.0e6 (FP64) or 4.0e6 (FP32) fit.  Stream-path
+ *    problems (n > 20,480 in FP64, 40,960 in FP32) also hold the operator's
+ *    sliced-ELL copy, about 1.5 * average degree * n more entries.
  *  - The scratch need not start at zero: each call clears its barrier
  *    counters, info words and Lanczos coefficients on `stream` before use.
  *  - One scratch per device: calls whose work may overlap in time on the

@@ -209,34 +209,37 @@ __device__ void cta_matvec3(const double* M, const double* x, int s, double* par
 // LU with partial pivoting and solve, whole CTA (G&VL Alg. 3.4.1, right-looking
 // with a one-column look-ahead).  A is stored column-major (A[c * lda + i] is
 // row i, column c), so every column access of the pivot chain is contiguous.
-// On GB300 a dependent FP64 operation costs ~64 cycles and a division ~440,
-// so the pivot chain of each column is kept off the critical path: while warps
-// 1..7 eliminate b and apply the rank-1 update of column j to columns j+2..,
-// warp 0 updates column j+1 (lane q holds rows j+1+q, j+33+q, j+65+q in
-// registers), picks the next pivot from those registers (largest |a|, ties to
-// the smaller row index as in LAPACK; warp reduction instructions on the
-// integer keys of |a|), forms its reciprocal and the next multipliers.  Rows
-// are swapped physically at the start of each column.  L is not stored: b is
-// eliminated alongside.  Every element sees the arithmetic of the textbook
-// algorithm (a_ic - l_i a_jc, l_i = a_ij * (1/a_jj)).
+// On GB300 an FP64 warp instruction holds its SM sub-partition's FP64 pipe for
+// 64 cycles, so the pivot chain of each column is kept off the critical path:
+// while warps 1..7 eliminate b and apply the rank-1 update of column j to
+// columns j+2.., warp 0 updates column j+1 (lane q holds rows j+1+q, j+33+q,
+// j+65+q in registers, and only the blocks that still hold rows take part),
+// picks the next pivot from those registers (largest |a|, ties to the smaller
+// row index as in LAPACK; warp reduction instructions on the integer keys of
+// |a|), forms its reciprocal and the next multipliers.  Rows are swapped
+// physically at the start of each column.  L is not stored: b is eliminated
+// alongside.  Every element sees the arithmetic of the textbook algorithm
+// (a_ic - l_i a_jc, l_i = a_ij * (1/a_jj)).  Partial pivoting is needed: in
+// the bundle subproblems' Newton systems about two thirds of the
+// factorisations exchange rows somewhere.
 constexpr int LU_RPL = (IPM_MAXS + 31) / 32;   // rows per lane of warp 0
 __device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* dinv, double* lcol,
-                             int* piv_out, int* ok_out) {
+                             int* ok_out) {
   const int tid = threadIdx.x, lane = tid & 31;
   __shared__ double lnext[IPM_MAXS];
   __shared__ int pnext[2];   // pivot of column j in pnext[j & 1] (written one column ahead)
   double* lc = lcol;         // multipliers of the current column (indexed by row)
   double* ln = lnext;        // multipliers of the next column
-  // warp 0: rows r = j + lane + 32 q of column j are in v[q]; pivot, reciprocal
-  // and multipliers of column j
-  auto pick = [&](int j, const double (&v)[LU_RPL], double* lout) {
+  // warp 0: rows r = j + lane + 32 q of column j are in v[q] (q < nq); pivot,
+  // reciprocal and multipliers of column j
+  auto pick = [&](int j, const double (&v)[LU_RPL], double* lout, int nq) {
     // lane-local candidate: largest |a| key, smallest row among equal keys
     unsigned long long best = 0ull;
     int bi = 0x7fffffff;
 #pragma unroll
     for (int q = 0; q < LU_RPL; ++q) {
       const int i = j + lane + 32 * q;
-      if (i < n) {
+      if (q < nq && i < n) {
         const unsigned long long kk = abs_key(v[q]);
         if (bi == 0x7fffffff || kk > best) { best = kk; bi = i; }
       }
@@ -265,7 +268,7 @@ __device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* dinv,
 #pragma unroll
     for (int q = 0; q < LU_RPL; ++q) {
       const int i = j + lane + 32 * q;
-      if (i < n) lout[i] = v[q] * inv;
+      if (q < nq && i < n) lout[i] = v[q] * inv;
     }
     if (lane == 0) {
       pnext[j & 1] = bi;
@@ -282,12 +285,11 @@ __device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* dinv,
       const int i = lane + 32 * q;
       v[q] = (i < n) ? A[i] : 0.0;
     }
-    pick(0, v, lc);
+    pick(0, v, lc, LU_RPL);
   }
   __syncthreads();
   for (int j = 0; j < n; ++j) {
     const int piv = pnext[j & 1];
-    if (j == 0) *piv_out = piv;
     // swap rows j and piv (columns j.., b and the multipliers of column j)
     if (piv != j) {
       for (int c = j + tid; c < n; c += blockDim.x) {
@@ -307,21 +309,26 @@ __device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* dinv,
       // column j+1 for rows j+1.. (all loads first), then the look-ahead
       const double* colj1 = A + (size_t)(j + 1) * lda;
       const double ujn = colj1[j];
+      const int nq = (w + 31) >> 5;   // register blocks holding rows, warp-uniform
       double a[LU_RPL], l[LU_RPL];
 #pragma unroll
       for (int q = 0; q < LU_RPL; ++q) {
         const int i = j + 1 + lane + 32 * q;
-        a[q] = (i < n) ? colj1[i] : 0.0;
-        l[q] = (i < n) ? lc[i] : 0.0;
+        a[q] = (q < nq && i < n) ? colj1[i] : 0.0;
+        l[q] = (q < nq && i < n) ? lc[i] : 0.0;
       }
       double v[LU_RPL];
 #pragma unroll
       for (int q = 0; q < LU_RPL; ++q) {
-        const int i = j + 1 + lane + 32 * q;
-        v[q] = a[q] - l[q] * ujn;
-        if (i < n) A[(size_t)(j + 1) * lda + i] = v[q];
+        if (q < nq) {
+          const int i = j + 1 + lane + 32 * q;
+          v[q] = a[q] - l[q] * ujn;
+          if (i < n) A[(size_t)(j + 1) * lda + i] = v[q];
+        } else {
+          v[q] = 0.0;
+        }
       }
-      pick(j + 1, v, ln);
+      pick(j + 1, v, ln, nq);
     } else {
       const int nt = (int)blockDim.x - 32, t = tid - 32;
       // b for rows j+1.. (forward elimination of the right-hand side)
@@ -330,17 +337,17 @@ __device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* dinv,
         b[i] = b[i] - lc[i] * b[j];
       }
       if (w > 1) {
-      // columns j+2.. of rows j+1..: flat over warps 1..7, lanes along rows
-      const int cpp = nt / w;                 // columns per pass
-      const int cc = t / w, r = t - (t / w) * w;
-      if (cc < cpp) {
-        const int i = j + 1 + r;
-        const double li = lc[i];
-        for (int c = j + 2 + cc; c < n; c += cpp) {
-          double* col = A + (size_t)c * lda;
-          col[i] = col[i] - li * col[j];
+        // columns j+2.. of rows j+1..: flat over warps 1..7, lanes along rows
+        const int cpp = nt / w;                 // columns per pass
+        const int cc = t / w, r = t - (t / w) * w;
+        if (cc < cpp) {
+          const int i = j + 1 + r;
+          const double li = lc[i];
+          for (int c = j + 2 + cc; c < n; c += cpp) {
+            double* col = A + (size_t)c * lda;
+            col[i] = col[i] - li * col[j];
+          }
         }
-      }
       }
     }
     __syncthreads();
@@ -363,9 +370,11 @@ __device__ void ipm_lu_solve(double* A, int lda, double* b, int n, double* dinv,
       const double* colj = A + (size_t)j * lda;
 #pragma unroll
       for (int q = 0; q < LU_RPL; ++q) {
-        const int i = lane + 32 * q;
-        if (i == j) br[q] = bj;
-        else if (i < j) br[q] -= colj[i] * bj;
+        if (q <= oq) {   // blocks holding rows at or above j, warp-uniform
+          const int i = lane + 32 * q;
+          if (i == j) br[q] = bj;
+          else if (i < j) br[q] -= colj[i] * bj;
+        }
       }
     }
 #pragma unroll
@@ -587,7 +596,7 @@ __global__ void __launch_bounds__(IPM_BLOCK, 1) ipm_kernel(const __grid_constant
     }
     __syncthreads();
     if (tid == 0) { const long long c = clock64(); ph0 += c - tclk; tclk = c; }
-    ipm_lu_solve(coeff, s, sh.ord, s, sh.dinv, sh.lcol, &s_piv, &s_ok);
+    ipm_lu_solve(coeff, s, sh.ord, s, sh.dinv, sh.lcol, &s_ok);
     if (tid == 0) { const long long c = clock64(); ph1 += c - tclk; tclk = c; }
     if (tid == 0 && !s_ok) atomicOr(A.status, ST_SMALL_DENSE_FAIL);
     // sh.ord now holds dsS
