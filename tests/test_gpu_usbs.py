@@ -292,6 +292,39 @@ def test_usbs_graph_replay_equals_eager(cuda, monkeypatch, precision, cond_base)
     assert binfo["lanczos_launches"] >= 1 and binfo["lanczos_ms"] > 0
 
 
+@pytest.mark.parametrize("precision,renumber", [(64, False), (32, False), (64, True)])
+def test_usbs_single_pass_rows_equals_two_passes(cuda, monkeypatch, precision, renumber):
+    """MaxCut's constraints are single diagonal entries, so the solver evaluates
+    A(F F^T) in the pass over V's rows that updates the sketch and the kept
+    directions, one kernel instead of two.  Each value is computed as the
+    separate constraint kernel computes it: traces and final iterates are
+    bit-identical to the two-pass solve (USBS_FUSED_ROWS=0), with one launch
+    fewer per outer iteration; the row-to-constraint map also holds after an
+    RCM renumbering."""
+    from usbs_gb300 import solver
+    W = wl.torus_graph(30, 1)
+    st = omaxcut.initialize_state(W, 10)
+    n = st.C.shape[0]
+    q0 = orng.default_q0(n)
+    args = (st, n, n, 2.0 * n, 2.0, S["rho"], S["beta"], 10, 1, 6, np.inf, -1.0, -1.0, -1.0, 32,
+            10, 1e-7, S["subprob_max_iters"])
+    kw = dict(q0=q0, precision=precision, return_trace=True, return_info=True,
+              renumber=renumber)
+    monkeypatch.setenv("USBS_FUSED_ROWS", "0")
+    a, atr, ainfo = solver.usbs(*args, **kw)
+    monkeypatch.setenv("USBS_FUSED_ROWS", "1")
+    b, btr, binfo = solver.usbs(*args, **kw)
+    assert ainfo["status"] == binfo["status"] == 0
+    assert len(atr) == len(btr) == 6
+    assert ainfo["kernel_launches"] - binfo["kernel_launches"] == 6
+    for x, y in zip(atr, btr):
+        assert np.array_equal(np.array(list(x.values())), np.array(list(y.values())),
+                              equal_nan=True), (x, y)
+    for f in ("y", "z", "P"):
+        assert np.array_equal(getattr(a, f).cpu().numpy(), getattr(b, f).cpu().numpy()), f
+    assert a.primal_obj == b.primal_obj and a.tr_X == b.tr_X
+
+
 def test_usbs_graph_not_used_with_inequalities(cuda):
     """The QAP relaxation decides its upsilon loop on the host: it runs eagerly."""
     from usbs_gb300 import solver

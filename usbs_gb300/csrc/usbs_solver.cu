@@ -501,11 +501,37 @@ struct RowsArgs {
   double* Vn;
   int ldvn;
   const int* skip;
+  // constraint evaluation in the same pass (every constraint one diagonal
+  // entry): row i is constraint row_con[i]; nullptr leaves it to quadform_kernel
+  const int* row_con;
+  const int* con_ptr;
+  const double* t_a;
+  double* AF;
+  double* AFc;
 };
+
+// Constraint of each row when every constraint is a single diagonal entry
+// (A(X)_c = a_c X_ii, as in MaxCut's diag(X) = b): row_con[i] = c.  row_con
+// starts at -1 and row_con[n] at 0; row_con[n] becomes non-zero unless the
+// map is a bijection between the constraints (m = n) and the rows.
+__global__ void diag_map_kernel(int n, int m, const int* __restrict__ con_ptr,
+                                const int* __restrict__ t_row, const int* __restrict__ t_col,
+                                int* __restrict__ row_con) {
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < m; c += gridDim.x * blockDim.x) {
+    const int t0 = con_ptr[c], t1 = con_ptr[c + 1];
+    bool ok = (t1 - t0 == 1);
+    const int i = ok ? t_row[t0] : -1;
+    if (ok && (t_col[t0] != i || i < 0 || i >= n)) ok = false;
+    if (ok && atomicExch(&row_con[i], c) != -1) ok = false;
+    if (!ok) atomicOr(&row_con[n], 1);
+  }
+}
 
 // P <- eta P_bar + F (F^T Omega), P_bar <- eta P_bar + F_c (F_c^T Omega) and the
 // kept directions V W[:, k_curr:] of the next basis (solver/usbs.py:572-580,
-// 628-636, 640).  One thread per row.
+// 628-636, 640).  One thread per row.  With row_con, the same pass over V also
+// evaluates the constraints A(F F^T) and A(F_c F_c^T) (solver/usbs.py:411-412,
+// 570-571), each row's value computed as quadform_kernel computes it.
 __global__ void rows_update_kernel(RowsArgs a) {
   if (a.skip && *a.skip) return;
   __shared__ double Ms[IPM_MAXK * 64], Mcs[IPM_MAXK * 64], Wp[IPM_MAXK * IPM_MAXK];
@@ -514,7 +540,7 @@ __global__ void rows_update_kernel(RowsArgs a) {
   const double* sm = a.smalls;
   if (a.mode == 0)
     for (int e = threadIdx.x; e < k * ssk; e += blockDim.x) { Ms[e] = sm[a.o_M + e]; Mcs[e] = sm[a.o_Mc + e]; }
-  if (a.mode == 2)
+  if (a.mode == 2 || a.row_con)
     for (int e = threadIdx.x; e < k * k; e += blockDim.x) { Sp[e] = sm[a.o_Splus + e]; Scp[e] = sm[a.o_Scplus + e]; }
   for (int e = threadIdx.x; e < k * kp; e += blockDim.x) Wp[e] = sm[a.o_Wpast + e];
   __syncthreads();
@@ -523,6 +549,28 @@ __global__ void rows_update_kernel(RowsArgs a) {
     double v[IPM_MAXK];
 #pragma unroll
     for (int q = 0; q < IPM_MAXK; ++q) v[q] = (q < k) ? a.V[(size_t)q * a.ldv + i] : 0.0;
+    if (a.row_con) {
+      // v^T S+ v and v^T Sc+ v in quadform_kernel's order (u = w = v)
+      double s1 = 0.0, s2 = 0.0;
+#pragma unroll
+      for (int p = 0; p < IPM_MAXK; ++p) {
+        if (p < k) {
+          double r1 = 0.0, r2 = 0.0;
+#pragma unroll
+          for (int q = 0; q < IPM_MAXK; ++q)
+            if (q < k) { r1 += Sp[p * k + q] * v[q]; r2 += Scp[p * k + q] * v[q]; }
+          s1 += v[p] * r1;
+          s2 += v[p] * r2;
+        }
+      }
+      const int c = a.row_con[i];
+      const double ta = a.t_a[a.con_ptr[c]];
+      double a1 = 0.0, a2 = 0.0;
+      a1 += ta * s1;
+      a2 += ta * s2;
+      a.AF[c] = a1;
+      if (a.AFc) a.AFc[c] = a2;
+    }
     if (a.mode == 0) {
       for (int c = 0; c < ssk; ++c) {
         double s1 = 0.0, s2 = 0.0;
@@ -735,6 +783,8 @@ struct Layout {
   double *smalls, *CV, *CV2, *Vn, *op64, *op64b, *bmu, *AF, *AFc, *ycand, *zbar, *ups, *Pm,
       *gpart, *gpart2, *mpart, *Pbar, *Xbar, *alpha, *beta;
   void *opL, *Q, *lz_work, *q0L;
+  int* row_con;     // n + 4: constraint of each row, flag at [n] (diag_map_kernel)
+  bool diag = false;   // every constraint one diagonal entry: one pass over V
   unsigned int* counters;
   int* status;
   int* ctl;
@@ -787,6 +837,7 @@ static int plan(const usbs_problem* P, const usbs_params* Pa, const DeviceInfo& 
   L.status = ar.take<int>(32);
   L.ctl = L.status + 16;
   L.skip = ar.take<int>(4);
+  L.row_con = ar.take<int>((size_t)L.n + 4);
   const bool stream = Pa->lanczos_path == 2;
   const int nct = lanczos_team_size(di, L.n, Pa->precision, stream);
   L.lz_work = ar.take<char>(
@@ -926,6 +977,18 @@ struct Solver {
     if (b > L.grid_red) b = L.grid_red;
     return b < 1 ? 1 : b;
   }
+  RowsArgs rows_args(bool with_constraints) const {
+    RowsArgs ra;
+    const double* V = S->V;
+    ra.n = L.n; ra.k = L.k; ra.kp = L.kp; ra.ssk = L.ssk; ra.mode = Pa->sketch_mode;
+    ra.V = V; ra.ldv = L.ld; ra.P = S->P; ra.Pbar = L.Pbar; ra.ldp = L.ld; ra.smalls = L.smalls;
+    ra.o_sc = L.o_sc; ra.o_M = L.o_M; ra.o_Mc = L.o_Mc; ra.o_Splus = L.o_Splus;
+    ra.o_Scplus = L.o_Scplus; ra.o_Wpast = L.o_Wpast; ra.Vn = L.Vn; ra.ldvn = L.ld;
+    ra.skip = nullptr;
+    ra.row_con = with_constraints ? L.row_con : nullptr;
+    ra.con_ptr = P->con_ptr; ra.t_a = P->t_a; ra.AF = L.AF; ra.AFc = L.AFc;
+    return ra;
+  }
   int rgrid() const {
     int b = (L.n + 255) / 256;
     if (b > di.sm_count * 8) b = di.sm_count * 8;
@@ -1057,11 +1120,20 @@ static int body(Solver& X, int t) {
     CK(X.run_ipm(0));
     ++X.launches;
     CK(launch_eigS(ea, st));
-    ++X.launches;
-    quadform_kernel<<<qblocks, 256, 0, st>>>(L.m, P->con_ptr, P->t_row, P->t_col, P->t_a, V, L.ld,
-                                             L.k, L.smalls + L.o_Splus, L.smalls + L.o_Scplus,
-                                             L.AF, L.AFc, nullptr);
-    CK(kerr("quadform"));
+    if (L.diag) {
+      // constraint evaluation and the sketch / kept-direction updates in one
+      // pass over V (nothing in between reads P, P_bar or the kept directions)
+      RowsArgs ra = X.rows_args(true);
+      ++X.launches;
+      rows_update_kernel<<<X.rgrid(), 256, 0, st>>>(ra);
+      CK(kerr("rows_update"));
+    } else {
+      ++X.launches;
+      quadform_kernel<<<qblocks, 256, 0, st>>>(L.m, P->con_ptr, P->t_row, P->t_col, P->t_a, V,
+                                               L.ld, L.k, L.smalls + L.o_Splus,
+                                               L.smalls + L.o_Scplus, L.AF, L.AFc, nullptr);
+      CK(kerr("quadform"));
+    }
     if (!P->has_ineq) break;       // upsilon stays 0: the loop ends after one pass
     MvecArgs ma = X.margs();
     ++X.launches;
@@ -1096,13 +1168,8 @@ static int body(Solver& X, int t) {
                                                     L.o_Scplus, S->X, L.Xbar, nullptr);
     CK(kerr("xmode"));
   }
-  {
-    RowsArgs ra;
-    ra.n = L.n; ra.k = L.k; ra.kp = L.kp; ra.ssk = L.ssk; ra.mode = Pa->sketch_mode;
-    ra.V = V; ra.ldv = L.ld; ra.P = S->P; ra.Pbar = L.Pbar; ra.ldp = L.ld; ra.smalls = L.smalls;
-    ra.o_sc = L.o_sc; ra.o_M = L.o_M; ra.o_Mc = L.o_Mc; ra.o_Splus = L.o_Splus;
-    ra.o_Scplus = L.o_Scplus; ra.o_Wpast = L.o_Wpast; ra.Vn = L.Vn; ra.ldvn = L.ld;
-    ra.skip = nullptr;
+  if (!L.diag) {
+    RowsArgs ra = X.rows_args(false);
     ++X.launches;
     rows_update_kernel<<<X.rgrid(), 256, 0, st>>>(ra);
     CK(kerr("rows_update"));
@@ -1539,10 +1606,27 @@ int usbs_solve(const usbs_problem* P, const usbs_params* Pa, usbs_state* S, void
       CK(kerr("rinv"));
     }
   }
+  // one pass over V for the constraints and the row updates when every
+  // constraint is a single diagonal entry (USBS_FUSED_ROWS=0 keeps two passes)
+  int diag_flag = 1;
+  {
+    const char* e = getenv("USBS_FUSED_ROWS");
+    if (!P->has_ineq && L.m == L.n && !(e && atoi(e) == 0)) {
+      cudaMemsetAsync(L.row_con, 0xff, (size_t)L.n * sizeof(int), st);
+      cudaMemsetAsync(L.row_con + L.n, 0, sizeof(int), st);
+      diag_map_kernel<<<X.mgrid(), 256, 0, st>>>(L.n, L.m, P->con_ptr, P->t_row, P->t_col,
+                                                 L.row_con);
+      CK(kerr("diag map"));
+      if (cudaMemcpyAsync(&diag_flag, L.row_con + L.n, sizeof(int), cudaMemcpyDeviceToHost, st) !=
+          cudaSuccess)
+        return kerr("diag map read");
+    }
+  }
   double alpha0 = 0.0;
   if (cudaMemcpyAsync(&alpha0, L.alpha, sizeof(double), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
     return kerr("init eig");
+  L.diag = (diag_flag == 0);
   double by0 = 0.0;
   {
     MvecArgs ma = X.margs();
