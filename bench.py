@@ -210,24 +210,40 @@ def spmv_gbs(device, reps=20):
         lib.usbs_gather_values(L["stored"], p(src), p(vals_dev), p(slv), 32, api._stream())
         ms = timed(lambda: lib.usbs_operator_apply_sell(n, p(slp), p(slc), p(slv), p(slr), p(x),
                                                          p(y), 32, api._stream()))
-        return ms, L["stored"]
+        return ms, L["stored"], slc, slv
 
     ms_csr = timed(lambda: lib.usbs_operator_apply(n, nnz, p(prob.rowptr), p(prob.col), p(op),
                                                    p(x), p(y), 32, api._stream()))
-    ms_sell, stored = sell_case(host.rowptr, host.col, op)
+    ms_sell, stored, _, _ = sell_case(host.rowptr, host.col, op)
     # renumbered copy of the same operator
     Cop = sp.csr_matrix((op.cpu().numpy(), host.col, host.rowptr), shape=(n, n))
     perm = reverse_cuthill_mckee(Cop, symmetric_mode=True)
     Cr = Cop[perm][:, perm].tocsr()
     Cr.sort_indices()
-    ms_rcm, _ = sell_case(Cr.indptr, Cr.indices,
-                          torch.as_tensor(Cr.data, device=device, dtype=torch.float32))
+    ms_rcm, _, slc, slv = sell_case(Cr.indptr, Cr.indices,
+                                    torch.as_tensor(Cr.data, device=device, dtype=torch.float32))
+    # what a kernel of this size reaches: one coalesced 16-byte pass over the same
+    # column and value arrays (no gathers), timed the same way
+    pb = (slc.numel() * 4) // 16 * 16
+    sums = torch.empty(4 * 152 * 8, dtype=torch.float32, device=device)
+    xors = torch.empty(4 * 152 * 8, dtype=torch.int32, device=device)
+    ms_stream = {}
+    for blocks in (152 * 8, 152 * 32):
+        ms_stream[blocks] = timed(lambda: lib.usbs_stream_probe(
+            p(slc), pb, p(slv), pb, blocks, p(sums), p(xors), api._stream()))
+    ms_probe = min(ms_stream.values())
     gbs = lambda ms: alg / (ms * 1e-3) / 1e9
     return {"graph": "rgg n=1e6 k=6", "nnz": int(nnz), "alg_bytes": alg,
             "kernel": "sell_spmv_kernel<float>", "ms": ms_sell, "gbs": gbs(ms_sell),
             "stored_over_nnz": stored / nnz,
             "csr_kernel": {"ms": ms_csr, "gbs": gbs(ms_csr)},
             "sell_after_rcm_renumbering": {"ms": ms_rcm, "gbs": gbs(ms_rcm)},
+            "stream_probe_same_arrays": {
+                "bytes": 2 * pb, "ms": ms_probe, "gbs": 2 * pb / (ms_probe * 1e-3) / 1e9,
+                "note": "one coalesced pass over the renumbered operator's column and value "
+                        "arrays (no gathers, x and y not touched), one launch after the L2 "
+                        "flush: the bandwidth a kernel of this size reaches here",
+                "sell_after_rcm_gbs_over_probe_gbs": gbs(ms_rcm) / (2 * pb / (ms_probe * 1e-3) / 1e9)},
             "eigsh": eigsh_leg(device, prob, n, flush, flush_rd),
             "eigsh_after_rcm_renumbering": eigsh_renumbered(device, st, n, flush, flush_rd),
             "usbs_solve": rgg_solve_leg(device, st, n)}

@@ -75,6 +75,17 @@ int usbs_operator_apply_sell(int n, const int* sl_ptr, const int* sl_col, const 
                              const unsigned char* sl_row, const void* x, void* y, int precision,
                              void* stream);
 
+/* Bandwidth reference for the operator apply, no counterpart in the
+ * reference: one pass over a (a_bytes, read as 16-byte integer words) and b
+ * (b_bytes, read as groups of four floats) with coalesced 16-byte loads and
+ * no gathers, on `blocks` blocks of 256 threads.  Block k writes the sum of
+ * the floats it read to out_sum[k] and the XOR of the 32-bit words of a it
+ * read to out_xor[k].  Timed like usbs_operator_apply_sell over the same
+ * bytes, it gives the bandwidth a kernel of that size reaches on this GPU.
+ * Byte counts must be multiples of 16 and both buffers 16-byte aligned. */
+int usbs_stream_probe(const void* a, long long a_bytes, const void* b, long long b_bytes,
+                      int blocks, float* out_sum, unsigned* out_xor, void* stream);
+
 /* dst[e] = src[map[e]] (0 where map[e] < 0), `total` entries of the
  * `precision` type: the CSR operator values moved into sliced-ELL order. */
 int usbs_gather_values(long long total, const int* map, const void* src, void* dst,

@@ -224,6 +224,34 @@ def test_sell_apply_matches_csr(cuda, shape, precision):
     assert np.all(np.abs(y.double().cpu().numpy() - ref) <= tol * scale)
 
 
+@pytest.mark.parametrize("a_words,b_words,blocks", [(1000, 3000, 7), (4096, 0, 1), (0, 777, 3)])
+def test_stream_probe_reads_every_word_once(cuda, a_words, b_words, blocks):
+    """usbs_stream_probe (the bandwidth reference of the bench's SpMV leg) reads
+    each 16-byte word of both buffers exactly once: the blocks' XORs combine to
+    the XOR of a, their sums to the sum of b; unaligned sizes are rejected."""
+    import ctypes
+    import torch
+    from usbs_gb300 import _lib
+    lib = _lib.load()
+    rng = np.random.default_rng(a_words + b_words)
+    a = torch.tensor(rng.integers(-2 ** 31, 2 ** 31, 4 * max(a_words, 1)), dtype=torch.int32,
+                     device=cuda)
+    b = torch.tensor(rng.integers(-8, 9, 4 * max(b_words, 1)), dtype=torch.float32, device=cuda)
+    sums = torch.full((blocks,), float("nan"), dtype=torch.float32, device=cuda)
+    xors = torch.full((blocks,), -1, dtype=torch.int32, device=cuda)
+    p = lambda t: ctypes.c_void_p(t.data_ptr())
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.usbs_stream_probe(p(a), 16 * a_words, p(b), 16 * b_words, blocks, p(sums), p(xors),
+                                 s) == 0
+    torch.cuda.synchronize()
+    want_x = np.bitwise_xor.reduce(a.cpu().numpy()[:4 * a_words]) if a_words else 0
+    got_x = np.bitwise_xor.reduce(xors.cpu().numpy())
+    assert got_x == want_x
+    # small integers: every partial sum is exact in FP32
+    assert float(sums.double().sum()) == float(b.cpu().numpy()[:4 * b_words].sum())
+    assert lib.usbs_stream_probe(p(a), 8, p(b), 0, 1, p(sums), p(xors), s) == -2
+
+
 # Problems too large for one cluster: the cooperative team kernel while x fits
 # in shared memory (n = 15,625 in FP64), the stream path past that (a
 # sequence of full-GPU launches; n > 20,480 in FP64, 40,960 in FP32)

@@ -25,6 +25,7 @@ SIGNATURES = {
     "usbs_operator_apply": (c_int, [c_int, c_ll, P, P, P, P, P, c_int, P]),
     "usbs_operator_apply_sell": (c_int, [c_int, P, P, P, P, P, P, c_int, P]),
     "usbs_gather_values": (c_int, [c_ll, P, P, P, c_int, P]),
+    "usbs_stream_probe": (c_int, [P, c_ll, P, c_ll, c_int, P, P, P]),
     "usbs_apply_A_operator": (c_int, [c_int, c_int, P, P, P, P, P, c_int, P, P]),
     "usbs_apply_A_adjoint": (c_int, [c_int, c_int, P, P, P, P, P, P, c_int, P, c_int, P]),
     "usbs_lanczos_kernel": (c_int, [c_int, c_int, c_int]),

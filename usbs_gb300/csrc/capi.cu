@@ -163,6 +163,24 @@ int usbs_operator_apply_sell(int n, const int* sl_ptr, const int* sl_col, const 
   return sell_spmv(n, sl_ptr, sl_col, sl_val, sl_row, x, y, precision, (cudaStream_t)stream);
 }
 
+int usbs_stream_probe(const void* a, long long a_bytes, const void* b, long long b_bytes,
+                      int blocks, float* out_sum, unsigned* out_xor, void* stream) {
+  if (a_bytes < 0 || b_bytes < 0 || (a_bytes & 15) || (b_bytes & 15)) {
+    set_error("usbs_stream_probe: byte counts must be non-negative multiples of 16");
+    return -2;
+  }
+  if ((a_bytes && ((uintptr_t)a & 15)) || (b_bytes && ((uintptr_t)b & 15))) {
+    set_error("usbs_stream_probe: buffers must be 16-byte aligned");
+    return -2;
+  }
+  if (blocks < 1 || !out_sum || !out_xor) {
+    set_error("usbs_stream_probe: blocks >= 1 and both outputs are required");
+    return -2;
+  }
+  return stream_probe(a_bytes / 16, a, b_bytes / 16, b, blocks, out_sum, out_xor,
+                      (cudaStream_t)stream);
+}
+
 int usbs_gather_values(long long total, const int* map, const void* src, void* dst,
                        int precision, void* stream) {
   if (precision != 32 && precision != 64) { set_error("precision must be 32 or 64"); return -2; }

@@ -75,6 +75,9 @@ int csr_spmv(int n, long long nnz, const int* rowptr, const int* col, const void
 // y = M x for M in the sliced-ELL layout (windows of 256 rows, 32-row slices)
 int sell_spmv(int n, const int* sl_ptr, const int* col, const void* val,
               const unsigned char* sl_row, const void* x, void* y, int prec, cudaStream_t stream);
+// one pass over a (int4 words) and b (float4 words); per-block sum / XOR
+int stream_probe(long long a_words, const void* a, long long b_words, const void* b, int blocks,
+                 float* out_sum, unsigned* out_xor, cudaStream_t stream);
 // dst[e] = src[map[e]], 0 where map[e] < 0
 int gather_values(long long total, const int* map, const void* src, void* dst, int prec,
                   cudaStream_t stream);

@@ -167,6 +167,57 @@ int sell_spmv(int n, const int* sl_ptr, const int* col, const void* val,
   return 0;
 }
 
+// Streaming reference for the SpMV's bandwidth: one pass over a (int4 words)
+// and b (float4 words) with 16-byte loads, grid-stride, no gathers; block k
+// writes the sum of the floats it read to out_sum[k] and the XOR of the words
+// it read to out_xor[k].  Timed like the SpMV (one launch after an L2 flush),
+// it shows what a kernel moving the same bytes can reach at that size.
+__global__ void __launch_bounds__(256) stream_probe_kernel(long long na, const int4* __restrict__ a,
+                                                           long long nb, const float4* __restrict__ b,
+                                                           float* __restrict__ out_sum,
+                                                           unsigned* __restrict__ out_xor) {
+  __shared__ float ssum[8];
+  __shared__ unsigned sxor[8];
+  float acc = 0.f;
+  unsigned x = 0u;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long nmax = na > nb ? na : nb;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < nmax; i += stride) {
+    if (i < na) {
+      const int4 u = __ldg(a + i);
+      x ^= (unsigned)u.x ^ (unsigned)u.y ^ (unsigned)u.z ^ (unsigned)u.w;
+    }
+    if (i < nb) {
+      const float4 v = __ldg(b + i);
+      acc += (v.x + v.y) + (v.z + v.w);
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    x ^= __shfl_xor_sync(0xffffffffu, x, o);
+  }
+  const int warp = threadIdx.x >> 5;
+  if ((threadIdx.x & 31) == 0) { ssum[warp] = acc; sxor[warp] = x; }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float t = 0.f;
+    unsigned u = 0u;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) { t += ssum[w]; u ^= sxor[w]; }
+    out_sum[blockIdx.x] = t;
+    out_xor[blockIdx.x] = u;
+  }
+}
+
+int stream_probe(long long a_words, const void* a, long long b_words, const void* b, int blocks,
+                 float* out_sum, unsigned* out_xor, cudaStream_t stream) {
+  if (blocks < 1) return 0;
+  stream_probe_kernel<<<blocks, 256, 0, stream>>>(a_words, (const int4*)a, b_words,
+                                                  (const float4*)b, out_sum, out_xor);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) { set_error("stream_probe: %s", cudaGetErrorString(e)); return -5; }
+  return 0;
+}
+
 // dst[e] = src[map[e]] (0 where map[e] < 0): operator values from CSR to sliced-ELL order
 template <typename VT>
 __global__ void gather_values_kernel(long long total, const int* __restrict__ map,
