@@ -9,6 +9,17 @@ from any implementation:
   - complete graph K_n, unit weights: n^2 / 4;
   - even side x side torus, unit weights (bipartite, 4-regular): the bound
     (n/4) lambda_max(L) = 2n is met by the bipartition, so the value is |E| = 2n.
+  - vertex-transitive graphs, unit weights: the value is (n/4) lambda_max(L)
+    (Delorme and Poljak, "Laplacian eigenvalues and the maximum cut problem",
+    Math. Programming 62, 1993: the eigenvalue bound with the optimal diagonal
+    correction, which is zero for a vertex-transitive graph, equals the SDP
+    value).  Non-bipartite cases, where the value lies strictly above the
+    maximum cut:
+    - odd cycle C_n: lambda_max(L) = 2 + 2 cos(pi / n), value (n/2)(1 + cos(pi/n));
+    - Petersen graph: adjacency spectrum {3, 1, -2}, so lambda_max(L) = 5 and
+      the value is 12.5 (its maximum cut is 12);
+    - odd side x side torus: lambda_max(L) = 2 (2 + 2 cos(pi / side)), value
+      side^2 (1 + cos(pi / side)).
 
 Run:  python tests/golden/make_known_answers.py
 """
@@ -32,6 +43,12 @@ def main():
         "cycle_laplacian": {"n": 150, "smallest": cycle_spectrum(150, 5)},
         "maxcut_sdp_complete_graph": {"n": 12, "value": 12 * 12 / 4.0},
         "maxcut_sdp_even_torus": {"side": 6, "n": 36, "edges": 72, "value": 72.0},
+        "maxcut_sdp_vertex_transitive": [
+            {"graph": ["cycle", 7], "n": 7, "value": 3.5 * (1.0 + math.cos(math.pi / 7))},
+            {"graph": ["cycle", 9], "n": 9, "value": 4.5 * (1.0 + math.cos(math.pi / 9))},
+            {"graph": ["petersen"], "n": 10, "value": 12.5},
+            {"graph": ["torus_unit", 5], "n": 25, "value": 25.0 * (1.0 + math.cos(math.pi / 5))},
+        ],
     }
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "known_answers.json")
     with open(path, "w") as f:

@@ -71,3 +71,30 @@ def test_er800_to_1e2_matches_oracle_solution(cuda, precision):
     assert last["obj_gap"] <= eps and last["infeas_gap"] <= eps and last["max_infeas"] <= eps
     assert abs(out.primal_obj - rec["primal_obj"]) <= 2 * eps * abs(rec["primal_obj"])
     assert abs(info["iterations"] - rec["iterations"]) <= 0.25 * rec["iterations"]
+
+
+KNOWN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "known_answers.json")
+
+
+@pytest.mark.parametrize("precision", [64, 32])
+@pytest.mark.parametrize("idx", range(4))
+def test_solve_reaches_vertex_transitive_closed_form(cuda, idx, precision):
+    """Odd cycles, the Petersen graph and the odd 5 x 5 torus: the MaxCut SDP
+    value (n/4) lambda_max(L) lies strictly above the maximum cut and comes
+    from mathematics, not from an implementation.  The device solve reaches it
+    in FP64 and in mixed precision, with the dual bound above it."""
+    from usbs_gb300 import solver
+    from usbs_gb300.problems import maxcut
+    with open(KNOWN) as f:
+        g = json.load(f)["maxcut_sdp_vertex_transitive"][idx]
+    W = wl.graph_from_spec(g["graph"])
+    n = W.shape[0]
+    st = maxcut.initialize_state(W, 4)
+    out, tr, info = solver.usbs(st, n, n, 2.0 * n, 2.0, 0.01, 0.25, 3, 1, 300, np.inf, 1e-6, 1e-6,
+                                1e-6, min(n, 32), 10, 1e-7, 100, precision=precision,
+                                return_trace=True)
+    assert info["status"] == 0
+    tol = 1e-4 if precision == 64 else 1e-3
+    assert abs(out.primal_obj - g["value"]) / g["value"] < tol
+    assert tr[-1]["max_infeas"] < 10 * tol
+    assert tr[-1]["obj_ub"] >= g["value"] * (1.0 - 1e-6)

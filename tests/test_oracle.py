@@ -252,3 +252,22 @@ def test_golden_maxcut_sdp_even_torus():
     out, fin = ousbs.usbs(st, n, n, 2.0 * n, 2.0, 0.01, 0.25, 3, 1, 300, np.inf, 1e-6, 1e-6,
                           1e-6, min(n, 32), 10, 1e-7, 100)
     assert abs(out.primal_obj - g["value"]) / g["value"] < 2e-3
+
+
+@pytest.mark.parametrize("idx", range(4))
+def test_golden_maxcut_sdp_vertex_transitive(idx):
+    """Vertex-transitive graphs (odd cycles, the Petersen graph, the odd torus):
+    the MaxCut SDP value is (n/4) lambda_max(L), strictly above the maximum
+    cut; the oracle's solve reaches it."""
+    from usbs_gb300 import workloads as wl
+    g = _golden()["maxcut_sdp_vertex_transitive"][idx]
+    W = wl.graph_from_spec(g["graph"])
+    n = W.shape[0]
+    assert n == g["n"]
+    L = np.diag(np.asarray(W.sum(axis=1)).ravel()) - W.toarray()
+    assert abs(n / 4.0 * np.linalg.eigvalsh(L)[-1] - g["value"]) < 1e-12 * g["value"]
+    st = omaxcut.initialize_state(W, 4)
+    out, fin = ousbs.usbs(st, n, n, 2.0 * n, 2.0, 0.01, 0.25, 3, 1, 300, np.inf, 1e-6, 1e-6,
+                          1e-6, min(n, 32), 10, 1e-7, 100)
+    assert abs(out.primal_obj - g["value"]) / g["value"] < 1e-4
+    assert fin["max_infeas"] < 1e-4

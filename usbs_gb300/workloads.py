@@ -121,13 +121,33 @@ def serving_stream(num_requests=1024, rate=20.0, seed=4, n_lo=200, n_hi=50000, d
     return reqs
 
 
+def cycle_graph(n):
+    """The n-cycle, unit weights."""
+    i = np.arange(n)
+    A = sp.coo_matrix((np.ones(n), (i, (i + 1) % n)), shape=(n, n))
+    return (A + A.T).tocsr()
+
+
+def petersen_graph():
+    """The Petersen graph: outer 5-cycle, spokes i -- i+5, inner pentagram."""
+    e = ([(i, (i + 1) % 5) for i in range(5)] + [(i, i + 5) for i in range(5)]
+         + [(5 + i, 5 + (i + 2) % 5) for i in range(5)])
+    i, j = (np.array(v) for v in zip(*e))
+    A = sp.coo_matrix((np.ones(i.size), (i, j)), shape=(10, 10))
+    return (A + A.T).tocsr()
+
+
 def graph_from_spec(spec):
-    """("er", n, edges, seed) or ("torus_unit", side): the graphs named in
-    recorded solves."""
+    """("er", n, edges, seed), ("torus_unit", side), ("cycle", n) or
+    ("petersen",): the graphs named in recorded solves and known answers."""
     if spec[0] == "er":
         return er_graph(int(spec[1]), int(spec[2]), int(spec[3]))
     if spec[0] == "torus_unit":
         return torus_graph(int(spec[1]), 0, weights="unit")
+    if spec[0] == "cycle":
+        return cycle_graph(int(spec[1]))
+    if spec[0] == "petersen":
+        return petersen_graph()
     raise ValueError(f"unknown graph spec {spec!r}")
 
 
