@@ -45,6 +45,10 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
+# the serving legs run up to 32 solves at once, two streams each: give CUDA
+# enough hardware queues that their streams do not share queue heads (8 by
+# default; read when the CUDA context is created, so set before any CUDA use)
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
 
 import numpy as np  # noqa: E402
 
@@ -690,7 +694,7 @@ def solves_leg(device):
     return out
 
 
-def serving_stream_leg(device, count=1024, iters=20, slots=16, serial_sample=32):
+def serving_stream_leg(device, count=1024, iters=20, slots=32, serial_sample=32):
     """The serving workload: `count` Erdos-Renyi MaxCut requests with Poisson
     arrivals at 20/s, n log-uniform in [200, 50000], mean degree uniform in
     [4, 40], unit weights; 30% are variants of an earlier request (1% of its

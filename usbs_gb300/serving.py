@@ -33,6 +33,14 @@ waiting forever. A request that is still queued can be withdrawn with
 ``SolverService.cancel()`` (``wait()`` then raises ``RequestCancelled``); a
 solve that has started runs to its end.
 
+Concurrency on the device: every running solve uses two CUDA streams, and CUDA
+maps streams onto CUDA_DEVICE_MAX_CONNECTIONS hardware queues (8 by default),
+where a kernel waits behind whatever heads its queue. A process that runs many
+slots should set CUDA_DEVICE_MAX_CONNECTIONS=32 before CUDA is initialised (the
+library cannot change it afterwards). Measured on the 1,024-request serving
+stream (n up to 50,000): 17.2 solves/s, p50 5.6 s, p99 7.5 s with 16 slots and
+8 queues; 18.3 solves/s, p50 3.6 s, p99 4.9 s with 32 slots and 32 queues.
+
 The reference has no serving layer. Each result is the same as a solve of that
 request alone: the kernels are deterministic and share no state between solves.
 """
