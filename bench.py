@@ -54,7 +54,7 @@ import numpy as np  # noqa: E402
 
 METRIC = "SDP solves/s and p50/p99 latency at 1e-4 rel gap; Lanczos SpMV HBM GB/s"
 UNIT = "USBS outer iterations/s"
-LANCZOS_CLUSTER_TRAFFIC_TORUS100 = 687616   # bytes per launch (ncu, GB300)
+LANCZOS_CLUSTER_TRAFFIC_TORUS100 = 653312   # bytes per launch (ncu, GB300)
 SETTINGS = dict(k_curr=10, k_past=1, sketch_dim=10, rho=0.01, beta=0.25, trace_factor=2.0,
                 subprob_eps=1e-7, subprob_max_iters=100, lanczos_inner_iterations=32,
                 lanczos_max_restarts=10, gap_eps=1e-4)
