@@ -94,6 +94,7 @@ struct LzShared {
       double W[MAXM * MP1];
     } rs;
     VT Ys[MAXM * MAXM];          // saved Ritz vectors, every CTA, after the restart barrier
+    double red4[4][MP1];         // cluster reduction: the four level-two sums
   } u;
   double h[MP1];
   VT hv[MP1];                    // h in the vector type, converted once per reduction
@@ -1396,27 +1397,37 @@ __host__ __device__ inline ClLayout cl_layout(int m, int rc, int csr_cap) {
 }
 
 // h[c] = sum over the cluster's CTAs r = 0..C-1 of part_r[c], c < nv, summed
-// as a fixed pairwise tree (FP64 adds are ~64 cycles dependent on this part).
+// as a fixed pairwise tree over 16 slots (slots r >= C hold 0): level one adds
+// slots r and r+8, level two r and r+4, level three r and r+2, level four r and
+// r+1.  An FP64 add holds its SM sub-partition's FP64 pipe for ~64 cycles, so
+// warps 0..3 (one per sub-partition) each form one level-two sum
+// R_w = (v_w + v_{w+8}) + (v_{w+4} + v_{w+12}), and warp 0 then forms
+// (R_0 + R_2) + (R_1 + R_3): the tree's association, spread over four pipes.
 // With norm set (nv = 1), lane 0 also forms sh.bnorm = sqrt(h[0]) and
 // sh.binv = 1 / bnorm once for the CTA (FP64 square roots and divisions are
-// long dependent DFMA chains on this part's narrow FP64 pipe).
+// long dependent chains on this part's narrow FP64 pipe).
+static_assert(CL_MAX_CTAS == 16, "the reduction tree below is written for 16 slots");
 template <typename VT>
 __device__ __forceinline__ void cl_reduce(const double* part, int C, int nv, LzShared<VT>& sh,
                                           bool norm = false) {
-  const int lane = threadIdx.x & 31;
-  if (threadIdx.x < 32) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (wid < 4) {
     for (int c = lane; c < nv; c += 32) {
-      double v[CL_MAX_CTAS];
-#pragma unroll
-      for (int r = 0; r < CL_MAX_CTAS; ++r) v[r] = (r < C) ? cl_ld(cl_map(part + c, r), 0.0) : 0.0;
-#pragma unroll
-      for (int h = CL_MAX_CTAS / 2; h >= 1; h >>= 1)
-#pragma unroll
-        for (int r = 0; r < h; ++r) v[r] = v[r] + v[r + h];
-      sh.h[c] = v[0];
-      sh.hv[c] = (VT)v[0];
+      const double a = (wid < C) ? cl_ld(cl_map(part + c, wid), 0.0) : 0.0;
+      const double b = (wid + 8 < C) ? cl_ld(cl_map(part + c, wid + 8), 0.0) : 0.0;
+      const double d = (wid + 4 < C) ? cl_ld(cl_map(part + c, wid + 4), 0.0) : 0.0;
+      const double e = (wid + 12 < C) ? cl_ld(cl_map(part + c, wid + 12), 0.0) : 0.0;
+      sh.u.red4[wid][c] = (a + b) + (d + e);
+    }
+  }
+  __syncthreads();
+  if (wid == 0) {
+    for (int c = lane; c < nv; c += 32) {
+      const double v = (sh.u.red4[0][c] + sh.u.red4[2][c]) + (sh.u.red4[1][c] + sh.u.red4[3][c]);
+      sh.h[c] = v;
+      sh.hv[c] = (VT)v;
       if (norm) {
-        const double b = sqrt(v[0]);
+        const double b = sqrt(v);
         sh.bnorm = b;
         sh.binv = (VT)(1.0 / b);
       }
