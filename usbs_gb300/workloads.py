@@ -161,11 +161,12 @@ def stream_adjacency(req):
     return A
 
 
-CONFIGS = {
-    "cfg0_er800": dict(kind="maxcut", gen=lambda: er_graph(800, 19176, 0)),
-    "cfg1_torus100": dict(kind="maxcut", gen=lambda: torus_graph(100, 1)),
-    "cfg2_rgg1m": dict(kind="maxcut", gen=lambda: rgg_knn_graph(10 ** 6, 6, 0)),
-    "cfg3_qap30": dict(kind="qap", gen=lambda: qap_instance(30, 0)),
+# the benchmark instances, by what they are
+INSTANCES = {
+    "maxcut_er800_19176": dict(kind="maxcut", gen=lambda: er_graph(800, 19176, 0)),
+    "maxcut_torus100_pm1": dict(kind="maxcut", gen=lambda: torus_graph(100, 1)),
+    "maxcut_rgg1m_knn6": dict(kind="maxcut", gen=lambda: rgg_knn_graph(10 ** 6, 6, 0)),
+    "qap30_grid10": dict(kind="qap", gen=lambda: qap_instance(30, 0)),
 }
 
 # USBS settings of the MaxCut configs (README example command of the reference)
