@@ -107,7 +107,7 @@ __device__ __forceinline__ bool pd_test(const double* A, const double* dA, doubl
 
 struct IpmScal {
   double eta, zeta, omega, mu, step, trS, k1, k2, den, ze, F2, d_eta, d_omega, d_zeta, st, cS,
-      cT, q22, h2, t1, t2, t3, t4;
+      cT, q22, h2, t1, t2, t3, t4, rden;
   int cont, it;
 };
 
@@ -138,17 +138,18 @@ __device__ bool cta_inverse(double* A, int n, double* Ainv, double* fcol, int* p
   __syncthreads();
   for (int j = 0; j < n; ++j) {
     if (tid < 32) {
-      unsigned long long best = 0ull;
-      int bi = 0x7fffffff;
-      if (lane >= j && lane < n) { best = abs_key(A[lane * n + j]); bi = lane; }
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        const unsigned long long k2 = __shfl_xor_sync(0xffffffffu, best, o);
-        const int r2 = __shfl_xor_sync(0xffffffffu, bi, o);
-        if (r2 != 0x7fffffff && (bi == 0x7fffffff || k2 > best || (k2 == best && r2 < bi))) {
-          best = k2; bi = r2;
-        }
-      }
+      // largest |a| key among rows j.., ties to the smaller row: warp reduction
+      // instructions on the high word, then the low word among the lanes
+      // holding the top high word, then the smallest row among ties
+      const bool valid = lane >= j && lane < n;
+      const unsigned long long key = valid ? abs_key(A[lane * n + j]) : 0ull;
+      const unsigned hi = (unsigned)(key >> 32), lo = (unsigned)key;
+      const unsigned mhi = __reduce_max_sync(0xffffffffu, valid ? hi : 0u);
+      const bool th = valid && hi == mhi;
+      const unsigned mlo = __reduce_max_sync(0xffffffffu, th ? lo : 0u);
+      const bool tl = th && lo == mlo;
+      const unsigned mrow = __reduce_min_sync(0xffffffffu, tl ? (unsigned)lane : 0xffffffffu);
+      int bi = (mrow == 0xffffffffu) ? 0x7fffffff : (int)mrow;
       if (lane == 0) {
         if (bi == 0x7fffffff) bi = j;
         *piv_s = bi;
@@ -508,35 +509,48 @@ __global__ void __launch_bounds__(IPM_BLOCK, 1) ipm_kernel(const __grid_constant
       const bool cont = (sc.it < maxit) &&
           ((A.mode == 0) ? (sc.mu > eps && sc.step > eps * eps) : (sc.mu > eps));
       sc.cont = cont;
-      if (cont) {
-        sc.k1 = (1 - sc.trS - sc.eta) / sc.omega;
-        sc.k2 = sc.zeta / sc.eta + q22;
-        sc.den = sc.k1 * sc.k2 + 1;
-        sc.ze = sc.zeta / sc.eta;
-      }
     }
     __syncthreads();
     if (!sc.cont) break;
     const double mu = sc.mu, eta_ = sc.eta, zeta = sc.zeta, omega = sc.omega, tIS = sc.trS;
-    const double k1 = sc.k1, k2 = sc.k2, den = sc.den, ze = sc.ze;
     // ---- Newton system ----
+    // The step's scalar coefficients are chains of FP64 divisions, each
+    // holding an SM sub-partition's FP64 pipe for hundreds of cycles: the last
+    // warp forms them once (k1, k2, den, ze, F2, 1/den and, for the quadratic
+    // subproblem, t1 and t2), while the other warps form F1 = Q11 svec(S) + ...
+    // They are read after the barrier that follows the copy of S below.
+    if (wid == IPM_BLOCK / 32 - 1) {
+      double F2 = 0.0;
+      if (A.mode == 0) {
+        const double d = wdot(sh.q12, sh.sS, s);
+        F2 = d + eta_ * q22 + h2;
+        F2 = F2 + (-zeta + omega);
+      }
+      if (lane == 0) {
+        const double k1 = (1 - tIS - eta_) / omega;
+        const double k2 = zeta / eta_ + q22;
+        const double den = k1 * k2 + 1;
+        const double ze = zeta / eta_;
+        sc.k1 = k1; sc.k2 = k2; sc.den = den; sc.ze = ze;
+        sc.F2 = F2;
+        sc.rden = 1.0 / den;
+        if (A.mode == 0) {
+          sc.t1 = (mu / omega + tIS + eta_ - 1 + k1 * (F2 - mu / eta_ + zeta)) / den;
+          sc.t2 = (F2 - mu / eta_ + zeta - k2 * (mu / omega + tIS + eta_ - 1)) / den;
+        }
+      }
+    }
     if (A.mode == 0) {
       cta_matvec3(Q11, sh.sS, s, sh.part3, sh.F1);
       for (int a = tid; a < s; a += IPM_BLOCK) {
         const double f = sh.F1[a] + eta_ * sh.q12[a] + sh.h1[a];
         sh.F1[a] = f + (-sh.sT[a] + omega * sh.sI[a]);
       }
-      if (wid == 1) {
-        const double d = wdot(sh.q12, sh.sS, s);
-        if (lane == 0) {
-          double F2 = d + eta_ * q22 + h2;
-          sc.F2 = F2 + (-zeta + omega);
-        }
-      }
     }
     // S^-1 (the reference's jnp.linalg.inv, solver/usbs.py:91)
     for (int e = tid; e < k * k; e += IPM_BLOCK) sh.wk[e] = sh.S[e];
     __syncthreads();
+    const double k1 = sc.k1, k2 = sc.k2, den = sc.den, ze = sc.ze;
     {
       const bool okinv = cta_inverse(sh.wk, k, sh.Si, sh.lcol, &s_piv, sh.redv);
       if (!okinv && tid == 0) atomicOr(A.status, ST_SMALL_DENSE_FAIL);
@@ -548,7 +562,7 @@ __global__ void __launch_bounds__(IPM_BLOCK, 1) ipm_kernel(const __grid_constant
     // floating point; mirroring one triangle measurably degrades the Newton
     // steps once the system is ill-conditioned near the end of the IPM)
     const double lbc = (A.mode == 1) ? (ze / (k1 * ze + 1)) : 0.0;
-    const double rden = 1.0 / den;
+    const double rden = sc.rden;
     if (A.mode == 0) {
       for (int a2 = tid; a2 < s; a2 += IPM_BLOCK) {
         sh.u2[a2] = k1 * sh.q12[a2] + sh.sI[a2];
@@ -571,14 +585,9 @@ __global__ void __launch_bounds__(IPM_BLOCK, 1) ipm_kernel(const __grid_constant
       }
       coeff[a2 * s + a] = v;
     }
-    if (tid == 0) {
-      if (A.mode == 0) {
-        sc.t1 = (mu / omega + tIS + eta_ - 1 + k1 * (F2 - mu / eta_ + zeta)) / den;
-        sc.t2 = (F2 - mu / eta_ + zeta - k2 * (mu / omega + tIS + eta_ - 1)) / den;
-      } else {
-        sc.t1 = ze * (-k1 * (mu / eta_ - h2 - omega) + mu / omega + tIS + eta_ - 1) / (-k1 * ze - 1);
-        sc.t2 = h2 - mu / eta_;
-      }
+    if (tid == 0 && A.mode == 1) {
+      sc.t1 = ze * (-k1 * (mu / eta_ - h2 - omega) + mu / omega + tIS + eta_ - 1) / (-k1 * ze - 1);
+      sc.t2 = h2 - mu / eta_;
     }
     __syncthreads();
     for (int a = tid; a < s; a += IPM_BLOCK) {
