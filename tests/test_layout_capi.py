@@ -146,3 +146,41 @@ def test_sell_layout_covers_every_entry_once(shape):
         for k in range(lens[r]):
             e = L["sl_ptr"][q // 32] + 32 * k + q % 32
             assert src[e] == rowptr[r] + k
+
+
+def test_reference_style_calls_reuse_the_device_layout():
+    """eigsh_smallest(n, C, A_data, A_indices, ...) with host arrays, called
+    again with the same problem (as the reference's solver loop does), reuses
+    the resident layout; a changed array, even changed in place, gets a new one;
+    device inputs are laid out afresh."""
+    from usbs_gb300 import api
+    st = omaxcut.initialize_state(wl.er_graph(50, 200, 1), 2)
+    n = st.C.shape[0]
+    made = []
+
+    def make():
+        made.append(object())
+        return made[-1]
+
+    api._LAYOUTS.clear()
+    a = api._problem_for(st.C, st.A_data, st.A_indices, n, "cuda", make=make)
+    b = api._problem_for(st.C.copy(), st.A_data.copy(), st.A_indices.copy(), n, "cuda", make=make)
+    assert a is b and len(made) == 1
+    Ad = st.A_data.copy()
+    Ad[3] *= 2.0
+    c = api._problem_for(st.C, Ad, st.A_indices, n, "cuda", make=make)
+    assert c is not a and len(made) == 2
+    C2 = st.C.copy()
+    C2.data[0] += 1.0
+    d = api._problem_for(C2, st.A_data, st.A_indices, n, "cuda", make=make)
+    assert d is not a and len(made) == 3
+    e = api._problem_for(st.C, st.A_data, st.A_indices, n + 1, "cuda", make=make)   # other m
+    assert e is not a and len(made) == 4
+    assert api._problem_for(st.C, list(st.A_data), st.A_indices, n, "cuda", make=make) is made[-1]
+    assert len(made) == 5                                  # not a host array: no caching
+    for _ in range(10):                                    # bounded
+        Ad = Ad.copy()
+        Ad[0] += 1.0
+        api._problem_for(st.C, Ad, st.A_indices, n, "cuda", make=make)
+    assert len(api._LAYOUTS) == api._LAYOUTS_MAX
+    api._LAYOUTS.clear()

@@ -13,7 +13,9 @@ DLPack producer such as a JAX device array (used in place, no copy, when its
 dtype matches); the outputs are CUDA torch tensors.  There is no CPU path:
 without a CUDA device or without the built library every call raises.
 """
+import collections
 import ctypes
+import hashlib
 
 import numpy as np
 import scipy.sparse as sp
@@ -53,10 +55,52 @@ def _vt(precision):
     raise ValueError("precision must be 64 or 32")
 
 
-def _problem_for(C, A_data, A_indices, m, device):
+# Device layouts of recent reference-style calls (SciPy C, NumPy A_data and
+# A_indices), keyed by the content of those arrays: a caller that passes the same
+# problem every iteration, as the reference's solver loop does, gets the resident
+# layout back instead of a host rebuild and a fresh upload.  A changed array
+# (even in place) changes the key.
+_LAYOUTS = collections.OrderedDict()
+_LAYOUTS_MAX = 4
+
+
+def _digest(*arrays):
+    h = hashlib.blake2b(digest_size=16)
+    for a in arrays:
+        a = np.ascontiguousarray(a)
+        h.update(str((a.dtype.str, a.shape)).encode())
+        h.update(memoryview(a).cast("B"))
+    return h.digest()
+
+
+def _layout_key(C, A_data, A_indices, m, device):
+    """Content key of host inputs, or None when any input is not a host array
+    (device arrays are laid out afresh: hashing them would copy them back)."""
+    if not sp.issparse(C) or not isinstance(A_data, np.ndarray) or \
+            not isinstance(A_indices, np.ndarray):
+        return None
+    Cc = C.tocsr()
+    return (int(m), str(device), Cc.shape, _digest(Cc.data, Cc.indices, Cc.indptr),
+            _digest(A_data, A_indices))
+
+
+def _problem_for(C, A_data, A_indices, m, device, *, make=None):
     if isinstance(C, DeviceProblem):
         return C
-    return DeviceProblem(layout(C, A_data, A_indices, m=m), device=device)
+    make = make if make is not None else \
+        (lambda: DeviceProblem(layout(C, A_data, A_indices, m=m), device=device))
+    key = _layout_key(C, A_data, A_indices, m, device)
+    if key is None:
+        return make()
+    prob = _LAYOUTS.get(key)
+    if prob is None:
+        prob = make()
+        _LAYOUTS[key] = prob
+        while len(_LAYOUTS) > _LAYOUTS_MAX:
+            _LAYOUTS.popitem(last=False)
+    else:
+        _LAYOUTS.move_to_end(key)
+    return prob
 
 
 def _cols(U, n, device):
