@@ -21,7 +21,7 @@ import numpy as np
 import scipy.sparse as sp
 
 from . import _lib
-from .arrays import as_torch, to_device
+from .arrays import as_torch, shape_of, to_device
 from .problem import DeviceProblem, layout
 
 
@@ -118,8 +118,8 @@ def apply_A_operator_batched(m, A_data, A_indices, vecs, *, problem=None, n=None
     torch = _torch()
     lib = _lib.load()
     if problem is None:
-        nn = n if n is not None else int(np.asarray(vecs).shape[0])
-        problem = DeviceProblem(layout(sp.csr_matrix((nn, nn)), A_data, A_indices, m=m), device)
+        nn = n if n is not None else int(shape_of(vecs)[0])
+        problem = _problem_for(sp.csr_matrix((nn, nn)), A_data, A_indices, m, device)
     Ucm, ld, k = _cols(vecs, problem.n, problem.device)
     out = torch.empty(m, dtype=torch.float64, device=problem.device)
     _lib.check(lib.usbs_apply_A_operator(m, k, _p(problem.con_ptr), _p(problem.t_row),
@@ -139,8 +139,7 @@ def apply_A_adjoint_batched(n, A_data, A_indices, z, vecs, *, problem=None, devi
     lib = _lib.load()
     zz = _dev(z, torch.float64, device if problem is None else problem.device)
     if problem is None:
-        problem = DeviceProblem(layout(sp.csr_matrix((n, n)), A_data, A_indices, m=zz.numel()),
-                                device)
+        problem = _problem_for(sp.csr_matrix((n, n)), A_data, A_indices, zz.numel(), device)
     Ucm, ld, k = _cols(vecs, n, problem.device)
     out = torch.empty((k, n), dtype=torch.float64, device=problem.device)
     _lib.check(lib.usbs_apply_A_adjoint(n, k, _p(problem.row_ptr), _p(problem.r_con),
