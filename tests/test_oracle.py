@@ -271,3 +271,24 @@ def test_golden_maxcut_sdp_vertex_transitive(idx):
                           1e-6, min(n, 32), 10, 1e-7, 100)
     assert abs(out.primal_obj - g["value"]) / g["value"] < 1e-4
     assert fin["max_infeas"] < 1e-4
+
+
+@pytest.mark.parametrize("idx", [0, 2, 3])
+def test_golden_cgal_approaches_vertex_transitive_value(idx):
+    """The oracle's CGAL (solver/cgal.py) on the vertex-transitive known answers
+    (C_7, the Petersen graph, the odd 5 x 5 torus): its primal value approaches
+    (n/4) lambda_max(L) at CGAL's sublinear rate, within 5e-3 relative after
+    2000 iterations and closer than after 500."""
+    from oracle import cgal as ocgal
+    from usbs_gb300 import workloads as wl
+    g = _golden()["maxcut_sdp_vertex_transitive"][idx]
+    W = wl.graph_from_spec(g["graph"])
+    n = W.shape[0]
+    st = omaxcut.initialize_state(W, 4)
+    errs = []
+    for iters in (500, 2000):
+        out, fin = ocgal.cgal(st, n, n, float(n), 1.0, iters, np.inf, -1.0, -1.0, -1.0,
+                              min(n, 32), 10, 1e-7)
+        errs.append(abs(out.primal_obj - g["value"]) / g["value"])
+    assert errs[1] < 5e-3 and errs[1] < errs[0]
+    assert fin["max_infeas"] < 5e-3
