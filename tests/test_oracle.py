@@ -292,3 +292,43 @@ def test_golden_cgal_approaches_vertex_transitive_value(idx):
         errs.append(abs(out.primal_obj - g["value"]) / g["value"])
     assert errs[1] < 5e-3 and errs[1] < errs[0]
     assert fin["max_infeas"] < 5e-3
+
+
+@pytest.mark.parametrize("k", [2, 4, 6, 11])
+def test_quad_ipm_solution_is_certified_optimal(k):
+    """solve_quad_subprob_ipm (solver/usbs.py:25-192) minimises the convex
+    quadratic f(x) = x^T Q x / 2 + h^T x, x = (svec S, eta), over S psd,
+    eta >= 0, tr S + eta <= 1.  A feasible x is optimal exactly when the
+    gradient's inner product with x equals the minimum of that linear function
+    over the set, min(0, lambda_min(grad_S f), d f / d eta), which needs no
+    solver to evaluate: an optimality certificate independent of the reference."""
+    U = operators.create_svec_matrix(k)
+    s = k * (k + 1) // 2
+    rs = np.random.default_rng(k)
+    B = rs.standard_normal((s + 1, s + 1))
+    Q = B @ B.T / (s + 1)
+    h = rs.standard_normal(s + 1) * 2.0
+    consts = (1.0, Q[:s, :s], Q[:s, s], Q[s, s], h[:s], h[s])
+    eta, S = oipm.solve_quad_subprob_ipm(U, k, 1.0, consts, 0.5, np.eye(k) / (2 * k), 1e-9, 200)
+    assert np.linalg.eigvalsh(S)[0] > -1e-12 and eta > -1e-12
+    assert np.trace(S) + eta <= 1.0 + 1e-9
+    x = np.append(operators.svec(U, S), eta)
+    g = Q @ x + h
+    lowest = min(0.0, np.linalg.eigvalsh(operators.svec_inv(U, g[:s], k))[0], g[s])
+    assert 0.0 <= g @ x - lowest <= 1e-6 * max(1.0, np.abs(g).max())
+
+
+@pytest.mark.parametrize("k,g2", [(3, 0.0), (5, -4.0), (11, 0.0)])
+def test_lb_ipm_value_equals_its_closed_form(k, g2):
+    """compute_lb_spec_est_ipm (solver/usbs.py:195-356) minimises the linear
+    g_1 . svec S + g_2 eta over the same set; that minimum is
+    min(0, lambda_min(G_1), g_2), so the returned b.y - minimum has a closed
+    form (G_1 = V^T (A*(y) - C) V, g_2 from z_bar . y - the bar objective)."""
+    U = operators.create_svec_matrix(k)
+    rs = np.random.default_rng(10 + k)
+    G = rs.standard_normal((k, k))
+    G = G + G.T
+    by = 3.0
+    lb = oipm.compute_lb_spec_est_ipm(U, k, 1.0, by, np.zeros((k, k)), G, g2, 0.0, 1.0, 1e-9, 200)
+    closed = by - min(0.0, np.linalg.eigvalsh(G)[0], g2)
+    assert abs(lb - closed) <= 1e-6 * max(1.0, abs(closed))
