@@ -332,3 +332,23 @@ def test_lb_ipm_value_equals_its_closed_form(k, g2):
     lb = oipm.compute_lb_spec_est_ipm(U, k, 1.0, by, np.zeros((k, k)), G, g2, 0.0, 1.0, 1e-9, 200)
     closed = by - min(0.0, np.linalg.eigvalsh(G)[0], g2)
     assert abs(lb - closed) <= 1e-6 * max(1.0, abs(closed))
+
+
+def test_lanczos_matches_dense_eigh_on_a_maxcut_operator():
+    """The oracle's thick-restart Lanczos on C + A*(y) of an Erdos-Renyi MaxCut
+    instance with a random y: its converged smallest eigenpairs equal LAPACK's
+    dense eigendecomposition of the same matrix (built column by column from
+    the oracle's own adjoint, itself checked by the adjoint identity)."""
+    from usbs_gb300 import workloads as wl
+    st = omaxcut.initialize_state(wl.er_graph(150, 900, 5), 4)
+    n = st.C.shape[0]
+    y = np.random.default_rng(7).standard_normal(n) * 0.5
+    M = st.C.toarray() + operators.apply_A_adjoint_batched(n, st.A_data, st.A_indices, y,
+                                                           np.eye(n))
+    M = 0.5 * (M + M.T)
+    exact = np.linalg.eigvalsh(M)[:5]
+    vals, vecs, _ = lanczos.eigsh_smallest(n, st.C, st.A_data, st.A_indices, y, rng.default_q0(n),
+                                           5, 32, 300, 1e-10)
+    np.testing.assert_allclose(vals, exact, rtol=0, atol=1e-8 * np.abs(exact).max())
+    r = M @ vecs - vecs * vals[None, :]
+    assert np.linalg.norm(r, axis=0).max() < 1e-6 * np.abs(exact).max()
