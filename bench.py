@@ -142,6 +142,37 @@ def run_usbs(st, n, iters, inst, device, precision=32, q0=None):
                        return_info=True, instance=inst)
 
 
+def lanczos_step_chain(inst, st, n, precision=32):
+    """The cluster Lanczos kernel's own cycle counters for one eigsh call on the
+    benchmark operator (-C + A*(y) at the initial y, the solver's settings):
+    where the cycles of its step chain go.  The kernel keeps its basis in shared
+    memory, so this, not DRAM traffic, is its bound."""
+    from usbs_gb300 import api
+    from usbs_gb300.rng import default_q0
+    S = SETTINGS
+    info = None
+    for _ in range(3):
+        _, _, info = api.eigsh_smallest(n, inst.problem, None, None, np.asarray(st.y),
+                                        default_q0(n), S["k_curr"], S["lanczos_inner_iterations"],
+                                        S["lanczos_max_restarts"], S["subprob_eps"],
+                                        c_scale=-1.0, precision=precision, return_info=True)
+    bar, red, a, b, c = info.phase_kcycles
+    steps = max(info.matvecs, 1)
+    per = lambda kc: round(1024.0 * kc / steps)
+    return {"kernel": f"lanczos_cluster_kernel<{'float' if precision == 32 else 'double'}>",
+            "call_kcycles": info.total_kcycles, "steps": info.matvecs,
+            "restarts": info.restarts,
+            "cycles_per_step": per(bar + red + a + b + c),
+            "per_step": {"spmv_and_first_dots": per(a), "second_projection": per(b),
+                         "norm_pass": per(c), "cluster_reductions": per(red),
+                         "barrier_waits": per(bar)},
+            "restart_eigensolve_cycles_per_restart":
+                round(1024.0 * info.eig_kcycles / max(info.restarts, 1)),
+            "note": "clock64 counters of CTA 0 (1 kcycle = 1024 cycles); the phases are "
+                    "latency chains (shared and distributed shared memory loads, FP64 "
+                    "reductions, one cluster barrier each), not DRAM streams"}
+
+
 def cpu_oracle_iterations(st, n, iters):
     """Oracle (NumPy FP64 restatement) outer iterations; returns (iterations, seconds)."""
     from oracle import usbs as ousbs
@@ -933,6 +964,12 @@ def main():
     # launch; the summary and command are kept with the profiles)
     lz_traffic = LANCZOS_CLUSTER_TRAFFIC_TORUS100 if on_cluster else None
     achieved = (lz_bytes / max(lz_n, 1)) / ((lz_ms / max(lz_n, 1)) * 1e-3) / 1e9 if lz_n else 0.0
+    step_chain = None
+    if on_cluster:
+        try:
+            step_chain = lanczos_step_chain(inst, st, n)
+        except Exception as exc:  # the main line is still reported
+            step_chain = {"error": str(exc)[:200]}
 
     # e2e: public API from pinned host buffers (problem layout + state in, result out)
     host = inst.problem.host
@@ -1071,6 +1108,7 @@ def main():
                          "launches": lz_n, "ms_per_launch": lz_ms / max(lz_n, 1),
                          "alg_bytes_per_launch": lz_bytes / max(lz_n, 1),
                          "traffic": lz_traffic,
+                         "step_chain": step_chain,
                          "note": "the cluster kernel keeps the basis, work vectors and operator "
                                  "in shared memory, so the algorithmic (streaming) bytes never "
                                  "reach DRAM; it is bound by the latency of its step chain"
