@@ -127,8 +127,8 @@ struct TeamBarrier {
   }
 };
 
-// ---- mbarrier + bulk async copies (cp.async.bulk, completion counted on an
-// mbarrier in shared memory).  Every wait is bounded by a globaltimer limit.
+// ---- mbarrier in shared memory with a wait bounded by a globaltimer limit
+// (run by the wait self-test).
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
 }
@@ -138,11 +138,6 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
 }
 __device__ __forceinline__ void mbar_init_fence() {
   asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-}
-__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
-  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-               "r"(bytes)
-               : "memory");
 }
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
   unsigned ok;
@@ -163,50 +158,6 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* bar, unsigned parity, uint64
     if (mbar_try_wait(bar, parity)) return true;
     if ((it & 63u) == 0 && globaltimer_ns() - t0 > limit_ns) return false;
   }
-}
-// L2 eviction-priority policies (createpolicy) and their use: streamed data is
-// marked evict_first so that it does not displace a small, re-read working set
-// (marked evict_last) from L2
-__device__ __forceinline__ uint64_t l2_evict_first_policy() {
-  uint64_t pol;
-  asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
-  return pol;
-}
-__device__ __forceinline__ uint64_t l2_evict_last_policy() {
-  uint64_t pol;
-  asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(pol));
-  return pol;
-}
-// global -> shared bulk copy of `bytes` (a multiple of 16, both addresses
-// 16-byte aligned) with an L2 policy, completion counted on `bar`
-__device__ __forceinline__ void bulk_g2s_hint(void* dst, const void* src, unsigned bytes,
-                                              uint64_t* bar, uint64_t pol) {
-  asm volatile(
-      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint "
-      "[%0], [%1], %2, [%3], %4;"
-      ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(pol)
-      : "memory");
-}
-// L1-bypassing load (data written by other CTAs) with an L2 cache policy
-__device__ __forceinline__ float ldcg_pol(const float* p, uint64_t pol) {
-  float v;
-  asm("ld.global.cg.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(p), "l"(pol));
-  return v;
-}
-__device__ __forceinline__ double ldcg_pol(const double* p, uint64_t pol) {
-  double v;
-  asm("ld.global.cg.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(p), "l"(pol));
-  return v;
-}
-
-// order earlier generic-proxy accesses of shared memory before later async copies
-__device__ __forceinline__ void fence_proxy_async_smem() {
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-}
-// this thread's earlier global stores ordered before later async-proxy (bulk
-// copy) reads of them, once the reader has synchronised with this thread
-__device__ __forceinline__ void fence_proxy_async_global() {
-  asm volatile("fence.proxy.async.global;" ::: "memory");
 }
 
 // splitmix64 (Vigna) and Box-Muller: the counter-based normal generator that the

@@ -1,13 +1,13 @@
 // Self-test of the library's bounded device waits.
 //
-// Every spin-wait in the Lanczos kernels (the cooperative team barrier and the
-// mbarrier waits of the bulk copies) gives up after a time limit, records
-// ST_BARRIER_TIMEOUT in the caller's status word and returns, so the context
-// stays usable.  usbs_selftest_wait_limits runs exactly those two waits on a
-// condition that nothing ever satisfies (a team barrier that expects one CTA
-// more than the launch has; an mbarrier that no thread or copy arrives at),
-// with a caller-chosen limit, so a test can see the timeout path end in the
-// status word instead of a hang.  The reference has no device code and no
+// Every spin-wait of the library (the Lanczos team kernel's cooperative
+// barrier, and the bounded mbarrier wait of common.cuh) gives up after a time
+// limit, records ST_BARRIER_TIMEOUT in the caller's status word and returns, so
+// the context stays usable.  usbs_selftest_wait_limits runs exactly those two
+// waits on a condition that nothing ever satisfies (a team barrier that expects
+// one CTA more than the launch has; an mbarrier that no thread or copy arrives
+// at), with a caller-chosen limit, so a test can see the timeout path end in
+// the status word instead of a hang.  The reference has no device code and no
 // counterpart.
 #include "../../include/usbs_gb300.h"
 #include "common.cuh"
